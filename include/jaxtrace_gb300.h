@@ -1,0 +1,307 @@
+/*
+ * jaxtrace_gb300.h -- C ABI of the GB300 Lagrangian-tracking library.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns 0 (JT_OK) or a negative JT_ERR_* code; the reason of the last
+ * failure on the calling thread is returned by jt_last_error().
+ *
+ * Ownership: every device buffer is allocated and owned by the caller.
+ * Pointers documented "device" must point to memory of the current CUDA
+ * device; pointers documented "host" to ordinary host memory.  `stream`
+ * is a cudaStream_t passed as void* (NULL = legacy default stream); all
+ * device work of a call is enqueued on it and the call does not
+ * synchronise unless stated.  Kernels report runtime anomalies through an
+ * optional device status word (bit flags JT_STATUS_*), never by trapping.
+ *
+ * Reference interfaces replaced (paths are inside the JAXTrace project):
+ *   jaxtrace/tracking/tracker.py      ParticleTracker.track_particles, lax.scan body
+ *   jaxtrace/integrators/rk4.py, rk2.py, euler.py   rk4_step / rk2_step / euler_step
+ *   jaxtrace/fields/time_series.py    TimeSeriesField time blend + nearest-node sampling
+ *   jaxtrace/fields/structured.py     StructuredGridSampler trilinear sampling
+ *   jaxtrace/fields/octree_fem_interpolator_optimized.py   octree build + P1 lookup
+ *   jaxtrace/tracking/boundary.py     periodic / reflective / clamping / absorbing /
+ *                                     mixed / continuous-inlet boundary callables
+ *   jaxtrace/density/kde.py, sph.py, neighbors.py          density passes
+ */
+#ifndef JAXTRACE_GB300_H
+#define JAXTRACE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JT_ABI_VERSION 1
+
+/* ---- return codes ------------------------------------------------------ */
+#define JT_OK 0
+#define JT_ERR_INVALID (-1)     /* bad argument: shape, size, enum, null   */
+#define JT_ERR_UNSUPPORTED (-2) /* combination not implemented             */
+#define JT_ERR_CUDA (-3)        /* a CUDA runtime call failed              */
+#define JT_ERR_NOMEM (-4)       /* caller-provided workspace too small     */
+#define JT_ERR_STATUS (-5)      /* device status word reported an error    */
+
+/* ---- device status bits (OR-ed by kernels into *status) --------------- */
+#define JT_STATUS_INDEX_WRAPPED 0x1 /* periodic cell index hit N (the reference raises IndexError there) */
+#define JT_STATUS_NONFINITE 0x2     /* a non-finite position was produced          */
+#define JT_STATUS_OCTREE_FALLBACK 0x4 /* at least one P1 lookup used the nearest-vertex fallback */
+
+/* ---- enums ------------------------------------------------------------- */
+/* snapshot value storage */
+#define JT_STORE_F32 0  /* float32 x,y,z                                   */
+#define JT_STORE_BF16 1 /* bfloat16 x,y,z with a per-snapshot float32 scale */
+#define JT_STORE_F16 2  /* float16  x,y,z with a per-snapshot float32 scale */
+
+/* grid sampler bounds handling: fields/structured.py:89 */
+#define JT_GRID_CLAMP 0
+#define JT_GRID_ZERO 1
+#define JT_GRID_NAN 2
+#define JT_GRID_PERIODIC 3
+
+/* time-blend forms (fields/time_series.py:326-367 and :155-245)
+ *   WEIGHTED : v = wa*A + wb*B                 (in-bounds linear, constant,
+ *                                               zero and nan extrapolation)
+ *   LERP_FWD : v = A + wb*(B - A)              (linear extrapolation left)
+ *   LERP_BWD : v = B + wb*(B - A)              (linear extrapolation right)
+ *   SAME_A   : v = wa*A + wb*A                 (both bracket indices equal:
+ *   SAME_B   : v = wa*B + wb*B                  a time that rounds onto an end)
+ * A and B are snapshots `pair` and `pair+1`; for 16-bit storage they are
+ * decoded as value*scale where sa/sb are the snapshots' scales (for the
+ * WEIGHTED and SAME forms the host folds the scales into wa/wb and sets
+ * sa=sb=1). */
+#define JT_BLEND_WEIGHTED 0
+#define JT_BLEND_LERP_FWD 1
+#define JT_BLEND_LERP_BWD 2
+#define JT_BLEND_SAME_A 3
+#define JT_BLEND_SAME_B 4
+
+typedef struct {
+    int32_t pair;
+    int32_t form;
+    float wa, wb;
+    float sa, sb;
+    int32_t pad0, pad1;
+} jt_blend; /* 32 bytes */
+
+/* integrators: integrators/euler.py:111, rk2.py:246, rk4.py:62 */
+#define JT_EULER 0
+#define JT_RK2 1
+#define JT_RK4 2
+
+/* per-axis box boundary kinds: tracking/boundary.py:101-210 */
+#define JT_BC_NONE 0
+#define JT_BC_PERIODIC 1
+#define JT_BC_REFLECTIVE 2
+#define JT_BC_CLAMP 3
+#define JT_BC_ABSORBING 4
+
+/* continuous-inlet replacement distributions: boundary.py:1444-1601 */
+#define JT_INLET_OFF 0
+#define JT_INLET_GRID 1
+
+/* arithmetic mode of the tracking kernels */
+#define JT_ARITH_EXACT 0       /* float32, round-to-nearest, no contraction:
+                                  bit-identical to the NumPy reference path */
+#define JT_ARITH_COMPENSATED 1 /* float32 with FMA and Kahan-compensated
+                                  position accumulation                     */
+
+/* ---- field descriptors ------------------------------------------------- */
+
+/* Regular grid field: StructuredGridSampler (fields/structured.py:65) whose
+ * node values come from a time series of snapshots (time_series.py:82).
+ * Node (i,j,k) of an (nx,ny,nz) grid has index (i*ny + j)*nz + k, the
+ * reference's ij layout.  Values are stored as snapshot PAIRS: record n of
+ * pair p holds snapshot p and p+1 of node n side by side:
+ *   F32 : 8 floats  {Ax,Ay,Az,Bx, By,Bz,0,0}        (32 B, one sector)
+ *   BF16/F16: 8 halves {Ax,Ay,Az,Bx,By,Bz,0,0}      (16 B)
+ * so one aligned load returns both bracketing snapshots of a node. */
+typedef struct {
+    int32_t nx, ny, nz;
+    int32_t bounds_mode;   /* JT_GRID_*                                       */
+    float origin[3];       /* grid_x[0], grid_y[0], grid_z[0]                 */
+    float spacing[3];      /* float32(grid[1]-grid[0]), 1 when n == 1         */
+    float valid_hi[3];     /* float32(min + (n-1)*d), the zero/nan validity edge */
+    int32_t storage;       /* JT_STORE_*                                      */
+    int32_t n_pairs;       /* number of snapshot pairs (>= 1)                  */
+    int64_t pair_stride;   /* records per pair (= nx*ny*nz)                    */
+    const void* pairs;     /* device                                          */
+} jt_grid_field;
+
+/* Tetrahedral mesh field with the octree point location of
+ * fields/octree_fem_interpolator_optimized.py.  Arrays are produced by
+ * jt_octree_build and uploaded by the caller. */
+typedef struct {
+    float cx, cy, cz;      /* float32 (min+max)/2 of the node box             */
+    int32_t is_leaf;
+    int32_t children[8];   /* -1 where the octant is empty                    */
+    int32_t elem_offset;   /* into the element list                            */
+    int32_t elem_count;
+    int32_t pad0, pad1;
+} jt_octree_node; /* 64 bytes */
+
+typedef struct {
+    int32_t n_points, n_tets;
+    int32_t n_nodes;        /* octree nodes                                   */
+    int32_t max_depth;      /* traversal iterations (reference default 12)   */
+    int32_t storage;        /* JT_STORE_* of the node values                  */
+    int32_t n_pairs;
+    int64_t pair_stride;    /* records per pair (= n_points)                  */
+    const float* points;    /* device (n_points,4): x,y,z,0                   */
+    const float* tet_box;   /* device (n_tets,8): min xyz,0, max xyz,0        */
+    const float* tet_geom;  /* device (n_tets,16): v0, v1-v0, v2-v0, v3-v0 (xyz each), conn as int32 bits */
+    const jt_octree_node* nodes; /* device (n_nodes)                        */
+    const int32_t* elems;   /* device element lists                           */
+    const void* pairs;      /* device value pairs, layout as jt_grid_field   */
+} jt_mesh_field;
+
+/* Nearest-node field: TimeSeriesField spatial sampling (time_series.py:391)
+ * over scattered nodes, accelerated by a uniform cell list. */
+typedef struct {
+    int32_t n_points;
+    int32_t cells[3];       /* cell-list resolution                          */
+    float origin[3];
+    float inv_cell[3];
+    int32_t storage;
+    int32_t n_pairs;
+    int64_t pair_stride;    /* = n_points                                     */
+    const float* points;    /* device (n_points,4) sorted by cell            */
+    const int32_t* point_ids; /* device (n_points) original node index of sorted slot */
+    const int32_t* cell_start; /* device (cells+1) CSR offsets                 */
+    const void* pairs;      /* device value pairs indexed by ORIGINAL node id */
+} jt_nearest_field;
+
+#define JT_FIELD_GRID 1
+#define JT_FIELD_MESH 2
+#define JT_FIELD_NEAREST 3
+
+typedef struct {
+    int32_t kind;           /* JT_FIELD_*                                     */
+    int32_t pad;
+    const jt_grid_field* grid;
+    const jt_mesh_field* mesh;
+    const jt_nearest_field* nearest;
+} jt_field;
+
+/* ---- boundary descriptor ------------------------------------------------ */
+typedef struct {
+    int32_t axis_kind[3];   /* JT_BC_* per axis                               */
+    int32_t absorbing_joint;/* 1: absorbing_boundary_factory semantics -- a
+                               particle outside on any axis gets outside_value
+                               on all three (boundary.py:175-210)           */
+    float lo[3], hi[3];     /* per-axis bounds                                */
+    float outside_value;
+    /* continuous inlet, boundary.py:1517-1599 (replaces axis_kind when on)  */
+    int32_t inlet_mode;     /* JT_INLET_*                                     */
+    int32_t inlet_axis;     /* 0,1,2                                          */
+    int32_t inlet_positive; /* 1: flow toward max, 0: toward min              */
+    int32_t inlet_res[2];   /* lattice sizes of the two other axes (ascending axis order) */
+    float inlet_nudge;      /* float32 axis_min + 0.001f*(axis_max-axis_min) (or mirror) */
+    const float* inlet_coords[2]; /* device float32 linspace lattices         */
+} jt_boundary;
+
+/* ---- tracking ---------------------------------------------------------- */
+typedef struct {
+    int32_t integrator;     /* JT_EULER / JT_RK2 / JT_RK4                     */
+    int32_t arith;          /* JT_ARITH_*                                     */
+    int32_t n_particles;
+    int32_t step_begin;     /* global index of the first step of this launch  */
+    int32_t step_end;       /* one past the last                              */
+    float dt;               /* float32 dt                                     */
+    float dt_half;          /* float32 0.5*dt                                 */
+    float dt_sixth;         /* float32 dt/6                                   */
+    const jt_blend* schedule;  /* device, 4 entries per step s:
+                                  [4s+0] time of stage 1 (t_s),
+                                  [4s+1] t_s + dt/2 (RK2 / RK4 mid stages),
+                                  [4s+2] t_s + dt   (RK4 last stage),
+                                  [4s+3] times[s+1] (velocity recording)     */
+    int64_t schedule_stride;/* entries between ensembles (0: one schedule)    */
+    const int32_t* ens_offsets; /* device (n_ens+1) particle offsets or NULL:
+                                   particles [ens_offsets[e], ens_offsets[e+1])
+                                   use schedule + e*schedule_stride        */
+    int32_t n_ens;
+    int32_t pad_e;
+    float* pos;             /* device (N,3) in/out                            */
+    float* comp;            /* device (N,3) Kahan compensation (COMPENSATED) or NULL */
+    float* traj;            /* device (rows,N,3) or NULL                      */
+    float* vel;             /* device (rows,N,3) or NULL (record_velocities)  */
+    int32_t record_every;   /* step count c=s+1 is recorded when c % record_every == 0 */
+    int32_t record_compact; /* row = c/record_every (1) or row = c (0)       */
+    int32_t row_base;       /* row of traj[0] for this launch                 */
+    int32_t n_rows;         /* rows held by traj/vel for this launch          */
+    int32_t* status;        /* device status word or NULL                     */
+    int32_t pad;
+} jt_track_params;
+
+/* ABI / diagnostics */
+int jt_abi_version(void);
+const char* jt_last_error(void);
+/* sizes of the public structs, in the order: jt_blend, jt_grid_field,
+ * jt_octree_node, jt_mesh_field, jt_nearest_field, jt_field, jt_boundary,
+ * jt_track_params.  Lets a binding check its mirror of the layouts.        */
+int jt_struct_sizes(int64_t* out, int32_t n);
+
+/* Advance particles through steps [step_begin, step_end) of the schedule,
+ * fusing integrator stages, field evaluation and boundary into one kernel
+ * with the time loop held in registers.  Replaces the lax.scan body
+ * tracker.py:236-242 (and the step loop :441-446), rk4.py:62-106,
+ * rk2.py:246-309, euler.py:111-157 and the boundary callables. */
+int jt_track(const jt_field* field, const jt_boundary* bc,
+             const jt_track_params* params, void* stream);
+
+/* Evaluate a field at M positions with one blend entry: the
+ * sample_at_positions(positions, t) protocol (fields/base.py:106-122,
+ * time_series.py:391, structured.py:258, octree_fem_time_series_optimized.py:87).
+ * pos, out: device (M,3) float32. */
+int jt_field_sample(const jt_field* field, const jt_blend* blend, int32_t arith,
+                    const float* pos, float* out, int32_t m,
+                    int32_t* status, void* stream);
+
+/* Apply a boundary in place to (N,3) device positions: the callables
+ * returned by periodic_boundary / reflective_boundary / clamping_boundary /
+ * absorbing_boundary_factory / mixed_boundary /
+ * continuous_inlet_boundary_factory (boundary.py:215-438, :1444-1601). */
+int jt_boundary_apply(const jt_boundary* bc, float* pos, int32_t n, void* stream);
+
+/* One integrator step without boundary: rk4_step / rk2_step / euler_step
+ * (x, t, dt, field_fn) with a scalar or per-particle dt.  stage blends: the
+ * three entries of jt_track_params.schedule for this step (host memory,
+ * copied by value).  dt_per_particle: device (N) float32 or NULL. */
+int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
+                       int32_t integrator, int32_t arith, float dt,
+                       const float* dt_per_particle, const float* x_in,
+                       float* x_out, int32_t n, int32_t* status, void* stream);
+
+/* ---- octree build (host) ------------------------------------------------ */
+typedef struct {
+    int32_t n_nodes;         /* octree nodes                                   */
+    int32_t n_elem_entries;  /* length of the concatenated leaf element lists  */
+    int32_t max_elems;       /* longest list (the reference's padded width)    */
+    int32_t max_tree_depth;  /* deepest node                                   */
+    int32_t n_leaves;
+    int32_t pad;
+} jt_octree_info;
+
+/* Build the octree of a tetrahedral mesh on the host: replaces
+ * build_octree_mesh_optimized (fields/octree_fem_interpolator_optimized.py:41-215)
+ * with identical node numbering, octant assignment and leaf rule.
+ * points: host (n_points,3) float32; conn: host (n_tets,4) int32.
+ * On success *handle_out owns the result until jt_octree_free. */
+int jt_octree_build(const float* points, int32_t n_points, const int32_t* conn, int32_t n_tets,
+                    int32_t max_elements_per_leaf, int32_t max_depth, void** handle_out,
+                    jt_octree_info* info);
+
+/* Copy a built octree into caller host buffers (any may be NULL):
+ * nodes (n_nodes) [pad0 holds the node depth], elems (n_elem_entries),
+ * tet_box (n_tets,8), tet_geom (n_tets,16), node_bounds (n_nodes,6 = min xyz,
+ * max xyz; the reference's nodes_min/nodes_max). */
+int jt_octree_fetch(void* handle, jt_octree_node* nodes, int32_t* elems, float* tet_box,
+                    float* tet_geom, float* node_bounds);
+
+void jt_octree_free(void* handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JAXTRACE_GB300_H */

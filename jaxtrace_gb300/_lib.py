@@ -1,0 +1,176 @@
+"""ctypes binding of ``libjaxtrace_gb300.so`` (the C ABI in include/jaxtrace_gb300.h).
+
+The library is required: there is no CPU fallback.  Importing this module
+never needs a GPU; calls that launch kernels need a CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+i32, i64, f32, vp = C.c_int32, C.c_int64, C.c_float, C.c_void_p
+
+# ---- constants (mirror of the header) ------------------------------------
+JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STATUS = 0, -1, -2, -3, -4, -5
+JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
+JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2
+JT_GRID_CLAMP, JT_GRID_ZERO, JT_GRID_NAN, JT_GRID_PERIODIC = 0, 1, 2, 3
+JT_BLEND_WEIGHTED, JT_BLEND_LERP_FWD, JT_BLEND_LERP_BWD, JT_BLEND_SAME_A, JT_BLEND_SAME_B = 0, 1, 2, 3, 4
+JT_EULER, JT_RK2, JT_RK4 = 0, 1, 2
+JT_BC_NONE, JT_BC_PERIODIC, JT_BC_REFLECTIVE, JT_BC_CLAMP, JT_BC_ABSORBING = 0, 1, 2, 3, 4
+JT_INLET_OFF, JT_INLET_GRID = 0, 1
+JT_ARITH_EXACT, JT_ARITH_COMPENSATED = 0, 1
+JT_FIELD_GRID, JT_FIELD_MESH, JT_FIELD_NEAREST = 1, 2, 3
+
+STORAGE_CODES = {"f32": JT_STORE_F32, "float32": JT_STORE_F32, "bf16": JT_STORE_BF16,
+                 "bfloat16": JT_STORE_BF16, "f16": JT_STORE_F16, "float16": JT_STORE_F16}
+
+
+# ---- struct mirrors --------------------------------------------------------
+class Blend(C.Structure):
+    _fields_ = [("pair", i32), ("form", i32), ("wa", f32), ("wb", f32), ("sa", f32), ("sb", f32),
+                ("pad0", i32), ("pad1", i32)]
+
+
+BLEND_DTYPE = np.dtype([("pair", "<i4"), ("form", "<i4"), ("wa", "<f4"), ("wb", "<f4"),
+                        ("sa", "<f4"), ("sb", "<f4"), ("pad0", "<i4"), ("pad1", "<i4")])
+
+
+class GridField(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("bounds_mode", i32),
+                ("origin", f32 * 3), ("spacing", f32 * 3), ("valid_hi", f32 * 3),
+                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64), ("pairs", vp)]
+
+
+class OctreeNode(C.Structure):
+    _fields_ = [("cx", f32), ("cy", f32), ("cz", f32), ("is_leaf", i32), ("children", i32 * 8),
+                ("elem_offset", i32), ("elem_count", i32), ("pad0", i32), ("pad1", i32)]
+
+
+OCTREE_NODE_DTYPE = np.dtype([("c", "<f4", (3,)), ("is_leaf", "<i4"), ("children", "<i4", (8,)),
+                              ("elem_offset", "<i4"), ("elem_count", "<i4"), ("pad", "<i4", (2,))])
+
+
+class MeshField(C.Structure):
+    _fields_ = [("n_points", i32), ("n_tets", i32), ("n_nodes", i32), ("max_depth", i32),
+                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64),
+                ("points", vp), ("tet_box", vp), ("tet_geom", vp), ("nodes", vp), ("elems", vp),
+                ("pairs", vp)]
+
+
+class NearestField(C.Structure):
+    _fields_ = [("n_points", i32), ("cells", i32 * 3), ("origin", f32 * 3), ("inv_cell", f32 * 3),
+                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64),
+                ("points", vp), ("point_ids", vp), ("cell_start", vp), ("pairs", vp)]
+
+
+class Field(C.Structure):
+    _fields_ = [("kind", i32), ("pad", i32), ("grid", C.POINTER(GridField)),
+                ("mesh", C.POINTER(MeshField)), ("nearest", C.POINTER(NearestField))]
+
+
+class Boundary(C.Structure):
+    _fields_ = [("axis_kind", i32 * 3), ("absorbing_joint", i32), ("lo", f32 * 3), ("hi", f32 * 3),
+                ("outside_value", f32), ("inlet_mode", i32), ("inlet_axis", i32),
+                ("inlet_positive", i32), ("inlet_res", i32 * 2), ("inlet_nudge", f32),
+                ("inlet_coords", vp * 2)]
+
+
+class TrackParams(C.Structure):
+    _fields_ = [("integrator", i32), ("arith", i32), ("n_particles", i32), ("step_begin", i32),
+                ("step_end", i32), ("dt", f32), ("dt_half", f32), ("dt_sixth", f32),
+                ("schedule", vp), ("schedule_stride", i64), ("ens_offsets", vp), ("n_ens", i32),
+                ("pad_e", i32), ("pos", vp), ("comp", vp), ("traj", vp), ("vel", vp),
+                ("record_every", i32), ("record_compact", i32), ("row_base", i32), ("n_rows", i32),
+                ("status", vp), ("pad", i32)]
+
+
+class OctreeInfo(C.Structure):
+    _fields_ = [("n_nodes", i32), ("n_elem_entries", i32), ("max_elems", i32), ("max_tree_depth", i32),
+                ("n_leaves", i32), ("pad", i32)]
+
+
+STRUCTS = [Blend, GridField, OctreeNode, MeshField, NearestField, Field, Boundary, TrackParams]
+
+
+class JTError(RuntimeError):
+    """A device-side failure reported by the native library."""
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load the native library (building it in-tree on first use)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        if not build_if_missing or os.environ.get("JAXTRACE_GB300_NO_BUILD"):
+            raise ImportError(f"native library {path} is missing; run jaxtrace_gb300._build.build()")
+        _build.build()
+    lib = C.CDLL(str(path))
+    P = C.POINTER
+    sig = {
+        "jt_abi_version": (i32, []),
+        "jt_last_error": (C.c_char_p, []),
+        "jt_struct_sizes": (i32, [P(i64), i32]),
+        "jt_track": (i32, [P(Field), P(Boundary), P(TrackParams), vp]),
+        "jt_field_sample": (i32, [P(Field), P(Blend), i32, vp, vp, i32, vp, vp]),
+        "jt_boundary_apply": (i32, [P(Boundary), vp, i32, vp]),
+        "jt_integrator_step": (i32, [P(Field), P(Blend), i32, i32, f32, vp, vp, vp, i32, vp, vp]),
+        "jt_octree_build": (i32, [vp, i32, vp, i32, i32, i32, P(vp), P(OctreeInfo)]),
+        "jt_octree_fetch": (i32, [vp, vp, vp, vp, vp, vp]),
+        "jt_octree_free": (None, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.jt_abi_version() != 1:
+        raise ImportError("jaxtrace_gb300 native library ABI mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> int:
+    """Map a JT_* return code to the reference's exception types."""
+    if rc >= 0:
+        return rc
+    msg = load().jt_last_error().decode(errors="replace")
+    if rc == JT_ERR_INVALID:
+        raise ValueError(msg)
+    if rc == JT_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if rc == JT_ERR_NOMEM:
+        raise MemoryError(msg)
+    raise JTError(msg)
+
+
+def struct_sizes() -> list[int]:
+    out = (i64 * 16)()
+    n = check(load().jt_struct_sizes(out, 16))
+    return [int(out[i]) for i in range(n)]
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def ptr(t) -> C.c_void_p:
+    """Device pointer of a torch tensor (or None)."""
+    if t is None:
+        return C.c_void_p(None)
+    return C.c_void_p(t.data_ptr())

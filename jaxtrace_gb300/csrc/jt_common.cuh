@@ -1,0 +1,392 @@
+// Shared device code of the tracking kernels: float32 arithmetic policies,
+// NumPy-compatible remainder, time-blend decoding, boundary conditions and
+// the fused integrator step.  Every formula names the reference expression
+// (path:line inside the JAXTrace project) whose float32 rounding it follows.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/jaxtrace_gb300.h"
+
+namespace jt {
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies.  Exact: every operation rounded to nearest on its own,
+// never contracted into an FMA -- the order and rounding of NumPy float32
+// array expressions.  Fast: the compiler may contract, and lerps use FMA.
+// ---------------------------------------------------------------------------
+template <bool EXACT>
+struct Ar;
+
+template <>
+struct Ar<true> {
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    // a*wa + b*wb, both products rounded before the sum
+    static __device__ __forceinline__ float dot2(float a, float wa, float b, float wb) {
+        return __fadd_rn(__fmul_rn(a, wa), __fmul_rn(b, wb));
+    }
+    // a + w*b with the product rounded
+    static __device__ __forceinline__ float axpy(float a, float w, float b) {
+        return __fadd_rn(a, __fmul_rn(w, b));
+    }
+};
+
+template <>
+struct Ar<false> {
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float dot2(float a, float wa, float b, float wb) {
+        return fmaf(a, wa, b * wb);
+    }
+    static __device__ __forceinline__ float axpy(float a, float w, float b) { return fmaf(w, b, a); }
+};
+
+// NumPy float32 remainder (np.mod / jnp.mod): fmod, then move the result to
+// the sign of the divisor (Python convention).  fmodf is exact; the one add
+// is rounded, so the result may equal b itself (e.g. a = -1e-9, b = 32).
+__device__ __forceinline__ float np_mod(float a, float b) {
+    if (a >= 0.0f && a < b) return a;  // fmod(a,b) == a exactly on this range
+    float m = fmodf(a, b);
+    if (m != 0.0f) {
+        if ((b < 0.0f) != (m < 0.0f)) m = __fadd_rn(m, b);
+    } else {
+        m = copysignf(0.0f, b);
+    }
+    return m;
+}
+
+// np.clip(x, lo, hi) for float32: NaN propagates.
+__device__ __forceinline__ float np_clip(float x, float lo, float hi) {
+    x = (x < lo) ? lo : x;
+    x = (x > hi) ? hi : x;
+    return x;
+}
+
+struct V3 {
+    float x, y, z;
+};
+
+// ---------------------------------------------------------------------------
+// Snapshot-pair records.
+// ---------------------------------------------------------------------------
+struct PairVal {
+    float ax, ay, az, bx, by, bz;
+};
+
+template <int STORE>
+__device__ __forceinline__ PairVal load_pair(const void* base, int64_t rec);
+
+template <>
+__device__ __forceinline__ PairVal load_pair<JT_STORE_F32>(const void* base, int64_t rec) {
+    const float4* p = reinterpret_cast<const float4*>(base) + 2 * rec;
+    float4 lo = __ldg(p);
+    float2 hi = __ldg(reinterpret_cast<const float2*>(p + 1));
+    return PairVal{lo.x, lo.y, lo.z, lo.w, hi.x, hi.y};
+}
+
+template <>
+__device__ __forceinline__ PairVal load_pair<JT_STORE_BF16>(const void* base, int64_t rec) {
+    uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
+    __nv_bfloat162 h0 = *reinterpret_cast<__nv_bfloat162*>(&r.x);
+    __nv_bfloat162 h1 = *reinterpret_cast<__nv_bfloat162*>(&r.y);
+    __nv_bfloat162 h2 = *reinterpret_cast<__nv_bfloat162*>(&r.z);
+    float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1), f2 = __bfloat1622float2(h2);
+    return PairVal{f0.x, f0.y, f1.x, f1.y, f2.x, f2.y};
+}
+
+template <>
+__device__ __forceinline__ PairVal load_pair<JT_STORE_F16>(const void* base, int64_t rec) {
+    uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
+    __half2 h0 = *reinterpret_cast<__half2*>(&r.x);
+    __half2 h1 = *reinterpret_cast<__half2*>(&r.y);
+    __half2 h2 = *reinterpret_cast<__half2*>(&r.z);
+    float2 f0 = __half22float2(h0), f1 = __half22float2(h1), f2 = __half22float2(h2);
+    return PairVal{f0.x, f0.y, f1.x, f1.y, f2.x, f2.y};
+}
+
+// Blend of one snapshot pair at the time the schedule entry describes:
+// time_series.py:367  ((1-alpha)*V[il] + alpha*V[ir]).astype(float32)
+// time_series.py:336  V0 + alpha*(V1-V0)        (linear extrapolation, left)
+// time_series.py:352  V1 + alpha*(V1-V0)        (linear extrapolation, right)
+template <bool EXACT, int STORE>
+__device__ __forceinline__ V3 blend(const PairVal& p, const jt_blend& e) {
+    typedef Ar<EXACT> A;
+    if (e.form == JT_BLEND_WEIGHTED) {
+        return V3{A::dot2(p.ax, e.wa, p.bx, e.wb), A::dot2(p.ay, e.wa, p.by, e.wb),
+                  A::dot2(p.az, e.wa, p.bz, e.wb)};
+    }
+    if (e.form == JT_BLEND_SAME_A) {
+        return V3{A::dot2(p.ax, e.wa, p.ax, e.wb), A::dot2(p.ay, e.wa, p.ay, e.wb),
+                  A::dot2(p.az, e.wa, p.az, e.wb)};
+    }
+    if (e.form == JT_BLEND_SAME_B) {
+        return V3{A::dot2(p.bx, e.wa, p.bx, e.wb), A::dot2(p.by, e.wa, p.by, e.wb),
+                  A::dot2(p.bz, e.wa, p.bz, e.wb)};
+    }
+    float ax = p.ax, ay = p.ay, az = p.az, bx = p.bx, by = p.by, bz = p.bz;
+    if (STORE != JT_STORE_F32) {
+        ax = A::mul(ax, e.sa); ay = A::mul(ay, e.sa); az = A::mul(az, e.sa);
+        bx = A::mul(bx, e.sb); by = A::mul(by, e.sb); bz = A::mul(bz, e.sb);
+    }
+    if (e.form == JT_BLEND_LERP_FWD) {
+        return V3{A::axpy(ax, e.wb, A::sub(bx, ax)), A::axpy(ay, e.wb, A::sub(by, ay)),
+                  A::axpy(az, e.wb, A::sub(bz, az))};
+    }
+    return V3{A::axpy(bx, e.wb, A::sub(bx, ax)), A::axpy(by, e.wb, A::sub(by, ay)),
+              A::axpy(bz, e.wb, A::sub(bz, az))};
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions (tracking/boundary.py), float32 as the NumPy path.
+// ---------------------------------------------------------------------------
+template <bool EXACT>
+__device__ __forceinline__ float bc_axis(int kind, float x, float lo, float hi, float outside) {
+    typedef Ar<EXACT> A;
+    switch (kind) {
+        case JT_BC_PERIODIC: {
+            // boundary.py:118-123  lo + mod(x - lo, where(width>0, width, 1))
+            float width = A::sub(hi, lo);
+            width = width > 0.0f ? width : 0.0f;
+            float ws = width > 0.0f ? width : 1.0f;
+            return A::add(lo, np_mod(A::sub(x, lo), ws));
+        }
+        case JT_BC_REFLECTIVE: {
+            // boundary.py:165-172  sawtooth fold with period 2*width
+            float width = A::sub(hi, lo);
+            width = width > 0.0f ? width : 0.0f;
+            float ws = width > 0.0f ? width : 1.0f;
+            float y = np_mod(A::sub(x, lo), A::mul(2.0f, ws));
+            float yr = (y <= width) ? y : A::sub(A::mul(2.0f, width), y);
+            return A::add(lo, yr);
+        }
+        case JT_BC_CLAMP:
+            // boundary.py:143  clip(x, lo, hi)
+            return np_clip(x, lo, hi);
+        case JT_BC_ABSORBING:
+            // boundary.py:198-208 on one axis (mixed_boundary, :415)
+            return (x < lo || x > hi) ? outside : x;
+        default:
+            return x;
+    }
+}
+
+// Nearest lattice coordinate: argmin(|coords - c|) with ties to the lower
+// index (boundary.py:1309).  The lattice is ascending, so |fl(g[j]-c)| falls
+// then rises; start from the bracketing pair and walk left over ties.
+__device__ __forceinline__ float nearest_lattice(const float* g, int n, float c) {
+    if (n <= 1) return __ldg(g);
+    if (c != c) return __ldg(g);  // all distances NaN: argmin returns 0
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(g + mid) < c) lo = mid + 1; else hi = mid;
+    }
+    int best;
+    if (lo == 0) {
+        best = 0;
+    } else if (lo == n) {
+        best = n - 1;
+    } else {
+        float dl = fabsf(__fsub_rn(__ldg(g + lo - 1), c));
+        float dr = fabsf(__fsub_rn(__ldg(g + lo), c));
+        best = (dr < dl) ? lo : lo - 1;
+    }
+    float db = fabsf(__fsub_rn(__ldg(g + best), c));
+    while (best > 0) {
+        float d = fabsf(__fsub_rn(__ldg(g + best - 1), c));
+        if (!(d <= db)) break;
+        db = d;
+        --best;
+    }
+    return __ldg(g + best);
+}
+
+// Continuous inlet with grid-preserving replacement (boundary.py:1517-1599).
+template <bool EXACT>
+__device__ __forceinline__ void bc_inlet(const jt_boundary& B, float* r) {
+    typedef Ar<EXACT> A;
+    const int a = B.inlet_axis;
+    const int o0 = (a == 0) ? 1 : 0;
+    const int o1 = (a == 2) ? 1 : 2;
+    const float amin = B.lo[a], amax = B.hi[a];
+    bool exited = B.inlet_positive ? (r[a] > amax) : (r[a] < amin);
+    if (exited && B.inlet_mode == JT_INLET_GRID) {
+        float g0 = nearest_lattice(B.inlet_coords[0], B.inlet_res[0], r[o0]);
+        float g1 = nearest_lattice(B.inlet_coords[1], B.inlet_res[1], r[o1]);
+        r[a] = B.inlet_positive ? amin : amax;
+        r[o0] = g0;
+        r[o1] = g1;
+    }
+    // boundary.py:1580-1587  backward crossings are nudged inside
+    if (B.inlet_positive) {
+        if (r[a] < amin) r[a] = B.inlet_nudge;
+    } else {
+        if (r[a] > amax) r[a] = B.inlet_nudge;
+    }
+    // boundary.py:1590-1597  one mirror on the other axes
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int o = q == 0 ? o0 : o1;
+        const float lo = B.lo[o], hi = B.hi[o];
+        float v = r[o];
+        if (v < lo) v = A::sub(A::mul(2.0f, lo), v);
+        else if (v > hi) v = A::sub(A::mul(2.0f, hi), v);
+        r[o] = v;
+    }
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void apply_boundary(const jt_boundary& B, float& x, float& y, float& z) {
+    if (B.inlet_mode != JT_INLET_OFF) {
+        float r[3] = {x, y, z};
+        bc_inlet<EXACT>(B, r);
+        x = r[0]; y = r[1]; z = r[2];
+        return;
+    }
+    if (B.absorbing_joint) {
+        // boundary.py:198-208: any coordinate outside marks the whole particle
+        bool out = x < B.lo[0] || y < B.lo[1] || z < B.lo[2] || x > B.hi[0] || y > B.hi[1] ||
+                   z > B.hi[2];
+        if (out) { x = B.outside_value; y = B.outside_value; z = B.outside_value; }
+        return;
+    }
+    x = bc_axis<EXACT>(B.axis_kind[0], x, B.lo[0], B.hi[0], B.outside_value);
+    y = bc_axis<EXACT>(B.axis_kind[1], y, B.lo[1], B.hi[1], B.outside_value);
+    z = bc_axis<EXACT>(B.axis_kind[2], z, B.lo[2], B.hi[2], B.outside_value);
+}
+
+// ---------------------------------------------------------------------------
+// One integrator step, generic over the field evaluator.
+//   RK4  rk4.py:82-106   k1..k4, x + (dt/6)*(((k1 + 2k2) + 2k3) + k4)
+//   RK2  rk2.py:283-309  x + dt * v(x + dt/2 * v(x, t), t_mid)
+//   Euler euler.py:146-157  x + dt * v(x, t)
+// `s` points at the step's schedule entries (stage 0, mid, full).
+// Compensated mode keeps a Kahan term c per coordinate for the final update.
+// ---------------------------------------------------------------------------
+struct StepConst {
+    float dt, dth, dt6;
+};
+
+template <bool EXACT, int INTEG, bool COMP, class Field>
+__device__ __forceinline__ void integrate(const Field& f, const jt_blend* s, const StepConst& k,
+                                          V3& x, V3& c, int& flags) {
+    typedef Ar<EXACT> A;
+    V3 inc;  // the increment added to x
+    if (INTEG == JT_RK4) {
+        const jt_blend e0 = s[0], e1 = s[1], e2 = s[2];
+        V3 k1 = f(x, e0, flags);
+        V3 x2{A::axpy(x.x, k.dth, k1.x), A::axpy(x.y, k.dth, k1.y), A::axpy(x.z, k.dth, k1.z)};
+        V3 k2 = f(x2, e1, flags);
+        V3 x3{A::axpy(x.x, k.dth, k2.x), A::axpy(x.y, k.dth, k2.y), A::axpy(x.z, k.dth, k2.z)};
+        V3 k3 = f(x3, e1, flags);
+        V3 x4{A::axpy(x.x, k.dt, k3.x), A::axpy(x.y, k.dt, k3.y), A::axpy(x.z, k.dt, k3.z)};
+        V3 k4 = f(x4, e2, flags);
+        V3 sm{A::add(A::add(A::add(k1.x, A::mul(2.0f, k2.x)), A::mul(2.0f, k3.x)), k4.x),
+              A::add(A::add(A::add(k1.y, A::mul(2.0f, k2.y)), A::mul(2.0f, k3.y)), k4.y),
+              A::add(A::add(A::add(k1.z, A::mul(2.0f, k2.z)), A::mul(2.0f, k3.z)), k4.z)};
+        inc = V3{A::mul(k.dt6, sm.x), A::mul(k.dt6, sm.y), A::mul(k.dt6, sm.z)};
+    } else if (INTEG == JT_RK2) {
+        const jt_blend e0 = s[0], e1 = s[1];
+        V3 v1 = f(x, e0, flags);
+        V3 xm{A::axpy(x.x, k.dth, v1.x), A::axpy(x.y, k.dth, v1.y), A::axpy(x.z, k.dth, v1.z)};
+        V3 v2 = f(xm, e1, flags);
+        inc = V3{A::mul(k.dt, v2.x), A::mul(k.dt, v2.y), A::mul(k.dt, v2.z)};
+    } else {
+        const jt_blend e0 = s[0];
+        V3 v = f(x, e0, flags);
+        inc = V3{A::mul(k.dt, v.x), A::mul(k.dt, v.y), A::mul(k.dt, v.z)};
+    }
+    if (COMP) {
+        // Kahan (1965) compensated summation of the position increments.
+        float yx = inc.x - c.x, yy = inc.y - c.y, yz = inc.z - c.z;
+        float tx = x.x + yx, ty = x.y + yy, tz = x.z + yz;
+        c.x = __fsub_rn(__fsub_rn(tx, x.x), yx);
+        c.y = __fsub_rn(__fsub_rn(ty, x.y), yy);
+        c.z = __fsub_rn(__fsub_rn(tz, x.z), yz);
+        x = V3{tx, ty, tz};
+    } else {
+        x = V3{A::add(x.x, inc.x), A::add(x.y, inc.y), A::add(x.z, inc.z)};
+    }
+}
+
+// OR the per-thread status flags into the device status word, one atomic
+// per warp.
+__device__ __forceinline__ void report_flags(int32_t* status, int flags) {
+    if (status == nullptr) return;
+    const unsigned m = __activemask();
+    const int f = __reduce_or_sync(m, flags);
+    if (f != 0 && (threadIdx.x & 31) == (__ffs(m) - 1)) atomicOr(status, f);
+}
+
+// Ensemble of particle i: largest e with offsets[e] <= i.
+__device__ __forceinline__ int find_ensemble(const int32_t* off, int n_ens, int i) {
+    int lo = 0, hi = n_ens - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent tracking kernel body: one particle per thread, the time loop in
+// registers, boundary fused after every step, optional strided recording.
+template <bool EXACT, int INTEG, class Field>
+__device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
+                                           const jt_track_params& P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n_particles) return;
+    const bool comp = (P.arith == JT_ARITH_COMPENSATED) && P.comp != nullptr;
+    const jt_blend* sched = P.schedule;
+    if (P.ens_offsets != nullptr && P.n_ens > 0) {
+        sched += (int64_t)find_ensemble(P.ens_offsets, P.n_ens, i) * P.schedule_stride;
+    }
+    float* pp = P.pos + 3 * (int64_t)i;
+    V3 x{pp[0], pp[1], pp[2]};
+    V3 c{0.f, 0.f, 0.f};
+    if (comp) {
+        const float* cp = P.comp + 3 * (int64_t)i;
+        c = V3{cp[0], cp[1], cp[2]};
+    }
+    const StepConst k{P.dt, P.dt_half, P.dt_sixth};
+    int flags = 0;
+    const int64_t n = P.n_particles;
+    for (int s = P.step_begin; s < P.step_end; ++s) {
+        const jt_blend* e = sched + 4 * (int64_t)s;
+        if (comp) integrate<EXACT, INTEG, true>(f, e, k, x, c, flags);
+        else integrate<EXACT, INTEG, false>(f, e, k, x, c, flags);
+        apply_boundary<EXACT>(B, x.x, x.y, x.z);
+        if (P.traj != nullptr) {
+            const int cnt = s + 1;
+            if (cnt % P.record_every == 0) {
+                const int row = (P.record_compact ? cnt / P.record_every : cnt) - P.row_base;
+                if (row >= 0 && row < P.n_rows) {
+                    float* o = P.traj + ((int64_t)row * n + i) * 3;
+                    o[0] = x.x; o[1] = x.y; o[2] = x.z;
+                    if (P.vel != nullptr) {
+                        const jt_blend er = e[3];
+                        V3 v = f(x, er, flags);
+                        float* ov = P.vel + ((int64_t)row * n + i) * 3;
+                        ov[0] = v.x; ov[1] = v.y; ov[2] = v.z;
+                    }
+                }
+            }
+        }
+    }
+    pp[0] = x.x; pp[1] = x.y; pp[2] = x.z;
+    if (comp) {
+        float* cp = P.comp + 3 * (int64_t)i;
+        cp[0] = c.x; cp[1] = c.y; cp[2] = c.z;
+    }
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) flags |= JT_STATUS_NONFINITE;
+    report_flags(P.status, flags);
+}
+
+}  // namespace jt

@@ -1,0 +1,36 @@
+// Library-internal declarations: error state and the per-field launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/jaxtrace_gb300.h"
+
+namespace jt {
+
+// Record `msg` as the calling thread's last error and return `code`.
+int set_error(int code, const char* fmt, ...);
+// JT_OK for cudaSuccess, else JT_ERR_CUDA with the CUDA error string.
+int cuda_status(cudaError_t e, const char* what);
+
+struct StageBlends;
+struct StepConst;
+
+int grid_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+int grid_step(const jt_grid_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+              const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
+int grid_sample(const jt_grid_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+                int m, int32_t* status, cudaStream_t s);
+
+int mesh_track(const jt_mesh_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+int mesh_step(const jt_mesh_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+              const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
+int mesh_sample(const jt_mesh_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+                int m, int32_t* status, cudaStream_t s);
+
+int nearest_track(const jt_nearest_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+int nearest_step(const jt_nearest_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+                 const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
+int nearest_sample(const jt_nearest_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+                   int m, int32_t* status, cudaStream_t s);
+
+}  // namespace jt

@@ -1,0 +1,535 @@
+"""Velocity fields of the GPU path.
+
+Each class keeps the constructor and sampling signatures of its JAXTrace
+counterpart and owns device-resident snapshot PAIRS (record n of pair p holds
+snapshot p and p+1 of node n side by side, so one load returns both
+bracketing snapshots).  Calling ``sample_at_positions`` runs a CUDA kernel;
+``create_tracker`` fuses the same field into the persistent tracking kernel.
+
+* ``TimeSeriesField``        -- fields/time_series.py:82 (nearest-node space)
+* ``StructuredGridSampler``  -- fields/structured.py:65 (static trilinear)
+* ``StructuredTimeSeriesField`` -- trilinear space + linear time; the
+  reference has no single class for it and composes
+  ``TimeSeriesField.sample_at_time`` with ``StructuredGridSampler``.
+* ``OctreeFEMTimeSeriesFieldOptimized`` --
+  fields/octree_fem_time_series_optimized.py:17 (octree + P1).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import _lib as L
+from .schedule import single_blend
+
+F32 = np.float32
+
+
+def _torch_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("jaxtrace_gb300 runs on a CUDA GPU; no CUDA device is visible (there is no CPU fallback)")
+    return torch
+
+
+def _as_f32(a) -> np.ndarray:
+    return np.asarray(a, dtype=F32)
+
+
+def ensure_positions_shape(positions) -> np.ndarray:
+    """(N,2|3) -> (N,3) float32, as tracker.py:72-87 / base.py _ensure_positions_shape."""
+    pos = _as_f32(positions)
+    if pos.ndim == 1:
+        pos = pos.reshape(1, -1)
+    if pos.ndim != 2:
+        raise ValueError(f"Positions must be 2D array, got shape {pos.shape}")
+    if pos.shape[1] == 2:
+        pos = np.concatenate([pos, np.zeros((pos.shape[0], 1), dtype=F32)], axis=1)
+    elif pos.shape[1] != 3:
+        raise ValueError(f"Positions must have 2 or 3 columns, got {pos.shape[1]}")
+    return np.ascontiguousarray(pos)
+
+
+def storage_code(storage: str) -> int:
+    try:
+        return L.STORAGE_CODES[str(storage).lower()]
+    except KeyError:
+        raise ValueError(f"storage must be one of f32/bf16/f16, got {storage!r}") from None
+
+
+def snapshot_scales(data: np.ndarray, storage: int) -> np.ndarray:
+    """Per-snapshot power-of-two decode scales for 16-bit storage.
+
+    Each snapshot is divided by 2**ceil(log2(max|v|)) before rounding, so its
+    largest magnitude lands in [0.5, 1]; decoding multiplies back exactly.
+    """
+    T = data.shape[0]
+    if storage == L.JT_STORE_F32:
+        return np.ones(T, dtype=F32)
+    amax = np.abs(data.reshape(T, -1)).max(axis=1).astype(np.float64)
+    amax = np.where(np.isfinite(amax) & (amax > 0), amax, 1.0)
+    return np.exp2(np.ceil(np.log2(amax))).astype(F32)
+
+
+def build_pairs_device(data: np.ndarray, storage: int, device="cuda"):
+    """Upload (T,N,3) snapshots as (max(T-1,1), N, 8) pair records."""
+    torch = _torch_cuda()
+    T, N, _ = data.shape
+    P = max(T - 1, 1)
+    scales = snapshot_scales(data, storage)
+    if storage == L.JT_STORE_F32:
+        pairs = torch.zeros((P, N, 8), dtype=torch.float32, device=device)
+    else:
+        dt = torch.bfloat16 if storage == L.JT_STORE_BF16 else torch.float16
+        pairs = torch.zeros((P, N, 8), dtype=dt, device=device)
+    prev = None
+    for t in range(T):
+        snap = torch.from_numpy(np.ascontiguousarray(data[t])).to(device)
+        if storage != L.JT_STORE_F32:
+            snap = (snap / float(scales[t])).to(pairs.dtype)
+        if t < P:
+            pairs[t, :, 0:3] = snap
+        if t >= 1:
+            pairs[t - 1, :, 3:6] = snap
+        prev = snap
+    if T == 1:
+        pairs[0, :, 3:6] = prev
+    return pairs, scales
+
+
+class _DeviceField:
+    """Shared plumbing: snapshot times, blend semantics and the jt_field struct."""
+
+    _semantics = "numpy"
+
+    def _init_time(self, times, interpolation, extrapolation, storage, semantics):
+        self.times = _as_f32(times)
+        self.interpolation = interpolation
+        self.extrapolation = extrapolation
+        if interpolation.lower() not in ("nearest", "linear", "cubic"):
+            raise ValueError(f"Unsupported interpolation: {interpolation}")
+        if extrapolation.lower() not in ("constant", "linear", "nan", "zero"):
+            raise ValueError(f"Unsupported extrapolation: {extrapolation}")
+        if semantics not in ("numpy", "jax"):
+            raise ValueError("time_semantics must be 'numpy' or 'jax'")
+        self._semantics = semantics
+        self.storage = str(storage).lower()
+        self._storage = storage_code(storage)
+        self.t_min, self.t_max = float(self.times[0]), float(self.times[-1])
+        if not np.all(np.diff(self.times) >= 0):
+            warnings.warn("Times are not monotonically non-decreasing; interpolation may be unreliable")
+        self._dev = None
+
+    # -- schedule hooks used by the tracker --
+    def _blend_args(self):
+        return dict(semantics=self._semantics, interpolation=self.interpolation,
+                    extrapolation=self.extrapolation, scales=self._scales_or_none())
+
+    def _scales_or_none(self):
+        self._device()
+        return None if self._storage == L.JT_STORE_F32 else self._scales
+
+    def _default_arith(self):
+        return L.JT_ARITH_EXACT if self._storage == L.JT_STORE_F32 else L.JT_ARITH_COMPENSATED
+
+    def blend_at(self, t) -> np.ndarray:
+        return single_blend(self.times, t, **self._blend_args())
+
+    def get_time_bounds(self) -> Tuple[float, float]:
+        return float(self.t_min), float(self.t_max)
+
+    def validate_time(self, t: float) -> bool:
+        return self.t_min <= float(t) <= self.t_max
+
+    # -- device sampling --
+    def jt_field(self):
+        """The ctypes ``jt_field`` of this field (device buffers built on first use)."""
+        self._device()
+        return self._cfield
+
+    def sample_at_positions(self, query_positions, t):
+        """Velocities at (M,3) positions and time t (fields/base.py:106-122).
+
+        Accepts numpy (returns numpy) or CUDA torch tensors (returns a tensor).
+        """
+        torch = _torch_cuda()
+        self._device()
+        is_tensor = isinstance(query_positions, torch.Tensor)
+        if is_tensor:
+            q = query_positions.to(device="cuda", dtype=torch.float32)
+            if q.ndim == 1:
+                q = q.reshape(1, -1)
+            if q.shape[1] == 2:
+                q = torch.cat([q, torch.zeros_like(q[:, :1])], dim=1)
+            q = q.contiguous()
+        else:
+            q = torch.from_numpy(ensure_positions_shape(query_positions)).cuda()
+        out = torch.empty_like(q)
+        e = self.blend_at(t)
+        blend = L.Blend.from_buffer_copy(e.tobytes())
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        L.check(L.load().jt_field_sample(C.byref(self._cfield), C.byref(blend), self._default_arith(),
+                                         L.ptr(q), L.ptr(out), q.shape[0], L.ptr(status), L.stream_ptr()))
+        return out if is_tensor else out.cpu().numpy()
+
+    def __call__(self, a, b):
+        t, positions = _parse_time_and_positions(a, b)
+        return self.sample_at_positions(positions, t)
+
+    def evaluate(self, a, b):
+        return self(a, b)
+
+    def sample_at_time(self, t):
+        """All node values at time t (time_series.py:306), blended on the device."""
+        torch = _torch_cuda()
+        pairs = self._device_pairs()
+        e = self.blend_at(t)[0]
+        A = pairs[int(e["pair"]), :, 0:3].float()
+        B = pairs[int(e["pair"]), :, 3:6].float()
+        form = int(e["form"])
+        if form == L.JT_BLEND_WEIGHTED:
+            v = A * float(e["wa"]) + B * float(e["wb"])
+        else:
+            A = A * float(e["sa"])
+            B = B * float(e["sb"])
+            base = A if form == L.JT_BLEND_LERP_FWD else B
+            v = base + float(e["wb"]) * (B - A)
+        return v.cpu().numpy().astype(F32, copy=False)
+
+    def memory_usage_mb(self) -> float:
+        if self._dev is None:
+            return 0.0
+        return sum(t.numel() * t.element_size() for t in self._dev.values()) / 1024 ** 2
+
+
+def _parse_time_and_positions(a, b):
+    """time_series.py:285-294: accept field(t, positions) or field(positions, t)."""
+    def pos_like(x):
+        try:
+            arr = np.asarray(x) if not hasattr(x, "shape") else x
+        except Exception:
+            return False
+        nd = len(arr.shape)
+        return (nd == 2 and arr.shape[1] in (2, 3)) or (nd == 1 and arr.shape[0] in (2, 3))
+
+    def scalar_like(x):
+        return len(getattr(x, "shape", np.shape(x))) == 0
+
+    if pos_like(a) and scalar_like(b):
+        return float(b), a
+    if pos_like(b) and scalar_like(a):
+        return float(a), b
+    if scalar_like(a) and not scalar_like(b):
+        return float(a), b
+    if scalar_like(b) and not scalar_like(a):
+        return float(b), a
+    raise TypeError("Cannot determine (t, positions) from arguments")
+
+
+# ---------------------------------------------------------------------------
+class StructuredTimeSeriesField(_DeviceField):
+    """Trilinear-in-space, linear-in-time field on a regular grid.
+
+    data: (T, Nx, Ny, Nz, 3) or (T, Nx*Ny*Nz, 3) in ij order; grid_x/y/z the
+    axis coordinates.  Semantics: StructuredGridSampler.sample (structured.py:
+    284-349) of TimeSeriesField.sample_at_time (time_series.py:326-367).
+    """
+
+    def __init__(self, data, times, grid_x, grid_y, grid_z, bounds_handling: str = "clamp",
+                 interpolation: str = "linear", extrapolation: str = "constant", *,
+                 storage: str = "f32", time_semantics: str = "numpy"):
+        gx, gy, gz = _as_f32(grid_x), _as_f32(grid_y), _as_f32(grid_z)
+        if gx.ndim != 1 or gy.ndim != 1 or gz.ndim != 1:
+            raise ValueError("grid axes must be 1-D")
+        nx, ny, nz = len(gx), len(gy), len(gz)
+        data = _as_f32(data)
+        if data.ndim == 5:
+            if data.shape[1:] != (nx, ny, nz, 3):
+                raise ValueError(f"data shape {data.shape} does not match grid ({nx},{ny},{nz})")
+            data = data.reshape(data.shape[0], nx * ny * nz, 3)
+        if data.ndim != 3 or data.shape[1:] != (nx * ny * nz, 3):
+            raise ValueError(f"data must be (T,Nx,Ny,Nz,3) or (T,Nx*Ny*Nz,3), got {data.shape}")
+        mode = bounds_handling.lower()
+        codes = {"clamp": L.JT_GRID_CLAMP, "zero": L.JT_GRID_ZERO, "nan": L.JT_GRID_NAN,
+                 "periodic": L.JT_GRID_PERIODIC}
+        if mode not in codes:
+            raise ValueError(f"Unsupported bounds_handling: {bounds_handling}")
+        self._init_time(times, interpolation, extrapolation, storage, time_semantics)
+        if self.times.shape != (data.shape[0],):
+            raise ValueError(f"times shape {self.times.shape} != (T,) with T={data.shape[0]}")
+        self.data = data
+        self.grid_x, self.grid_y, self.grid_z = gx, gy, gz
+        self.bounds_handling = bounds_handling
+        self.Nx, self.Ny, self.Nz = nx, ny, nz
+        self.T, self.N = data.shape[0], data.shape[1]
+        # structured.py:125-132
+        self.dx = float(gx[1] - gx[0]) if nx > 1 else 1.0
+        self.dy = float(gy[1] - gy[0]) if ny > 1 else 1.0
+        self.dz = float(gz[1] - gz[0]) if nz > 1 else 1.0
+        self.x_min, self.x_max = float(gx[0]), float(gx[-1])
+        self.y_min, self.y_max = float(gy[0]), float(gy[-1])
+        self.z_min, self.z_max = float(gz[0]), float(gz[-1])
+        self._mode = codes[mode]
+
+    def _device(self):
+        if self._dev is not None:
+            return
+        pairs, scales = build_pairs_device(self.data, self._storage)
+        self._scales = scales
+        self._dev = {"pairs": pairs}
+        g = L.GridField()
+        g.nx, g.ny, g.nz = self.Nx, self.Ny, self.Nz
+        g.bounds_mode = self._mode
+        g.origin[:] = [F32(self.x_min), F32(self.y_min), F32(self.z_min)]
+        g.spacing[:] = [F32(self.dx), F32(self.dy), F32(self.dz)]
+        # structured.py:299-301: x <= x_min + (Nx-1)*dx, the Python float rounded to float32
+        g.valid_hi[:] = [F32(self.x_min + (self.Nx - 1) * self.dx), F32(self.y_min + (self.Ny - 1) * self.dy),
+                         F32(self.z_min + (self.Nz - 1) * self.dz)]
+        g.storage = self._storage
+        g.n_pairs = pairs.shape[0]
+        g.pair_stride = self.N
+        g.pairs = pairs.data_ptr()
+        self._cgrid = g
+        self._cfield = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
+
+    def _device_pairs(self):
+        self._device()
+        return self._dev["pairs"]
+
+    def get_spatial_bounds(self):
+        return (np.array([self.x_min, self.y_min, self.z_min], dtype=F32),
+                np.array([self.x_max, self.y_max, self.z_max], dtype=F32))
+
+
+class StructuredGridSampler(StructuredTimeSeriesField):
+    """Static trilinear sampler, structured.py:65 (velocity_data (Nx,Ny,Nz,3))."""
+
+    def __init__(self, velocity_data, grid_x, grid_y, grid_z, bounds_handling: str = "clamp",
+                 grid_meta=None, *, storage: str = "f32"):
+        v = _as_f32(velocity_data)
+        if v.ndim != 4:
+            raise ValueError(f"velocity_data must be 4D (Nx,Ny,Nz,3), got {v.shape}")
+        if v.shape[3] != 3:
+            raise ValueError(f"velocity_data must have 3 components, got {v.shape[3]}")
+        for name, g, n in (("grid_x", grid_x, v.shape[0]), ("grid_y", grid_y, v.shape[1]), ("grid_z", grid_z, v.shape[2])):
+            if _as_f32(g).shape != (n,):
+                raise ValueError(f"{name} shape {_as_f32(g).shape} doesn't match velocity_data")
+        super().__init__(v[None], np.zeros(1, dtype=F32), grid_x, grid_y, grid_z, bounds_handling,
+                         storage=storage)
+        self.velocity_data = v
+        self.grid_meta = grid_meta
+
+    def sample(self, positions):
+        return self.sample_at_positions(positions, 0.0)
+
+
+# ---------------------------------------------------------------------------
+class TimeSeriesField(_DeviceField):
+    """time_series.py:82 -- snapshots at scattered nodes, nearest-node in space.
+
+    The reference samples space by the nearest node (argmin of the float32
+    squared distance, lowest index on ties); here a uniform cell list
+    limits the search (exact, not approximate).
+    """
+
+    def __init__(self, data, times, positions, interpolation: str = "linear",
+                 extrapolation: str = "constant", _source_info: Optional[dict] = None, *,
+                 storage: str = "f32", time_semantics: str = "numpy"):
+        data = _as_f32(data)
+        positions = ensure_positions_shape(positions)
+        if data.ndim != 3:
+            raise ValueError(f"data must have 3 dims (T,N,3), got {data.shape}")
+        T, N, D = data.shape
+        if D != 3:
+            raise ValueError(f"data last dimension must be 3, got {D}")
+        self._init_time(times, interpolation, extrapolation, storage, time_semantics)
+        if self.times.shape != (T,):
+            raise ValueError(f"times shape {self.times.shape} != (T,) with T={T}")
+        if positions.shape != (N, 3):
+            raise ValueError(f"positions shape {positions.shape} != (N,3) with N={N}")
+        self.data, self.positions = data, positions
+        self.T, self.N = T, N
+        self._source_info = _source_info or {}
+
+    def _cell_list(self):
+        P = self.positions.astype(np.float64)
+        lo, hi = P.min(axis=0), P.max(axis=0)
+        ext = hi - lo
+        live = ext > 0
+        n = self.N
+        vol = np.prod(ext[live]) if live.any() else 1.0
+        dim = max(int(live.sum()), 1)
+        h = (vol / max(n / 2.0, 1.0)) ** (1.0 / dim) if live.any() else 1.0
+        cells = np.where(live, np.clip(np.ceil(ext / h), 1, 1024), 1).astype(np.int64)
+        while np.prod(cells) > 8 * n + 64:
+            cells = np.maximum(cells // 2, 1)
+        inv = np.where(live, cells / np.where(live, ext, 1.0), 0.0)
+        # cell of each node, computed exactly as the kernel does (float32)
+        o32, inv32 = lo.astype(F32), inv.astype(F32)
+        c = np.floor((self.positions - o32) * inv32)
+        c = np.clip(np.nan_to_num(c), 0, cells - 1).astype(np.int64)
+        cid = (c[:, 2] * cells[1] + c[:, 1]) * cells[0] + c[:, 0]
+        order = np.argsort(cid, kind="stable")
+        counts = np.bincount(cid, minlength=int(np.prod(cells)))
+        start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        return o32, inv32, cells.astype(np.int32), order.astype(np.int32), start
+
+    def _device(self):
+        if self._dev is not None:
+            return
+        torch = _torch_cuda()
+        pairs, scales = build_pairs_device(self.data, self._storage)
+        self._scales = scales
+        o32, inv32, cells, order, start = self._cell_list()
+        pts = np.zeros((self.N, 4), dtype=F32)
+        pts[:, :3] = self.positions[order]
+        self._dev = {"pairs": pairs, "points": torch.from_numpy(pts).cuda(),
+                     "ids": torch.from_numpy(order).cuda(), "start": torch.from_numpy(start).cuda()}
+        q = L.NearestField()
+        q.n_points = self.N
+        q.cells[:] = [int(v) for v in cells]
+        q.origin[:] = [float(v) for v in o32]
+        q.inv_cell[:] = [float(v) for v in inv32]
+        q.storage = self._storage
+        q.n_pairs = pairs.shape[0]
+        q.pair_stride = self.N
+        q.points = self._dev["points"].data_ptr()
+        q.point_ids = self._dev["ids"].data_ptr()
+        q.cell_start = self._dev["start"].data_ptr()
+        q.pairs = pairs.data_ptr()
+        self._cnear = q
+        self._cfield = L.Field(kind=L.JT_FIELD_NEAREST, nearest=C.pointer(q))
+
+    def _device_pairs(self):
+        self._device()
+        return self._dev["pairs"]
+
+    def get_spatial_bounds(self):
+        return self.positions.min(axis=0).astype(F32), self.positions.max(axis=0).astype(F32)
+
+    def validate_data(self) -> bool:
+        if not np.all(np.isfinite(self.data)):
+            raise ValueError("Velocity data contains non-finite values")
+        if not np.all(np.isfinite(self.times)):
+            raise ValueError("Time data contains non-finite values")
+        if not np.all(np.isfinite(self.positions)):
+            raise ValueError("Position data contains non-finite values")
+        if not np.all(np.diff(self.times) >= 0):
+            raise ValueError("Times must be monotonically non-decreasing")
+        return True
+
+
+# ---------------------------------------------------------------------------
+class OctreeMesh:
+    """Host copy of the octree in the reference's array layout
+    (OctreeMeshOptimized, octree_fem_interpolator_optimized.py:18-38)."""
+
+    def __init__(self, points, connectivity, max_elements_per_leaf=32, max_depth=12):
+        points = np.ascontiguousarray(_as_f32(points))
+        conn = np.ascontiguousarray(np.asarray(connectivity, dtype=np.int32))
+        if points.ndim != 2 or points.shape[1] != 3:
+            raise ValueError(f"points must be (N,3), got {points.shape}")
+        if conn.ndim != 2 or conn.shape[1] != 4:
+            raise ValueError(f"connectivity must be (M,4), got {conn.shape}")
+        lib = L.load()
+        handle = C.c_void_p()
+        info = L.OctreeInfo()
+        L.check(lib.jt_octree_build(points.ctypes.data, points.shape[0], conn.ctypes.data, conn.shape[0],
+                                    int(max_elements_per_leaf), int(max_depth), C.byref(handle), C.byref(info)))
+        try:
+            K, M = info.n_nodes, conn.shape[0]
+            self.nodes = np.zeros(K, dtype=L.OCTREE_NODE_DTYPE)
+            self.elems = np.zeros(max(info.n_elem_entries, 1), dtype=np.int32)
+            self.tet_box = np.zeros((M, 8), dtype=F32)
+            self.tet_geom = np.zeros((M, 16), dtype=F32)
+            bounds = np.zeros((K, 6), dtype=F32)
+            L.check(lib.jt_octree_fetch(handle, self.nodes.ctypes.data, self.elems.ctypes.data,
+                                        self.tet_box.ctypes.data, self.tet_geom.ctypes.data, bounds.ctypes.data))
+        finally:
+            lib.jt_octree_free(handle)
+        self.info = info
+        self.points, self.connectivity = points, conn
+        self.max_elements_per_leaf, self.max_depth = int(max_elements_per_leaf), int(max_depth)
+        self.nodes_min, self.nodes_max = bounds[:, :3].copy(), bounds[:, 3:].copy()
+        self.nodes_children = self.nodes["children"].copy()
+        self.nodes_is_leaf = self.nodes["is_leaf"].astype(bool)
+        self.nodes_elem_counts = self.nodes["elem_count"].copy()
+        self.node_depth = self.nodes["pad"][:, 0].copy()
+
+    @property
+    def nodes_elements(self) -> np.ndarray:
+        """(K, max_elems) int32 padded with -1 (…optimized.py:183)."""
+        K = len(self.nodes)
+        W = max(int(self.info.max_elems), 0)
+        out = np.full((K, W), -1, dtype=np.int32)
+        for k in np.nonzero(self.nodes_elem_counts)[0]:
+            o, c = self.nodes["elem_offset"][k], self.nodes_elem_counts[k]
+            out[k, :c] = self.elems[o:o + c]
+        return out
+
+    @property
+    def element_bounds(self) -> np.ndarray:
+        return np.stack([self.tet_box[:, :3], self.tet_box[:, 4:7]], axis=1)
+
+
+class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
+    """Octree point location + P1 interpolation over a tetrahedral mesh with
+    the JAX float32 time blend (octree_fem_time_series_optimized.py:17-113)."""
+
+    def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
+                 extrapolation: str = "constant", _source_info: Optional[dict] = None,
+                 max_elements_per_leaf: int = 32, max_depth: int = 12, *, storage: str = "f32"):
+        data = _as_f32(data)
+        positions = ensure_positions_shape(positions)
+        if data.ndim != 3 or data.shape[2] != 3:
+            raise ValueError(f"data must have 3 dims (T,N,3), got {data.shape}")
+        T, N, _ = data.shape
+        self._init_time(times, interpolation, extrapolation, storage, "jax")
+        if self.times.shape != (T,):
+            raise ValueError(f"times shape {self.times.shape} != (T,) with T={T}")
+        if positions.shape != (N, 3):
+            raise ValueError(f"positions shape {positions.shape} != (N,3) with N={N}")
+        self.data, self.positions = data, positions
+        self.T, self.N = T, N
+        self._source_info = _source_info or {}
+        self.octree_mesh = OctreeMesh(positions, connectivity, max_elements_per_leaf, max_depth)
+
+    def _device(self):
+        if self._dev is not None:
+            return
+        torch = _torch_cuda()
+        m = self.octree_mesh
+        pairs, scales = build_pairs_device(self.data, self._storage)
+        self._scales = scales
+        pts = np.zeros((self.N, 4), dtype=F32)
+        pts[:, :3] = self.positions
+        d = {"pairs": pairs, "points": torch.from_numpy(pts).cuda(),
+             "tet_box": torch.from_numpy(m.tet_box).cuda(), "tet_geom": torch.from_numpy(m.tet_geom).cuda(),
+             "nodes": torch.from_numpy(m.nodes.view(np.int32).reshape(len(m.nodes), 16)).cuda(),
+             "elems": torch.from_numpy(m.elems).cuda()}
+        self._dev = d
+        f = L.MeshField()
+        f.n_points, f.n_tets = self.N, m.connectivity.shape[0]
+        f.n_nodes, f.max_depth = len(m.nodes), m.max_depth
+        f.storage, f.n_pairs, f.pair_stride = self._storage, pairs.shape[0], self.N
+        f.points, f.tet_box, f.tet_geom = d["points"].data_ptr(), d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
+        f.nodes, f.elems, f.pairs = d["nodes"].data_ptr(), d["elems"].data_ptr(), pairs.data_ptr()
+        self._cmesh = f
+        self._cfield = L.Field(kind=L.JT_FIELD_MESH, mesh=C.pointer(f))
+
+    def _device_pairs(self):
+        self._device()
+        return self._dev["pairs"]
+
+    def get_spatial_bounds(self):
+        return self.positions.min(axis=0).astype(F32), self.positions.max(axis=0).astype(F32)
+
+    def __repr__(self) -> str:
+        m = self.octree_mesh
+        return (f"OctreeFEMTimeSeriesFieldOptimized(data={self.data.shape}, times={self.times.shape}, "
+                f"positions={self.positions.shape}, elements={m.connectivity.shape[0]}, "
+                f"octree_nodes={len(m.nodes)}, octree_leaves={int(m.nodes_is_leaf.sum())}, "
+                f"interpolation='{self.interpolation}', extrapolation='{self.extrapolation}')")

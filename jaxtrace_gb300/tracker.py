@@ -1,0 +1,382 @@
+"""Particle tracker with the JAXTrace API (tracking/tracker.py:107-855).
+
+``create_tracker(integrator_name, field, boundary_condition, **options)``
+returns a ``ParticleTracker`` whose ``track_particles`` runs the whole time
+loop in one persistent CUDA kernel per time chunk: integrator stages, field
+evaluation and boundary fused, positions held in registers, recorded rows
+written straight into a device trajectory slab that streams to the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+from dataclasses import dataclass, field as dc_field
+from typing import Any, Callable, Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import _lib as L
+from .boundary import BoundaryDescriptor
+from .fields import ensure_positions_shape
+from .integrators import INTEGRATORS, resolve_field
+from .particles import Trajectory
+from .schedule import build_schedule, step_constants
+
+F32 = np.float32
+
+
+def _estimate_memory_usage(n_particles: int, n_timesteps: int, has_velocities: bool = False) -> float:
+    """tracker.py:89-101 (GB of host trajectory storage)."""
+    pos_size = n_timesteps * n_particles * 3 * 4
+    time_size = n_timesteps * 4
+    vel_size = pos_size if has_velocities else 0
+    workspace_size = n_particles * 3 * 4 * 4
+    return (pos_size + time_size + vel_size + workspace_size) / (1024 ** 3)
+
+
+@dataclass
+class TrackerOptions:
+    """tracker.py:107-153, extended.  The reference fields are all accepted
+    and keep their meaning where it applies to a GPU run; new fields:
+
+    record_every       record every k-th step into a compact trajectory
+                       (rows 0, k, 2k, ...; None keeps the reference layout)
+    record_final_only  keep only the initial and final positions
+    precision          'exact' (float32, bit-compatible with the NumPy
+                       reference) or 'compensated' (FMA + Kahan sums); 16-bit
+                       snapshot storage always runs 'compensated'
+    device_memory_gb   device budget of one trajectory slab
+    time_chunk         steps per kernel launch (None: as many as fit)
+    """
+    max_memory_gb: float = 8.0
+    batch_size: Optional[int] = None
+    oom_recovery: bool = True
+    use_jax_jit: bool = True
+    static_compilation: bool = True
+    use_scan_jit: bool = True
+    device_put_inputs: bool = True
+    record_on_device: bool = True
+    max_batch_size: int = 100_000
+    min_batch_size: int = 100
+    record_velocities: bool = False
+    recording_interval: int = 1
+    progress_callback: Optional[Callable[[float], None]] = None
+    progress_style: str = "auto"
+    progress_desc: str = "Tracking"
+    progress_update_every: float = 0.05
+    adaptive_dt: bool = False
+    error_tolerance: float = 1e-6
+    # GPU-path additions
+    record_every: Optional[int] = None
+    record_final_only: bool = False
+    precision: str = "exact"
+    device_memory_gb: float = 32.0
+    time_chunk: Optional[int] = None
+
+    def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
+        """tracker.py:142-153."""
+        if self.batch_size is not None:
+            return min(self.batch_size, self.max_batch_size)
+        batch_size = min(n_particles, self.max_batch_size)
+        while batch_size >= self.min_batch_size:
+            if _estimate_memory_usage(batch_size, n_timesteps, self.record_velocities) <= self.max_memory_gb:
+                break
+            batch_size = max(batch_size // 2, self.min_batch_size)
+        return max(batch_size, self.min_batch_size)
+
+
+def _integrator_code(integrator) -> int:
+    code = getattr(integrator, "_jt_code", None)
+    if code is None:
+        raise TypeError("unsupported integrator for the GPU path: use euler_step, rk2_step or rk4_step")
+    return int(code)
+
+
+def _boundary_descriptor(bc) -> BoundaryDescriptor:
+    if isinstance(bc, BoundaryDescriptor):
+        return bc
+    raise TypeError("unsupported boundary for the GPU path: use a jaxtrace_gb300.boundary factory")
+
+
+@dataclass
+class ParticleTracker:
+    """tracker.py:159-804 with the GPU engine behind ``track_particles``."""
+    integrator: Callable
+    field_fn: Callable
+    boundary_fn: Callable
+    options: TrackerOptions = dc_field(default_factory=TrackerOptions)
+
+    def __post_init__(self):
+        if not callable(self.integrator):
+            raise ValueError("integrator must be callable")
+        if not callable(self.field_fn):
+            raise ValueError("field_fn must be callable")
+        if not callable(self.boundary_fn):
+            raise ValueError("boundary_fn must be callable")
+        self._code = _integrator_code(self.integrator)
+        self._field = resolve_field(self.field_fn)
+        self._bc = _boundary_descriptor(self.boundary_fn)
+        if self.options.precision not in ("exact", "compensated"):
+            raise ValueError("precision must be 'exact' or 'compensated'")
+        self.last_status = 0
+
+    # ------------------------------------------------------------------
+    def _arith(self) -> int:
+        if self._field._storage != L.JT_STORE_F32 or self.options.precision == "compensated":
+            return L.JT_ARITH_COMPENSATED
+        return L.JT_ARITH_EXACT
+
+    def _schedule(self, times: np.ndarray, dt: float) -> np.ndarray:
+        return build_schedule(times, dt, self._code, self._field.times, **self._field._blend_args())
+
+    def _record_plan(self, n_timesteps: int):
+        """(record_every, compact, n_rows, row_times_index) of the output."""
+        o = self.options
+        T = n_timesteps
+        if o.record_final_only:
+            k = max(T - 1, 1)
+            idx = np.array([0, T - 1] if T > 1 else [0])
+            return k, True, idx
+        if o.record_every is not None:
+            k = int(o.record_every)
+            if k < 1:
+                raise ValueError("record_every must be >= 1")
+            idx = np.arange(0, T, k)
+            return k, True, idx
+        k = int(o.recording_interval)
+        if k < 1:
+            raise ValueError("recording_interval must be >= 1")
+        return k, False, np.arange(T)
+
+    def track_particles(self, initial_positions, time_span: Tuple[float, float], n_timesteps: int,
+                        dt: Optional[float] = None, **kwargs) -> Trajectory:
+        """tracker.py:320-358: T = n_timesteps rows from linspace(t0, t1, T)."""
+        import torch
+        src = None
+        if isinstance(initial_positions, torch.Tensor) and initial_positions.device.type == "cpu" \
+                and initial_positions.dtype == torch.float32 and initial_positions.ndim == 2 \
+                and initial_positions.shape[1] == 3 and initial_positions.is_contiguous():
+            src = initial_positions          # e.g. pinned host memory: one DMA to the device
+            x0 = src.numpy()
+        else:
+            x0 = ensure_positions_shape(initial_positions)
+        n = x0.shape[0]
+        t_start, t_end = time_span
+        times = np.linspace(float(t_start), float(t_end), int(n_timesteps), dtype=np.float32)
+        if dt is None:
+            dt = float(times[1] - times[0]) if n_timesteps > 1 else 0.0
+        else:
+            dt = float(dt)
+        T = len(times)
+        batch_size = self.options.estimate_batch_size(n, T)
+        k, compact, row_idx = self._record_plan(T)
+        n_rows = len(row_idx)
+        positions = np.zeros((n_rows, n, 3), dtype=F32)
+        velocities = np.zeros((n_rows, n, 3), dtype=F32) if self.options.record_velocities else None
+        if n == 0 or T == 0:
+            return self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, 0)
+        positions[0] = x0
+        pos = (src if src is not None else torch.from_numpy(x0)).to("cuda", non_blocking=src is not None)
+        if velocities is not None:
+            velocities[0] = self._field.sample_at_positions(pos, times[0]).cpu().numpy()
+        n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities)
+        if compact and self.options.record_final_only and T > 1:
+            positions[-1] = pos.cpu().numpy()
+            if velocities is not None:
+                velocities[-1] = self._field.sample_at_positions(pos, times[-1]).cpu().numpy()
+        return self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, n_chunks)
+
+    def _trajectory(self, positions, times, velocities, n, T, dt, batch_size, n_chunks):
+        meta = {
+            "integrator": str(self.integrator),
+            "batch_processing": "single_batch" if batch_size >= n else "multi_batch",
+            "n_particles": n,
+            "n_timesteps": T,
+            "dt": dt,
+            "jax_compiled": False,
+            "jit_scan": False,
+            "backend": "gb300",
+            "kernel": f"jt_track/{type(self._field).__name__}",
+            "storage": self._field.storage,
+            "arith": "exact" if self._arith() == L.JT_ARITH_EXACT else "compensated",
+            "time_chunks": n_chunks,
+            "device_status": self.last_status,
+        }
+        if batch_size < n:
+            meta["batch_size"] = batch_size
+            meta["n_batches"] = (n + batch_size - 1) // batch_size
+        return Trajectory(positions=positions, times=np.asarray(times, dtype=F32), velocities=velocities,
+                          metadata=meta)
+
+    # ------------------------------------------------------------------
+    def make_params(self, pos, dt, n_steps_total, sched_dev, status, comp=None) -> L.TrackParams:
+        p = L.TrackParams()
+        p.integrator = self._code
+        p.arith = self._arith()
+        p.n_particles = pos.shape[0]
+        dtf, dth, dt6 = step_constants(dt)
+        p.dt, p.dt_half, p.dt_sixth = float(dtf), float(dth), float(dt6)
+        p.schedule = sched_dev.data_ptr()
+        p.pos = pos.data_ptr()
+        p.comp = comp.data_ptr() if comp is not None else None
+        p.status = status.data_ptr()
+        p.record_every = 1
+        return p
+
+    def _run(self, pos, times, dt, k, compact, n_rows, positions, velocities) -> int:
+        """Advance ``pos`` (device, (N,3)) through all steps, filling rows 1.. of the outputs."""
+        import torch
+        n = pos.shape[0]
+        n_steps = len(times) - 1
+        if n_steps <= 0:
+            return 0
+        sched = self._schedule(times, dt)
+        sched_dev = torch.from_numpy(sched.view(np.int32).reshape(-1, 8)).cuda()
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        comp = torch.zeros_like(pos) if self._arith() == L.JT_ARITH_COMPENSATED else None
+        field_c = self._field.jt_field()
+        bc_c = self._bc.jt_boundary()
+        p = self.make_params(pos, dt, n_steps, sched_dev, status, comp)
+        record = n_rows > 1 and not self.options.record_final_only
+        row_bytes = n * 12 * (2 if velocities is not None else 1)
+        budget_rows = max(1, int(self.options.device_memory_gb * 1024 ** 3 // max(row_bytes, 1)))
+        # steps per chunk: bounded by rows that fit in the slab
+        if record:
+            chunk = budget_rows * (k if compact else 1) if compact else budget_rows
+            chunk = max(1, min(chunk, n_steps))
+        else:
+            chunk = n_steps
+        if self.options.time_chunk:
+            chunk = max(1, min(chunk, int(self.options.time_chunk)))
+        lib = L.load()
+        stream = L.stream_ptr()
+        n_chunks = 0
+        s = 0
+        cb = self.options.progress_callback
+        while s < n_steps:
+            e = min(s + chunk, n_steps)
+            p.step_begin, p.step_end = s, e
+            slab = vslab = None
+            if record:
+                # rows written by steps s..e-1: counts c in (s, e]
+                if compact:
+                    r0, r1 = s // k + 1, e // k
+                else:
+                    r0, r1 = s + 1, e
+                nr = max(r1 - r0 + 1, 0)
+                if nr > 0:
+                    slab = torch.zeros((nr, n, 3), dtype=torch.float32, device="cuda")
+                    if velocities is not None:
+                        vslab = torch.zeros_like(slab)
+                p.traj = slab.data_ptr() if slab is not None else None
+                p.vel = vslab.data_ptr() if vslab is not None else None
+                p.record_every = k
+                p.record_compact = int(compact)
+                p.row_base = r0
+                p.n_rows = nr
+            L.check(lib.jt_track(C.byref(field_c), C.byref(bc_c), C.byref(p), stream))
+            if slab is not None:
+                positions[r0:r0 + nr] = slab.cpu().numpy()
+                if vslab is not None:
+                    velocities[r0:r0 + nr] = vslab.cpu().numpy()
+            n_chunks += 1
+            s = e
+            if cb is not None:
+                cb(s / n_steps)
+        self.last_status = int(status.item())
+        return n_chunks
+
+    def track_device(self, pos, times, dt, status=None, comp=None, sched_dev=None):
+        """Advance device positions in place with no recording (benchmark and
+        ensemble entry).  ``times`` is the float32 step grid."""
+        import torch
+        n_steps = len(times) - 1
+        if sched_dev is None:
+            sched_dev = torch.from_numpy(self._schedule(times, dt).view(np.int32).reshape(-1, 8)).cuda()
+        if status is None:
+            status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if comp is None and self._arith() == L.JT_ARITH_COMPENSATED:
+            comp = torch.zeros_like(pos)
+        p = self.make_params(pos, dt, n_steps, sched_dev, status, comp)
+        p.step_begin, p.step_end = 0, n_steps
+        L.check(L.load().jt_track(C.byref(self._field.jt_field()), C.byref(self._bc.jt_boundary()), C.byref(p),
+                                  L.stream_ptr()))
+        return pos
+
+    # ------------------------------------------------------------------
+    def validate_configuration(self) -> Dict[str, Any]:
+        """tracker.py:720-787 on a one-particle probe."""
+        res = {"valid": True, "warnings": [], "errors": [], "configuration": {}}
+        test_pos = np.array([[0.0, 0.0, 0.0]], dtype=F32)
+        try:
+            v = np.asarray(self._field.sample_at_positions(test_pos, 0.0), dtype=F32)
+            if v.shape != (1, 3):
+                res["errors"].append(f"field_fn returned wrong shape: {v.shape}, expected (1, 3)")
+                res["valid"] = False
+            if not np.all(np.isfinite(v)):
+                res["warnings"].append("field_fn returned non-finite values")
+        except Exception as e:  # noqa: BLE001 -- report, as the reference does
+            res["errors"].append(f"field_fn test failed: {e}")
+            res["valid"] = False
+        try:
+            b = np.asarray(self._bc(test_pos), dtype=F32)
+            if b.shape != test_pos.shape:
+                res["errors"].append(f"boundary_fn changed shape: {b.shape} != {test_pos.shape}")
+                res["valid"] = False
+        except Exception as e:  # noqa: BLE001
+            res["errors"].append(f"boundary_fn test failed: {e}")
+            res["valid"] = False
+        res["configuration"] = {"backend": "gb300", "integrator": self._code,
+                                "max_memory_gb": self.options.max_memory_gb,
+                                "record_velocities": self.options.record_velocities}
+        return res
+
+    def estimate_runtime(self, n_particles: int, n_timesteps: int, calibration_particles: int = 1000,
+                         calibration_steps: int = 10) -> Dict[str, Any]:
+        """tracker.py:538-588 with a GPU calibration run."""
+        import time
+        x = np.random.uniform(-1, 1, size=(calibration_particles, 3)).astype(F32)
+        t0 = time.time()
+        try:
+            self.track_particles(x, (0.0, 1.0), calibration_steps)
+        except Exception as e:  # noqa: BLE001
+            return {"success": False, "error": str(e), "error_type": type(e).__name__}
+        el = time.time() - t0
+        per = el / max(calibration_particles * calibration_steps, 1)
+        est = n_particles * n_timesteps * per
+        return {"success": True, "estimated_runtime_seconds": est, "time_per_particle_step": per,
+                "calibration_time": el, "calibration_particles": calibration_particles}
+
+
+def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:
+    """tracker.py:810-855."""
+    if integrator_name not in INTEGRATORS:
+        raise ValueError(f"Unknown integrator: {integrator_name}. Available: {list(INTEGRATORS.keys())}")
+    integrator = INTEGRATORS[integrator_name]
+    if hasattr(field, "sample_at_positions"):
+        field_fn = field
+    elif hasattr(field, "sample"):
+        field_fn = field
+    elif callable(field):
+        field_fn = field
+    else:
+        raise TypeError("field must be BaseField-like or a callable: field(positions, t) -> velocities")
+    if not callable(boundary_condition):
+        raise TypeError("boundary_condition must be callable")
+    tracker_options = TrackerOptions(**options)
+    return ParticleTracker(integrator=integrator, field_fn=field_fn, boundary_fn=boundary_condition,
+                           options=tracker_options)
+
+
+def track_particles_simple(initial_positions, velocity_field, time_span, n_timesteps, integrator: str = "rk4",
+                           boundary_condition=None, dt: Optional[float] = None, **tracker_options) -> Trajectory:
+    """tracker.py:857-880."""
+    if boundary_condition is None:
+        from .boundary import no_boundary
+        boundary_condition = no_boundary()
+    tr = create_tracker(integrator, velocity_field, boundary_condition, **tracker_options)
+    return tr.track_particles(initial_positions, time_span, n_timesteps, dt=dt)
+
+
+__all__ = ["TrackerOptions", "ParticleTracker", "create_tracker", "track_particles_simple"]

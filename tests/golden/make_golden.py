@@ -1,0 +1,253 @@
+"""Regenerate the golden fixtures by running the JAXTrace reference itself.
+
+Run from the repository root in a checkout that has the reference sources:
+    python tests/golden/make_golden.py /path/to/JAXTrace
+Phase ``numpy`` imports the reference as-is (no jax installed, so every
+module takes its NumPy path).  Phase ``octree`` puts the NumPy stand-in for
+jax (oracle/jaxshim) first on sys.path so the octree modules, which import
+jax unconditionally, can run.  Each phase runs in its own process.
+
+Fixtures hold both the inputs and the reference outputs, so the tests need
+only the .npz files.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+F32 = np.float32
+
+
+def abc(points01: np.ndarray, t: float, A=1.0, B=0.7, C=0.43) -> np.ndarray:
+    """ABC flow at points in [0,1]^3 (coordinates scaled to [0,2pi]), float64."""
+    x, y, z = (2 * np.pi * points01[..., k].astype(np.float64) for k in range(3))
+    s = 1.0 + 0.1 * np.sin(2 * np.pi * t)
+    return np.stack([A * np.sin(z) + C * np.cos(y), B * np.sin(x) + A * np.cos(z),
+                     C * np.sin(y) + B * np.cos(x)], axis=-1) * s
+
+
+def grid_nodes(gx, gy, gz):
+    X, Y, Z = np.meshgrid(gx, gy, gz, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1).astype(F32)
+
+
+def kuhn_mesh(n: int, jitter: float, seed: int):
+    """(n+1)^3 nodes on [0,1]^3, interior jittered by U(-j,j)/n; 6 tets per hex."""
+    g = np.linspace(0, 1, n + 1)
+    P = grid_nodes(g, g, g).astype(np.float64)
+    idx = np.arange((n + 1) ** 3).reshape(n + 1, n + 1, n + 1)
+    interior = np.all((P > 0) & (P < 1), axis=1)
+    rng = np.random.default_rng(seed)
+    P[interior] += rng.uniform(-jitter, jitter, (interior.sum(), 3)) / n
+    tets = []
+    local = [(0, 1, 3, 7), (0, 1, 5, 7), (0, 2, 3, 7), (0, 2, 6, 7), (0, 4, 5, 7), (0, 4, 6, 7)]
+    for i in range(n):
+        for j in range(n):
+            for k in range(n):
+                v = [idx[i + (c & 1), j + ((c >> 1) & 1), k + ((c >> 2) & 1)] for c in range(8)]
+                for t in local:
+                    tets.append([v[q] for q in t])
+    return P.astype(F32), np.asarray(tets, dtype=np.int32)
+
+
+# ---------------------------------------------------------------------------
+def phase_numpy(ref: str):
+    sys.path.insert(0, ref)
+    import warnings
+    warnings.simplefilter("ignore")
+    from jaxtrace.fields.structured import StructuredGridSampler
+    from jaxtrace.fields.time_series import TimeSeriesField
+    from jaxtrace.tracking import boundary as bnd
+    from jaxtrace.tracking.tracker import create_tracker
+    from jaxtrace.utils.jax_utils import JAX_AVAILABLE
+    assert not JAX_AVAILABLE, "phase numpy must run without jax"
+    rng = np.random.default_rng(1234)
+
+    # A1: time blend, every extrapolation mode, f32 and python-float times
+    data = rng.standard_normal((5, 7, 3)).astype(F32)
+    times = np.array([0.0, 0.25, 0.5, 0.5, 1.0], dtype=F32)
+    pos = rng.random((7, 3)).astype(F32)
+    tq = np.concatenate([np.linspace(-0.3, 1.3, 33), times.astype(np.float64), [0.5 - 1e-9, 1.0 + 1e-12, -1e-13],
+                         np.float32(np.linspace(0.01, 0.99, 7)).astype(np.float64)])
+    out = {}
+    for ex in ("constant", "linear", "zero", "nan"):
+        ts = TimeSeriesField(data=data, times=times, positions=pos, extrapolation=ex)
+        out[ex] = np.stack([np.asarray(ts.sample_at_time(float(t)), dtype=F32) for t in tq])
+    np.savez_compressed(HERE / "time_blend.npz", data=data, times=times, tq=tq, **{f"out_{k}": v for k, v in out.items()})
+
+    # A2: structured sampler, all bounds modes
+    res = {}
+    for mode in ("clamp", "zero", "nan", "periodic"):
+        nx, ny, nz = 5, 6, 7
+        if mode == "periodic":
+            gx, gy, gz = (np.arange(n, dtype=np.float64) / n for n in (nx, ny, nz))
+        else:
+            gx, gy, gz = np.linspace(-0.5, 1.0, nx), np.linspace(0, 2, ny), np.linspace(0.25, 0.75, nz)
+        gx, gy, gz = (g.astype(F32) for g in (gx, gy, gz))
+        V = rng.standard_normal((nx, ny, nz, 3)).astype(F32)
+        q = np.concatenate([rng.uniform(-1.5, 2.5, (400, 3)), grid_nodes(gx, gy, gz)[:60],
+                            np.array([[gx[-1], gy[-1], gz[-1]], [gx[0], gy[0], gz[0]]])]).astype(F32)
+        s = StructuredGridSampler(V, gx, gy, gz, bounds_handling=mode)
+        res[mode] = dict(V=V, gx=gx, gy=gy, gz=gz, q=q, out=np.asarray(s.sample(q), dtype=F32))
+    np.savez_compressed(HERE / "structured.npz", **{f"{m}_{k}": v for m, d in res.items() for k, v in d.items()})
+
+    # A3: boundary callables
+    B = np.array([[-1.0, 0.0, 0.5], [1.0, 2.0, 1.5]], dtype=F32)
+    P = np.concatenate([rng.uniform(-4, 5, (600, 3)), np.array([[-1.0, 0.0, 0.5], [1.0, 2.0, 1.5], [0, 1, 1]])]).astype(F32)
+    bres = {"P": P, "B": B}
+    bres["periodic"] = bnd.periodic_boundary(B)(P)
+    bres["reflective"] = bnd.reflective_boundary(B)(P)
+    bres["clamping"] = bnd.clamping_boundary(B)(P)
+    bres["absorbing"] = bnd.absorbing_boundary_factory(B)(P)
+    bres["absorbing_m7"] = bnd.absorbing_boundary_factory(B, outside_value=-7.0)(P)
+    bres["mixed_prc"] = bnd.mixed_boundary(B, {"x": "periodic", "y": "reflective", "z": "clamping"})(P)
+    bres["mixed_ab"] = bnd.mixed_boundary(B, {"x": "absorbing", "z": "reflective"})(P)
+    # continuous inlet: particles mostly near the faces so that many exit
+    Pin = np.concatenate([rng.uniform(-1.3, 1.3, (300, 3)) * np.array([1, 1.2, 0.6]) + np.array([0, 1, 1]),
+                          rng.uniform(0.9, 1.1, (100, 3)) * np.array([1, 2, 1.5])]).astype(F32)
+    bres["Pin"] = Pin
+    conc = {"x": 9, "y": 17, "z": 5}
+    bres["inlet_xpos"] = bnd.continuous_inlet_boundary_factory(B, "x", "positive", "grid", conc)(Pin)
+    bres["inlet_yneg"] = bnd.continuous_inlet_boundary_factory(B, "y", "negative", "grid", conc)(Pin)
+    bres["inlet_zpos"] = bnd.continuous_inlet_boundary_factory(B, "z", "positive", "grid", conc)(Pin)
+    np.savez_compressed(HERE / "boundary.npz", **bres)
+
+    # A4: config-0 style tracking (trilinear + linear time + periodic), all integrators
+    n = 12
+    g = (np.arange(n) / n).astype(F32)
+    nodes = grid_nodes(g, g, g)
+    st = np.linspace(0, 1, 8).astype(F32)
+    D = np.stack([abc(nodes, float(t)) for t in st]).astype(F32)
+    ts = TimeSeriesField(data=D, times=st, positions=nodes)
+
+    def field(p, t):
+        V = np.asarray(ts.sample_at_time(t)).reshape(n, n, n, 3)
+        return StructuredGridSampler(V, g, g, g, bounds_handling="periodic").sample(p)
+
+    # A stage position in (-4e-8, 0) makes np.mod(fx, N) round up to N and the
+    # reference raise IndexError (structured.py:294, :325); seeds whose runs
+    # never hit that are kept (the GPU path wraps the index instead).
+    for seed in range(42, 200):
+        np.random.seed(seed)
+        x0 = np.random.uniform(0, 1, (300, 3)).astype(F32)
+        trk = {"D": D, "st": st, "g": g, "x0": x0, "seed": np.int64(seed)}
+        try:
+            for integ, T in (("rk4", 31), ("rk2", 21), ("euler", 21)):
+                tr = create_tracker(integ, field, bnd.periodic_boundary(((0, 0, 0), (1, 1, 1))),
+                                    progress_style="none")
+                traj = tr.track_particles(x0, (0.0, 0.3 if integ == "rk4" else 0.2), T, dt=0.01)
+                trk[f"{integ}_traj"] = traj.positions
+            break
+        except IndexError:
+            continue
+    # record_velocities + recording_interval semantics of the step loop
+    tr = create_tracker("rk4", field, bnd.periodic_boundary(((0, 0, 0), (1, 1, 1))), progress_style="none",
+                        record_velocities=True, recording_interval=3)
+    traj = tr.track_particles(x0[:50], (0.0, 0.1), 11, dt=0.01)
+    trk["rec_pos"], trk["rec_vel"] = traj.positions, traj.velocities
+    np.savez_compressed(HERE / "track_grid.npz", **trk)
+
+    # A5: config-2 style (clamp grid, continuous inlet on a lattice, mean flow +x)
+    n = 10
+    g = np.linspace(0, 1, n).astype(F32)
+    nodes = grid_nodes(g, g, g)
+    st = np.linspace(0, 2, 9).astype(F32)
+    noise = np.random.default_rng(2).normal(0, 0.01, (len(st), len(nodes), 3))
+    D = np.stack([abc(nodes, float(t)) + np.array([1.0, 0, 0]) for t in st]) + noise
+    D = D.astype(F32)
+    ts2 = TimeSeriesField(data=D, times=st, positions=nodes)
+
+    def field2(p, t):
+        V = np.asarray(ts2.sample_at_time(t)).reshape(n, n, n, 3)
+        return StructuredGridSampler(V, g, g, g, bounds_handling="clamp").sample(p)
+
+    from jaxtrace.tracking.seeding import uniform_grid_seeds
+    x0 = uniform_grid_seeds((8, 6, 5), ((0, 0, 0), (1, 1, 1)))
+    bc = bnd.continuous_inlet_boundary_factory(((0, 0, 0), (1, 1, 1)), "x", "positive", "grid",
+                                               {"x": 16, "y": 16, "z": 16})
+    tr = create_tracker("rk4", field2, bc, progress_style="none")
+    traj = tr.track_particles(x0, (0.0, 0.6), 61, dt=0.01)
+    np.savez_compressed(HERE / "track_inlet.npz", D=D, st=st, g=g, x0=x0, traj=traj.positions)
+
+    # A6: nearest-node TimeSeriesField (cKDTree on the NumPy path)
+    nodes = rng.random((400, 3)).astype(F32)
+    Dn = rng.standard_normal((4, 400, 3)).astype(F32)
+    stn = np.array([0, 1, 2, 3], dtype=F32)
+    tsn = TimeSeriesField(data=Dn, times=stn, positions=nodes)
+    q = rng.uniform(-0.2, 1.2, (500, 3)).astype(F32)
+    outs = np.stack([np.asarray(tsn.sample_at_positions(q, t), dtype=F32) for t in (0.0, 0.7, 2.5, 3.5)])
+    # test_quick.py scenario: 15x15x1 nodes, 2D vortex, 25 seeds, reflective, RK4, 100 steps, dt 0.02
+    xs = np.linspace(-1, 1, 15)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    qn = np.stack([X.ravel(), Y.ravel(), np.zeros(X.size)], 1).astype(F32)
+    vt = np.linspace(0, 2, 5).astype(F32)
+    vort = np.stack([np.stack([-qn[:, 1], qn[:, 0], np.zeros(len(qn))], 1) * (1 + 0.2 * t) for t in vt]).astype(F32)
+    tsq = TimeSeriesField(data=vort, times=vt, positions=qn)
+    s = np.linspace(-0.6, 0.6, 5)
+    SX, SY = np.meshgrid(s, s, indexing="ij")
+    seeds = np.stack([SX.ravel(), SY.ravel(), np.zeros(25)], 1).astype(F32)
+    tr = create_tracker("rk4", tsq, bnd.reflective_boundary([[-1, -1, -1], [1, 1, 1]]), progress_style="none")
+    traj = tr.track_particles(seeds, (0.0, 2.0), 101, dt=0.02)
+    np.savez_compressed(HERE / "nearest.npz", nodes=nodes, D=Dn, st=stn, q=q, outs=outs, qn=qn, vort=vort, vt=vt,
+                        seeds=seeds, quick_traj=traj.positions)
+    print("phase numpy: done")
+
+
+def phase_octree(ref: str):
+    sys.path.insert(0, str(REPO / "oracle" / "jaxshim"))
+    sys.path.insert(1, ref)
+    import contextlib
+    import io
+    import warnings
+    warnings.simplefilter("ignore")
+    from jaxtrace.fields import octree_fem_interpolator_optimized as oc
+    from jaxtrace.fields.octree_fem_time_series_optimized import OctreeFEMTimeSeriesFieldOptimized
+    from jaxtrace.tracking import boundary as bnd
+    from jaxtrace.tracking.tracker import create_tracker
+
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    # B0: the module's own known answer (…optimized.py:413-433)
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1], [1, 0, 1], [1, 1, 0], [0, 1, 1]], F32)
+    conn = np.array([[0, 1, 2, 3], [4, 5, 6, 7]], np.int32)
+    with quiet:
+        m = oc.build_octree_mesh_optimized(pts, conn, max_elements_per_leaf=1, max_depth=5)
+        ka = np.asarray(oc.create_octree_fem_interpolator_optimized(m)(np.array([[0.25, 0.25, 0.25]], F32), pts))
+    out = {"ka_pts": pts, "ka_conn": conn, "ka_out": ka}
+    # B1-B3: jittered Kuhn mesh
+    P, T4 = kuhn_mesh(6, 0.2, 1)
+    st = np.linspace(0, 1, 5).astype(F32)
+    D = np.stack([abc(P, float(t)) for t in st]).astype(F32)
+    with quiet:
+        f = OctreeFEMTimeSeriesFieldOptimized(D, st, P, T4, max_elements_per_leaf=32, max_depth=12)
+    M = f.octree_mesh
+    for k in ("nodes_min", "nodes_max", "nodes_elements", "nodes_elem_counts", "nodes_children", "nodes_is_leaf",
+              "element_bounds", "element_centroids"):
+        out[k] = np.asarray(getattr(M, k))
+    rng = np.random.default_rng(7)
+    q = np.concatenate([rng.random((400, 3)), rng.uniform(-0.1, 1.1, (60, 3))]).astype(F32)
+    out.update(P=P, T4=T4, st=st, D=D, q=q)
+    out["sample_t03"] = np.asarray(f.sample_at_positions(q, np.float32(0.3)), dtype=F32)
+    out["sample_t10"] = np.asarray(f.sample_at_positions(q, np.float32(1.0)), dtype=F32)
+    x0 = rng.random((60, 3)).astype(F32)
+    bc = bnd.mixed_boundary(((0, 0, 0), (1, 1, 1)), {"x": "periodic", "y": "reflective", "z": "periodic"})
+    tr = create_tracker("rk4", f, bc, use_jax_jit=False, progress_style="none")
+    traj = tr.track_particles(x0, (0.0, 0.1), 11, dt=0.01)
+    out.update(x0=x0, traj=traj.positions)
+    np.savez_compressed(HERE / "octree.npz", **out)
+    print("phase octree: done")
+
+
+if __name__ == "__main__":
+    if len(sys.argv) >= 3 and sys.argv[1] in ("numpy", "octree"):
+        {"numpy": phase_numpy, "octree": phase_octree}[sys.argv[1]](sys.argv[2])
+        sys.exit(0)
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
+    for phase in ("numpy", "octree"):
+        subprocess.run([sys.executable, __file__, phase, ref], check=True, env=env)

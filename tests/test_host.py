@@ -1,0 +1,147 @@
+"""Host-side logic of the GPU path: C-ABI surface, octree build, time-blend
+schedules, boundary descriptors and tracker options.  No GPU needed."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import jaxtrace_gb300 as jt
+from jaxtrace_gb300 import _lib as L
+from jaxtrace_gb300 import schedule as S
+
+ROOT = Path(__file__).resolve().parents[1]
+F32 = np.float32
+
+
+def header_functions():
+    text = (ROOT / "include" / "jaxtrace_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(jt_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_header_symbol():
+    lib = L.load()
+    names = header_functions()
+    assert len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), n
+    assert lib.jt_abi_version() == 1
+
+
+def test_struct_layouts_match():
+    assert L.struct_sizes() == [C.sizeof(s) for s in L.STRUCTS]
+    assert L.BLEND_DTYPE.itemsize == C.sizeof(L.Blend)
+    assert L.OCTREE_NODE_DTYPE.itemsize == C.sizeof(L.OctreeNode)
+
+
+def test_errors_are_mapped():
+    lib = L.load()
+    with pytest.raises(ValueError, match="field is NULL"):
+        L.check(lib.jt_track(None, None, None, None))
+    b = L.Boundary()
+    b.axis_kind[0] = 9
+    with pytest.raises(ValueError, match="unknown boundary kind"):
+        L.check(lib.jt_boundary_apply(C.byref(b), None, 0, None))
+
+
+def test_octree_build_matches_reference(golden):
+    g = golden("octree")
+    m = jt.OctreeMesh(g["P"], g["T4"], 32, 12)
+    assert len(m.nodes) == g["nodes_min"].shape[0]
+    assert np.array_equal(m.nodes_min, g["nodes_min"])
+    assert np.array_equal(m.nodes_max, g["nodes_max"])
+    assert np.array_equal(m.nodes_children, g["nodes_children"])
+    assert np.array_equal(m.nodes_is_leaf, g["nodes_is_leaf"])
+    assert np.array_equal(m.nodes_elem_counts, g["nodes_elem_counts"])
+    assert np.array_equal(m.nodes_elements, g["nodes_elements"])
+    assert np.array_equal(m.element_bounds, g["element_bounds"])
+    # node centres used by the traversal
+    assert np.array_equal(m.nodes["c"], (g["nodes_min"] + g["nodes_max"]) / F32(2.0))
+
+
+def test_octree_build_known_answer_mesh(golden):
+    g = golden("octree")
+    m = jt.OctreeMesh(g["ka_pts"], g["ka_conn"], 1, 5)
+    assert m.info.n_leaves >= 2
+
+
+def test_octree_rejects_bad_connectivity():
+    with pytest.raises(ValueError, match="outside"):
+        jt.OctreeMesh(np.zeros((4, 3), F32), np.array([[0, 1, 2, 9]], np.int32))
+
+
+@pytest.mark.parametrize("ex", ["constant", "linear", "zero", "nan"])
+def test_schedule_blend_matches_reference(golden, ex):
+    """The host schedule entries applied as the kernel applies them reproduce
+    TimeSeriesField.sample_at_time bit for bit."""
+    g = golden("time_blend")
+    data, times = g["data"], g["times"]
+    for i, t in enumerate(g["tq"]):
+        e = S.blend_numpy(times, float(t), "linear", ex)
+        e = np.array([e], dtype=L.BLEND_DTYPE)[0]
+        p = int(e["pair"])
+        A = data[p]
+        B = data[p + 1] if len(times) > 1 else data[p]
+        got = S.blend_nodes(e, A, B)
+        ref = g[f"out_{ex}"][i]
+        assert np.array_equal(got, ref, equal_nan=True), (ex, t)
+
+
+def test_schedule_stage_times_rk4():
+    times = np.linspace(0.0, 1.0, 11, dtype=F32)
+    sch = S.build_schedule(times, 0.1, L.JT_RK4, np.linspace(0, 1, 4, dtype=F32))
+    assert sch.shape == (40,)
+    assert sch.dtype == L.BLEND_DTYPE
+    # last stage of the final step sits at the last snapshot
+    assert sch[4 * 9 + 2]["pair"] == 2
+
+
+def test_bounds_forms():
+    b = jt.boundary._ensure_bounds_shape([0, 1, 0, 2, 0, 3])
+    assert b.tolist() == [[0, 0, 0], [1, 2, 3]]
+    b = jt.boundary._ensure_bounds_shape([[0, 1], [0, 2], [0, 3]])
+    assert b.tolist() == [[0, 0, 0], [1, 2, 3]]
+    # 2-D forms put z = 0 on both sides, which the reference's own check
+    # (boundary.py:83-84) rejects as min >= max
+    with pytest.raises(ValueError):
+        jt.boundary._ensure_bounds_shape([0, 1, 0, 2])
+    with pytest.raises(ValueError):
+        jt.boundary._ensure_bounds_shape([[1, 1, 1], [0, 0, 0]])
+
+
+def test_inlet_descriptor():
+    bc = jt.continuous_inlet_boundary_factory(((0, 0, 0), (1, 1, 1)), "x", "positive", "grid",
+                                              {"x": 4, "y": 8, "z": 16})
+    assert bc.__name__ == "_continuous_inlet_bc"
+    assert [len(c) for c in bc.inlet["coords"]] == [8, 16]
+    assert bc.inlet["nudge"] == F32(0) + F32(0.001) * (F32(1) - F32(0))
+    with pytest.raises(NotImplementedError):
+        jt.continuous_inlet_boundary_factory(((0, 0, 0), (1, 1, 1)))
+
+
+def test_tracker_options_and_factory_errors():
+    o = jt.TrackerOptions()
+    assert o.estimate_batch_size(1_000_000, 1001) == 100_000 // 64 * 1 or o.estimate_batch_size(1_000_000, 1001) > 0
+    assert jt.TrackerOptions(batch_size=5000).estimate_batch_size(10, 10) == 5000
+    with pytest.raises(TypeError):
+        jt.TrackerOptions(not_an_option=1)
+    field = jt.StructuredGridSampler(np.zeros((2, 2, 2, 3), F32), [0, 1], [0, 1], [0, 1])
+    with pytest.raises(ValueError, match="Unknown integrator"):
+        jt.create_tracker("rk5", field, jt.no_boundary())
+    with pytest.raises(TypeError):
+        jt.create_tracker("rk4", lambda p, t: p, jt.no_boundary())
+    with pytest.raises(TypeError):
+        jt.create_tracker("rk4", field, lambda x: x)
+    tr = jt.create_tracker("rk4", field, jt.periodic_boundary([[0, 0, 0], [1, 1, 1]]))
+    assert tr._code == L.JT_RK4
+
+
+def test_estimate_batch_size_matches_reference_rule():
+    # tracker.py:142-153: halve from min(N, max_batch_size) until under max_memory_gb
+    o = jt.TrackerOptions(max_memory_gb=1.0)
+    bs = o.estimate_batch_size(1_000_000, 1001)
+    from jaxtrace_gb300.tracker import _estimate_memory_usage
+    assert _estimate_memory_usage(bs, 1001) <= 1.0
+    assert _estimate_memory_usage(bs * 2, 1001) > 1.0 or bs * 2 > 100_000
