@@ -58,7 +58,8 @@ struct GridField {
         grid_axis<EXACT>(p.y, F.origin[1], F.spacing[1], F.ny, F.bounds_mode, F.valid_hi[1], j0, j1, wy, vy, flags);
         grid_axis<EXACT>(p.z, F.origin[2], F.spacing[2], F.nz, F.bounds_mode, F.valid_hi[2], k0, k1, wz, vz, flags);
 
-        const int64_t base = (int64_t)e.pair * F.pair_stride;
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        const int64_t base = (int64_t)pr * F.pair_stride;
         const int ny = F.ny, nz = F.nz;
         const int64_t r00 = ((int64_t)i0 * ny + j0) * nz, r10 = ((int64_t)i1 * ny + j0) * nz;
         const int64_t r01 = ((int64_t)i0 * ny + j1) * nz, r11 = ((int64_t)i1 * ny + j1) * nz;

@@ -33,7 +33,7 @@ struct MeshField {
     static MeshField create(const jt_mesh_field& d, int) { return MeshField{d}; }
 
     __device__ __forceinline__ V3 node_value(int node, const jt_blend& e) const {
-        const int64_t base = (int64_t)e.pair * F.pair_stride;
+        const int64_t base = (int64_t)min(max(e.pair, 0), F.n_pairs - 1) * F.pair_stride;
         return blend<EXACT, STORE>(load_pair<STORE>(F.pairs, base + node), e);
     }
 

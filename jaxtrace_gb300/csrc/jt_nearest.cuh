@@ -19,7 +19,7 @@ struct NearestField {
 
     __device__ __forceinline__ V3 operator()(const V3& q, const jt_blend& e, int& flags) const {
         typedef Ar<EXACT> A;
-        const int64_t base = (int64_t)e.pair * F.pair_stride;
+        const int64_t base = (int64_t)min(max(e.pair, 0), F.n_pairs - 1) * F.pair_stride;
         if (q.x != q.x || q.y != q.y || q.z != q.z)  // all distances NaN: argmin is 0
             return blend<EXACT, STORE>(load_pair<STORE>(F.pairs, base), e);
         const float qq[3] = {q.x, q.y, q.z};
