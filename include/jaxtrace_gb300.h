@@ -231,7 +231,9 @@ typedef struct {
     int32_t row_base;       /* row of traj[0] for this launch                 */
     int32_t n_rows;         /* rows held by traj/vel for this launch          */
     int32_t* status;        /* device status word or NULL                     */
-    int32_t pad;
+    const int32_t* ids;     /* device (N): particle index of slot i, used as the
+                               row index of traj/vel writes after a locality
+                               sort, or NULL (slot i is particle i)           */
 } jt_track_params;
 
 /* ABI / diagnostics */
@@ -272,6 +274,33 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
                        int32_t integrator, int32_t arith, float dt,
                        const float* dt_per_particle, const float* x_in,
                        float* x_out, int32_t n, int32_t* status, void* stream);
+
+/* ---- locality sort ------------------------------------------------------ */
+/* Morton cell grid of the sort: cell = clamp(floor((x-origin)*inv_cell), 0, 2^bits-1). */
+typedef struct {
+    float origin[3];
+    float inv_cell[3];
+    int32_t bits;            /* 1..7 bits per axis                           */
+    int32_t pad;
+} jt_sort_grid;
+
+/* Bytes of device workspace jt_cell_sort needs (0 for invalid arguments). */
+size_t jt_cell_sort_workspace_bytes(int32_t n, int32_t bits);
+
+/* Reorder particles by Morton cell (counting sort) so that warps gather from
+ * few cache lines.  No reference counterpart changes meaning: the reference
+ * keeps particles in input order (tracker.py:428-446); particle results do
+ * not depend on their slot, and ids_out (slot -> original particle) lets
+ * jt_unpermute restore the input order.  pos_in/pos_out: device (N,3);
+ * comp_in/comp_out: optional Kahan terms; ids_in: device (N) or NULL for the
+ * identity; workspace: caller-allocated device memory of at least
+ * jt_cell_sort_workspace_bytes(n, bits).  Not in place. */
+int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_in, const float* comp_in,
+                 const int32_t* ids_in, float* pos_out, float* comp_out, int32_t* ids_out,
+                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* pos_out[ids[i]] = pos_sorted[i]: back to the caller's particle order. */
+int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* pos_out, void* stream);
 
 /* ---- octree build (host) ------------------------------------------------ */
 typedef struct {

@@ -87,7 +87,11 @@ class TrackParams(C.Structure):
                 ("schedule", vp), ("schedule_stride", i64), ("ens_offsets", vp), ("n_ens", i32),
                 ("pad_e", i32), ("pos", vp), ("comp", vp), ("traj", vp), ("vel", vp),
                 ("record_every", i32), ("record_compact", i32), ("row_base", i32), ("n_rows", i32),
-                ("status", vp), ("pad", i32)]
+                ("status", vp), ("ids", vp)]
+
+
+class SortGrid(C.Structure):
+    _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("bits", i32), ("pad", i32)]
 
 
 class OctreeInfo(C.Structure):
@@ -95,7 +99,7 @@ class OctreeInfo(C.Structure):
                 ("n_leaves", i32), ("pad", i32)]
 
 
-STRUCTS = [Blend, GridField, OctreeNode, MeshField, NearestField, Field, Boundary, TrackParams]
+STRUCTS = [Blend, GridField, OctreeNode, MeshField, NearestField, Field, Boundary, TrackParams, SortGrid]
 
 
 class JTError(RuntimeError):
@@ -132,6 +136,9 @@ def load(build_if_missing: bool = True):
         "jt_octree_build": (i32, [vp, i32, vp, i32, i32, i32, P(vp), P(OctreeInfo)]),
         "jt_octree_fetch": (i32, [vp, vp, vp, vp, vp, vp]),
         "jt_octree_free": (None, [vp]),
+        "jt_cell_sort_workspace_bytes": (C.c_size_t, [i32, i32]),
+        "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),
+        "jt_unpermute": (i32, [i32, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

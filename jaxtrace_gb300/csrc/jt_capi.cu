@@ -124,7 +124,8 @@ extern "C" int jt_struct_sizes(int64_t* out, int32_t n) {
     const int64_t s[] = {(int64_t)sizeof(jt_blend),         (int64_t)sizeof(jt_grid_field),
                          (int64_t)sizeof(jt_octree_node),   (int64_t)sizeof(jt_mesh_field),
                          (int64_t)sizeof(jt_nearest_field), (int64_t)sizeof(jt_field),
-                         (int64_t)sizeof(jt_boundary),      (int64_t)sizeof(jt_track_params)};
+                         (int64_t)sizeof(jt_boundary),      (int64_t)sizeof(jt_track_params),
+                         (int64_t)sizeof(jt_sort_grid)};
     const int k = (int)(sizeof(s) / sizeof(s[0]));
     if (out == nullptr || n < k) return set_error(JT_ERR_INVALID, "jt_struct_sizes needs room for %d values", k);
     for (int i = 0; i < k; ++i) out[i] = s[i];

@@ -368,12 +368,13 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
             if (cnt % P.record_every == 0) {
                 const int row = (P.record_compact ? cnt / P.record_every : cnt) - P.row_base;
                 if (row >= 0 && row < P.n_rows) {
-                    float* o = P.traj + ((int64_t)row * n + i) * 3;
+                    const int64_t id = P.ids != nullptr ? (int64_t)P.ids[i] : (int64_t)i;
+                    float* o = P.traj + ((int64_t)row * n + id) * 3;
                     o[0] = x.x; o[1] = x.y; o[2] = x.z;
                     if (P.vel != nullptr) {
                         const jt_blend er = e[3];
                         V3 v = f(x, er, flags);
-                        float* ov = P.vel + ((int64_t)row * n + i) * 3;
+                        float* ov = P.vel + ((int64_t)row * n + id) * 3;
                         ov[0] = v.x; ov[1] = v.y; ov[2] = v.z;
                     }
                 }

@@ -1,0 +1,175 @@
+// Particle reordering by cell for gather locality (a counting sort on Morton
+// cell keys).  Particles are independent, so their slot order never changes
+// a result; sorting only makes the 32 particles of a warp fall into a few
+// neighbouring cells, so each corner gather touches a few cache lines
+// instead of 32.  The slot -> particle map travels with the positions and is
+// undone once at the end (jt_unpermute).
+#include <stdint.h>
+
+#include "jt_internal.h"
+#include "jt_kernels.cuh"
+
+namespace jt {
+
+constexpr int kScanBlock = 1024;            // threads of the scan kernels
+constexpr int kScanItems = 2 * kScanBlock;  // bins per scan block
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000ff;
+    v = (v | (v << 8)) & 0x0300f00f;
+    v = (v | (v << 4)) & 0x030c30c3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+
+__global__ void __launch_bounds__(kBlock) k_cell_keys(jt_sort_grid g, const float* __restrict__ pos, int n,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int lim = (1 << g.bits) - 1;
+    uint32_t c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float f = floorf((pos[3 * (int64_t)i + a] - g.origin[a]) * g.inv_cell[a]);
+        int ci = (f != f) ? 0 : (f < 0.0f ? 0 : (f > (float)lim ? lim : (int)f));
+        c[a] = (uint32_t)ci;
+    }
+    const uint32_t key = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+    keys[i] = key;
+    atomicAdd(hist + key, 1u);
+}
+
+// Exclusive scan, phase 1: each block scans kScanItems bins in shared memory
+// (Hillis-Steele over the per-thread pair sums) and records its total.
+__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(uint32_t* __restrict__ data, int64_t n,
+                                                            uint32_t* __restrict__ sums) {
+    __shared__ uint32_t s[kScanBlock];
+    const int64_t base = (int64_t)blockIdx.x * kScanItems;
+    const int t = threadIdx.x;
+    const int64_t i0 = base + 2 * t, i1 = i0 + 1;
+    const uint32_t a = i0 < n ? data[i0] : 0u, b = i1 < n ? data[i1] : 0u;
+    s[t] = a + b;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        const uint32_t v = t >= off ? s[t - off] : 0u;
+        __syncthreads();
+        s[t] += v;
+        __syncthreads();
+    }
+    const uint32_t excl = s[t] - (a + b);
+    if (i0 < n) data[i0] = excl;
+    if (i1 < n) data[i1] = excl + a;
+    if (t == kScanBlock - 1) sums[blockIdx.x] = s[t];
+}
+
+// Phase 2: add the scanned block totals (sums holds an exclusive scan).
+__global__ void __launch_bounds__(kScanBlock) k_scan_add(uint32_t* __restrict__ data, int64_t n,
+                                                         const uint32_t* __restrict__ sums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanItems;
+    const uint32_t add = sums[blockIdx.x];
+    for (int k = threadIdx.x; k < kScanItems; k += kScanBlock) {
+        const int64_t i = base + k;
+        if (i < n) data[i] += add;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter(int n, const uint32_t* __restrict__ keys,
+                                                    uint32_t* __restrict__ cursor, const float* __restrict__ pos_in,
+                                                    const float* __restrict__ comp_in, const int32_t* __restrict__ ids_in,
+                                                    float* __restrict__ pos_out, float* __restrict__ comp_out,
+                                                    int32_t* __restrict__ ids_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t slot = atomicAdd(cursor + keys[i], 1u);
+    if (slot >= (uint32_t)n) return;  // impossible for a consistent histogram; never write out of range
+    const int64_t s3 = 3 * (int64_t)slot, i3 = 3 * (int64_t)i;
+    pos_out[s3] = pos_in[i3];
+    pos_out[s3 + 1] = pos_in[i3 + 1];
+    pos_out[s3 + 2] = pos_in[i3 + 2];
+    if (comp_in != nullptr) {
+        comp_out[s3] = comp_in[i3];
+        comp_out[s3 + 1] = comp_in[i3 + 1];
+        comp_out[s3 + 2] = comp_in[i3 + 2];
+    }
+    ids_out[slot] = ids_in != nullptr ? ids_in[i] : i;
+}
+
+__global__ void __launch_bounds__(kBlock) k_unpermute(int n, const float* __restrict__ src,
+                                                      const int32_t* __restrict__ ids, float* __restrict__ dst) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t d = ids[i];
+    if (d < 0 || d >= n) return;
+    dst[3 * (int64_t)d] = src[3 * (int64_t)i];
+    dst[3 * (int64_t)d + 1] = src[3 * (int64_t)i + 1];
+    dst[3 * (int64_t)d + 2] = src[3 * (int64_t)i + 2];
+}
+
+static int64_t n_bins(int bits) { return (int64_t)1 << (3 * bits); }
+
+static int64_t scan_blocks(int64_t n) { return (n + kScanItems - 1) / kScanItems; }
+
+// Workspace layout (bytes, 256-aligned pieces): hist/cursor [bins], keys [n],
+// block sums [scan_blocks(bins)], block-sum sums [1 block].
+size_t sort_workspace_bytes(int32_t n, int32_t bits) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const int64_t bins = n_bins(bits);
+    return al(bins * 4) + al((size_t)n * 4) + al(scan_blocks(bins) * 4) + al(4 * kScanItems);
+}
+
+int cell_sort(const jt_sort_grid& g, int32_t n, const float* pos_in, const float* comp_in, const int32_t* ids_in,
+              float* pos_out, float* comp_out, int32_t* ids_out, void* ws, cudaStream_t st) {
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const int64_t bins = n_bins(g.bits);
+    const int64_t nb = scan_blocks(bins);
+    char* w = static_cast<char*>(ws);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(w);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(w + al(bins * 4));
+    uint32_t* sums = reinterpret_cast<uint32_t*>(w + al(bins * 4) + al((size_t)n * 4));
+    uint32_t* sums2 = reinterpret_cast<uint32_t*>(w + al(bins * 4) + al((size_t)n * 4) + al(nb * 4));
+    cudaError_t e = cudaMemsetAsync(hist, 0, bins * 4, st);
+    if (e != cudaSuccess) return cuda_status(e, "cell sort memset");
+    k_cell_keys<<<grid_blocks(n), kBlock, 0, st>>>(g, pos_in, n, keys, hist);
+    k_scan_blocks<<<(unsigned)nb, kScanBlock, 0, st>>>(hist, bins, sums);
+    k_scan_blocks<<<1, kScanBlock, 0, st>>>(sums, nb, sums2);  // nb <= kScanItems (checked by the caller)
+    k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(hist, bins, sums);
+    k_scatter<<<grid_blocks(n), kBlock, 0, st>>>(n, keys, hist, pos_in, comp_in, ids_in, pos_out, comp_out, ids_out);
+    return cuda_status(cudaGetLastError(), "cell sort launch");
+}
+
+}  // namespace jt
+
+using namespace jt;
+
+extern "C" size_t jt_cell_sort_workspace_bytes(int32_t n, int32_t bits) {
+    if (n < 0 || bits < 1 || bits > 7) return 0;
+    return sort_workspace_bytes(n, bits);
+}
+
+extern "C" int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_in, const float* comp_in,
+                            const int32_t* ids_in, float* pos_out, float* comp_out, int32_t* ids_out, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+    if (g == nullptr) return set_error(JT_ERR_INVALID, "sort grid is NULL");
+    if (g->bits < 1 || g->bits > 7) return set_error(JT_ERR_INVALID, "bits must be 1..7 (got %d)", g->bits);
+    if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
+    if (n == 0) return JT_OK;
+    if (pos_in == nullptr || pos_out == nullptr || ids_out == nullptr || workspace == nullptr)
+        return set_error(JT_ERR_INVALID, "pos_in, pos_out, ids_out and workspace are required");
+    if ((comp_in == nullptr) != (comp_out == nullptr))
+        return set_error(JT_ERR_INVALID, "comp_in and comp_out go together");
+    if (pos_in == pos_out || ids_in == ids_out) return set_error(JT_ERR_INVALID, "cell sort cannot run in place");
+    if (workspace_bytes < sort_workspace_bytes(n, g->bits))
+        return set_error(JT_ERR_NOMEM, "workspace of %zu bytes < %zu needed", workspace_bytes,
+                         sort_workspace_bytes(n, g->bits));
+    return cell_sort(*g, n, pos_in, comp_in, ids_in, pos_out, comp_out, ids_out, workspace, (cudaStream_t)stream);
+}
+
+extern "C" int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* pos_out, void* stream) {
+    if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
+    if (n == 0) return JT_OK;
+    if (pos_sorted == nullptr || ids == nullptr || pos_out == nullptr || pos_sorted == pos_out)
+        return set_error(JT_ERR_INVALID, "pos_sorted, ids and a distinct pos_out are required");
+    k_unpermute<<<grid_blocks(n), kBlock, 0, (cudaStream_t)stream>>>(n, pos_sorted, ids, pos_out);
+    return cuda_status(cudaGetLastError(), "unpermute launch");
+}

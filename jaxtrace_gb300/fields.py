@@ -138,6 +138,17 @@ class _DeviceField:
     def blend_at(self, t) -> np.ndarray:
         return single_blend(self.times, t, **self._blend_args())
 
+    def sort_grid(self, bits: int = 7):
+        """Morton cell grid (2^bits per axis over the field's bounding box)
+        used to reorder particles for gather locality."""
+        lo, hi = (np.asarray(v, dtype=np.float64) for v in self.get_spatial_bounds())
+        ext = hi - lo
+        g = L.SortGrid()
+        g.origin[:] = [float(v) for v in lo]
+        g.inv_cell[:] = [float((1 << bits) / e) if e > 0 else 0.0 for e in ext]
+        g.bits = bits
+        return g
+
     def get_time_bounds(self) -> Tuple[float, float]:
         return float(self.t_min), float(self.t_max)
 
@@ -192,6 +203,10 @@ class _DeviceField:
         form = int(e["form"])
         if form == L.JT_BLEND_WEIGHTED:
             v = A * float(e["wa"]) + B * float(e["wb"])
+        elif form == L.JT_BLEND_SAME_A:
+            v = A * float(e["wa"]) + A * float(e["wb"])
+        elif form == L.JT_BLEND_SAME_B:
+            v = B * float(e["wa"]) + B * float(e["wb"])
         else:
             A = A * float(e["sa"])
             B = B * float(e["sb"])

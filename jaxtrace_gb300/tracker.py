@@ -48,6 +48,8 @@ class TrackerOptions:
                        snapshot storage always runs 'compensated'
     device_memory_gb   device budget of one trajectory slab
     time_chunk         steps per kernel launch (None: as many as fit)
+    sort_every         re-sort particles by cell every k steps for gather
+                       locality (None: 100 from 2^18 particles up, 0: never)
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -73,6 +75,7 @@ class TrackerOptions:
     precision: str = "exact"
     device_memory_gb: float = 32.0
     time_chunk: Optional[int] = None
+    sort_every: Optional[int] = None
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
         """tracker.py:142-153."""
@@ -224,6 +227,22 @@ class ParticleTracker:
         p.record_every = 1
         return p
 
+    def _sort_every(self, n: int) -> int:
+        se = self.options.sort_every
+        if se is None:
+            return 100 if n >= (1 << 18) else 0
+        return max(int(se), 0)
+
+    def _engine(self, pos, times, dt, sched_dev=None, status=None, comp=None):
+        import torch
+        if sched_dev is None:
+            sched_dev = torch.from_numpy(self._schedule(times, dt).view(np.int32).reshape(-1, 8)).cuda()
+        if status is None:
+            status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if comp is None and self._arith() == L.JT_ARITH_COMPENSATED:
+            comp = torch.zeros_like(pos)
+        return _Engine(self, pos, len(times) - 1, dt, sched_dev, status, comp, self._sort_every(pos.shape[0]))
+
     def _run(self, pos, times, dt, k, compact, n_rows, positions, velocities) -> int:
         """Advance ``pos`` (device, (N,3)) through all steps, filling rows 1.. of the outputs."""
         import torch
@@ -231,78 +250,50 @@ class ParticleTracker:
         n_steps = len(times) - 1
         if n_steps <= 0:
             return 0
-        sched = self._schedule(times, dt)
-        sched_dev = torch.from_numpy(sched.view(np.int32).reshape(-1, 8)).cuda()
-        status = torch.zeros(1, dtype=torch.int32, device="cuda")
-        comp = torch.zeros_like(pos) if self._arith() == L.JT_ARITH_COMPENSATED else None
-        field_c = self._field.jt_field()
-        bc_c = self._bc.jt_boundary()
-        p = self.make_params(pos, dt, n_steps, sched_dev, status, comp)
+        eng = self._engine(pos, times, dt)
         record = n_rows > 1 and not self.options.record_final_only
         row_bytes = n * 12 * (2 if velocities is not None else 1)
         budget_rows = max(1, int(self.options.device_memory_gb * 1024 ** 3 // max(row_bytes, 1)))
-        # steps per chunk: bounded by rows that fit in the slab
-        if record:
-            chunk = budget_rows * (k if compact else 1) if compact else budget_rows
-            chunk = max(1, min(chunk, n_steps))
-        else:
-            chunk = n_steps
+        chunk = n_steps
+        if record:  # steps per launch bounded by the rows that fit in one slab
+            chunk = max(1, min(budget_rows * (k if compact else 1), n_steps))
         if self.options.time_chunk:
             chunk = max(1, min(chunk, int(self.options.time_chunk)))
-        lib = L.load()
-        stream = L.stream_ptr()
-        n_chunks = 0
-        s = 0
         cb = self.options.progress_callback
+        s = 0
         while s < n_steps:
             e = min(s + chunk, n_steps)
-            p.step_begin, p.step_end = s, e
             slab = vslab = None
+            rec = None
             if record:
-                # rows written by steps s..e-1: counts c in (s, e]
-                if compact:
-                    r0, r1 = s // k + 1, e // k
-                else:
-                    r0, r1 = s + 1, e
+                # rows written by steps s..e-1 are the counts c in (s, e]
+                r0, r1 = (s // k + 1, e // k) if compact else (s + 1, e)
                 nr = max(r1 - r0 + 1, 0)
                 if nr > 0:
                     slab = torch.zeros((nr, n, 3), dtype=torch.float32, device="cuda")
                     if velocities is not None:
                         vslab = torch.zeros_like(slab)
-                p.traj = slab.data_ptr() if slab is not None else None
-                p.vel = vslab.data_ptr() if vslab is not None else None
-                p.record_every = k
-                p.record_compact = int(compact)
-                p.row_base = r0
-                p.n_rows = nr
-            L.check(lib.jt_track(C.byref(field_c), C.byref(bc_c), C.byref(p), stream))
+                rec = (slab, vslab, k, compact, r0, nr)
+            eng.advance(s, e, rec)
             if slab is not None:
                 positions[r0:r0 + nr] = slab.cpu().numpy()
                 if vslab is not None:
                     velocities[r0:r0 + nr] = vslab.cpu().numpy()
-            n_chunks += 1
             s = e
             if cb is not None:
                 cb(s / n_steps)
-        self.last_status = int(status.item())
-        return n_chunks
+        eng.finish()
+        self.last_status = int(eng.status.item())
+        return eng.launches
 
     def track_device(self, pos, times, dt, status=None, comp=None, sched_dev=None):
-        """Advance device positions in place with no recording (benchmark and
-        ensemble entry).  ``times`` is the float32 step grid."""
-        import torch
-        n_steps = len(times) - 1
-        if sched_dev is None:
-            sched_dev = torch.from_numpy(self._schedule(times, dt).view(np.int32).reshape(-1, 8)).cuda()
-        if status is None:
-            status = torch.zeros(1, dtype=torch.int32, device="cuda")
-        if comp is None and self._arith() == L.JT_ARITH_COMPENSATED:
-            comp = torch.zeros_like(pos)
-        p = self.make_params(pos, dt, n_steps, sched_dev, status, comp)
-        p.step_begin, p.step_end = 0, n_steps
-        L.check(L.load().jt_track(C.byref(self._field.jt_field()), C.byref(self._bc.jt_boundary()), C.byref(p),
-                                  L.stream_ptr()))
-        return pos
+        """Advance device positions (N,3) in place through every step of the
+        float32 time grid ``times`` without recording (benchmark and ensemble
+        entry).  Returns the number of tracking-kernel launches."""
+        eng = self._engine(pos, times, dt, sched_dev, status, comp)
+        eng.advance(0, len(times) - 1, None)
+        eng.finish()
+        return eng.launches
 
     # ------------------------------------------------------------------
     def validate_configuration(self) -> Dict[str, Any]:
@@ -347,6 +338,80 @@ class ParticleTracker:
         est = n_particles * n_timesteps * per
         return {"success": True, "estimated_runtime_seconds": est, "time_per_particle_step": per,
                 "calibration_time": el, "calibration_particles": calibration_particles}
+
+
+class _Engine:
+    """Buffers of one run: positions in slot order, optional Kahan terms, the
+    slot -> particle map of the locality sort and the sort workspace."""
+
+    def __init__(self, tracker, pos, n_steps, dt, sched_dev, status, comp, sort_every):
+        import torch
+        self.t, self.out, self.n_steps = tracker, pos, n_steps
+        self.status, self.sched = status, sched_dev
+        self.n = pos.shape[0]
+        self.sort_every = sort_every
+        self.launches = 0
+        self.field_c = tracker._field.jt_field()
+        self.bc_c = tracker._bc.jt_boundary()
+        self.lib = L.load()
+        self.stream = L.stream_ptr()
+        self.pos, self.comp, self.ids = pos, comp, None
+        if sort_every > 0 and self.n > 0:
+            self.grid = tracker._field.sort_grid()
+            self.pos = torch.empty_like(pos)
+            self.pos_alt = torch.empty_like(pos)
+            self.comp_alt = torch.empty_like(comp) if comp is not None else None
+            self.ids = torch.empty(self.n, dtype=torch.int32, device=pos.device)
+            self.ids_alt = torch.empty_like(self.ids)
+            ws = int(self.lib.jt_cell_sort_workspace_bytes(self.n, self.grid.bits))
+            self.ws = torch.empty(ws, dtype=torch.uint8, device=pos.device)
+            self._sort(first=True)
+        self.p = tracker.make_params(self.pos, dt, n_steps, sched_dev, status, self.comp)
+
+    def _sort(self, first=False):
+        src_pos = self.out if first else self.pos
+        dst_pos = self.pos if first else self.pos_alt
+        src_ids = None if first else self.ids
+        dst_ids = self.ids if first else self.ids_alt
+        comp_dst = None
+        if self.comp is not None:
+            comp_dst = self.comp_alt
+        L.check(self.lib.jt_cell_sort(C.byref(self.grid), self.n, L.ptr(src_pos), L.ptr(self.comp), L.ptr(src_ids),
+                                      L.ptr(dst_pos), L.ptr(comp_dst), L.ptr(dst_ids), L.ptr(self.ws),
+                                      self.ws.numel(), self.stream))
+        if not first:
+            self.pos, self.pos_alt = self.pos_alt, self.pos
+            self.ids, self.ids_alt = self.ids_alt, self.ids
+        if self.comp is not None:
+            self.comp, self.comp_alt = self.comp_alt, self.comp
+
+    def advance(self, s, e, rec):
+        """Steps [s, e) with optional recording (slab, vslab, k, compact, row0, rows)."""
+        p = self.p
+        while s < e:
+            stop = e
+            if self.sort_every > 0:
+                if s > 0 and s % self.sort_every == 0:
+                    self._sort()
+                stop = min(e, (s // self.sort_every + 1) * self.sort_every)
+            p.pos = self.pos.data_ptr()
+            p.comp = self.comp.data_ptr() if self.comp is not None else None
+            p.ids = self.ids.data_ptr() if self.ids is not None else None
+            p.step_begin, p.step_end = s, stop
+            if rec is not None:
+                slab, vslab, k, compact, r0, nr = rec
+                p.traj = slab.data_ptr() if slab is not None else None
+                p.vel = vslab.data_ptr() if vslab is not None else None
+                p.record_every, p.record_compact, p.row_base, p.n_rows = k, int(compact), r0, nr
+            else:
+                p.traj = p.vel = None
+            L.check(self.lib.jt_track(C.byref(self.field_c), C.byref(self.bc_c), C.byref(p), self.stream))
+            self.launches += 1
+            s = stop
+
+    def finish(self):
+        if self.ids is not None:
+            L.check(self.lib.jt_unpermute(self.n, L.ptr(self.pos), L.ptr(self.ids), L.ptr(self.out), self.stream))
 
 
 def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:

@@ -194,3 +194,64 @@ def test_periodic_wrap_is_flagged():
     spec = oracle.GridSpec(V[None], np.zeros(1, F32), g, g, g, "periodic")
     ref, _ = oracle.sample(spec, np.array([[0.5, 0.5, -6.05359673500061e-09]], F32), 0.0)
     assert same(out, ref)
+
+
+# ---------------------------------------------------------------- locality sort
+def test_cell_sort_is_a_permutation_in_morton_order():
+    import ctypes as C
+    import torch
+    n = 100_003
+    x = torch.rand((n, 3), device="cuda")
+    g = L.SortGrid()
+    g.origin[:] = [0.0, 0.0, 0.0]
+    g.inv_cell[:] = [16.0, 16.0, 16.0]
+    g.bits = 4
+    lib = L.load()
+    ws = torch.empty(int(lib.jt_cell_sort_workspace_bytes(n, 4)), dtype=torch.uint8, device="cuda")
+    out = torch.empty_like(x)
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    L.check(lib.jt_cell_sort(C.byref(g), n, L.ptr(x), None, None, L.ptr(out), None, L.ptr(ids), L.ptr(ws),
+                             ws.numel(), L.stream_ptr()))
+    ids_h = ids.cpu().numpy()
+    assert np.array_equal(np.sort(ids_h), np.arange(n))
+    assert torch.equal(out, x[ids.long()])
+    c = np.clip(np.floor(out.cpu().numpy() * 16), 0, 15).astype(np.int64)
+
+    def spread(v):
+        r = np.zeros_like(v)
+        for b in range(4):
+            r |= ((v >> b) & 1) << (3 * b)
+        return r
+    key = spread(c[:, 0]) | (spread(c[:, 1]) << 1) | (spread(c[:, 2]) << 2)
+    assert np.all(np.diff(key) >= 0)
+    back = torch.empty_like(x)
+    L.check(lib.jt_unpermute(n, L.ptr(out), L.ptr(ids), L.ptr(back), L.stream_ptr()))
+    assert torch.equal(back, x)
+
+
+def test_sorted_tracking_is_bit_identical(golden):
+    g = golden("track_grid")
+    f = jt.StructuredTimeSeriesField(g["D"], g["st"], g["g"], g["g"], g["g"], "periodic")
+    bc = jt.periodic_boundary(((0, 0, 0), (1, 1, 1)))
+    ref = g["rk4_traj"]
+    tr = jt.create_tracker("rk4", f, bc, sort_every=4, record_velocities=True)
+    traj = tr.track_particles(g["x0"], (0.0, 0.3), 31, dt=0.01)
+    assert same(traj.positions, ref)
+    assert traj.metadata["time_chunks"] == 8
+    plain = jt.create_tracker("rk4", f, bc, sort_every=0, record_velocities=True).track_particles(
+        g["x0"], (0.0, 0.3), 31, dt=0.01)
+    assert same(traj.velocities, plain.velocities)
+
+
+def test_sorted_compensated_precision_matches_unsorted():
+    from jaxtrace_gb300 import workloads as W
+    c = W.precision_case(n=24, n_snap=8, seeds=(24, 24, 24), lattice=24, n_steps=200, dt=0.005)
+    g = c["grid"][0]
+    bc = jt.continuous_inlet_boundary_factory(W.UNIT, "x", "positive", "grid", c["concentrations"])
+    outs = []
+    for se in (0, 16):
+        f = jt.StructuredTimeSeriesField(c["data"], c["times"], g, g, g, "clamp", storage="bf16")
+        tr = jt.create_tracker("rk4", f, bc, record_final_only=True, sort_every=se)
+        outs.append(tr.track_particles(c["x0"], c["time_span"], c["n_timesteps"], dt=c["dt"]).positions[-1])
+    # FMA contraction is the same per particle whatever its slot
+    assert same(outs[0], outs[1])
