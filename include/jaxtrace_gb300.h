@@ -299,6 +299,28 @@ int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_in, const fl
                  const int32_t* ids_in, float* pos_out, float* comp_out, int32_t* ids_out,
                  void* workspace, size_t workspace_bytes, void* stream);
 
+/* Allocation-free jt_cell_sort.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they call in (an
+ * application that owns every device allocation through its own pool, or a
+ * time-critical loop where cudaMalloc/cudaFree and their device-wide
+ * synchronisation are not allowed): the scratch is a fixed array in the
+ * library's own device memory, so the call allocates nothing.
+ *   limits: n <= JT_NOALLOC_SORT_MAX_PARTICLES, bits <= JT_NOALLOC_SORT_MAX_BITS
+ *           (larger sizes return JT_ERR_INVALID); the array (about 9 MiB) is
+ *           held on every GPU that loads the library until the process exits.
+ *   set-up: the first call on a device looks up the array's device address
+ *           (cudaGetSymbolAddress) with that device current; make that first
+ *           call before any stream capture.
+ *   sharing: every call uses the same array, which keeps the last call's
+ *           contents (the call clears what it accumulates into); calls whose
+ *           work overlaps on the GPU race -- serialise them on one stream.
+ * Arguments as jt_cell_sort without the workspace. */
+#define JT_NOALLOC_SORT_MAX_PARTICLES (1 << 21)
+#define JT_NOALLOC_SORT_MAX_BITS 6
+int jt_cell_sort_noalloc(const jt_sort_grid* g, int32_t n, const float* pos_in, const float* comp_in,
+                         const int32_t* ids_in, float* pos_out, float* comp_out, int32_t* ids_out,
+                         void* stream);
+
 /* pos_out[ids[i]] = pos_sorted[i]: back to the caller's particle order. */
 int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* pos_out, void* stream);
 

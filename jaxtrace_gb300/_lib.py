@@ -139,6 +139,7 @@ def load(build_if_missing: bool = True):
         "jt_cell_sort_workspace_bytes": (C.c_size_t, [i32, i32]),
         "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),
         "jt_unpermute": (i32, [i32, vp, vp, vp, vp]),
+        "jt_cell_sort_noalloc": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -6,6 +6,8 @@
 // undone once at the end (jt_unpermute).
 #include <stdint.h>
 
+#include <mutex>
+
 #include "jt_internal.h"
 #include "jt_kernels.cuh"
 
@@ -163,6 +165,83 @@ extern "C" int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_i
         return set_error(JT_ERR_NOMEM, "workspace of %zu bytes < %zu needed", workspace_bytes,
                          sort_workspace_bytes(n, g->bits));
     return cell_sort(*g, n, pos_in, comp_in, ids_in, pos_out, comp_out, ids_out, workspace, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free cell sort.
+//
+// Some callers cannot allocate device memory at the moment they call this
+// library: a host application that owns all device memory through its own
+// pool and lends the library nothing but its particle buffers, or a
+// time-critical loop in which a cudaMalloc or cudaFree (both may synchronise
+// the whole device) is not allowed.  jt_cell_sort_noalloc serves them: its
+// scratch is one fixed-size array in the library's own device memory, sized
+// for JT_NOALLOC_SORT_MAX_PARTICLES particles at up to
+// JT_NOALLOC_SORT_MAX_BITS bits per axis (about 9 MiB, held on every GPU that
+// loads the library until the process exits).
+namespace {
+
+constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+constexpr size_t sort_bytes_c(int64_t n, int bits) {
+    return align256((size_t)(((int64_t)1 << (3 * bits)) * 4)) + align256((size_t)n * 4) +
+           align256((size_t)((((int64_t)1 << (3 * bits)) + jt::kScanItems - 1) / jt::kScanItems) * 4) +
+           align256((size_t)4 * jt::kScanItems);
+}
+
+constexpr size_t kNoAllocBytes = sort_bytes_c(JT_NOALLOC_SORT_MAX_PARTICLES, JT_NOALLOC_SORT_MAX_BITS);
+
+// The scratch itself.  In host code this name is only a stand-in for the
+// device array; the kernels get the device address obtained below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+static void* g_noalloc_addr[kMaxDevices];
+static std::mutex g_noalloc_mu;
+
+// Device address of the scratch on the current device, looked up once per
+// device (with that device current) and cached.
+int noalloc_scratch(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return jt::cuda_status(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return jt::set_error(JT_ERR_UNSUPPORTED, "device ordinal %d >= %d", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_addr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return jt::cuda_status(e, "cudaGetSymbolAddress of the no-alloc sort scratch");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return JT_OK;
+}
+
+}  // namespace
+
+extern "C" int jt_cell_sort_noalloc(const jt_sort_grid* g, int32_t n, const float* pos_in, const float* comp_in,
+                                    const int32_t* ids_in, float* pos_out, float* comp_out, int32_t* ids_out,
+                                    void* stream) {
+    if (g == nullptr) return set_error(JT_ERR_INVALID, "sort grid is NULL");
+    if (g->bits < 1 || g->bits > JT_NOALLOC_SORT_MAX_BITS)
+        return set_error(JT_ERR_INVALID, "no-alloc sort takes 1..%d bits per axis (got %d)", JT_NOALLOC_SORT_MAX_BITS,
+                         g->bits);
+    if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
+    if (n > JT_NOALLOC_SORT_MAX_PARTICLES)
+        return set_error(JT_ERR_INVALID, "no-alloc sort holds at most %d particles (got %d); use jt_cell_sort with a "
+                         "workspace", JT_NOALLOC_SORT_MAX_PARTICLES, n);
+    if (n == 0) return JT_OK;
+    if (pos_in == nullptr || pos_out == nullptr || ids_out == nullptr)
+        return set_error(JT_ERR_INVALID, "pos_in, pos_out and ids_out are required");
+    if ((comp_in == nullptr) != (comp_out == nullptr))
+        return set_error(JT_ERR_INVALID, "comp_in and comp_out go together");
+    if (pos_in == pos_out || ids_in == ids_out) return set_error(JT_ERR_INVALID, "cell sort cannot run in place");
+    void* ws = nullptr;
+    const int rc = noalloc_scratch(&ws);
+    if (rc != JT_OK) return rc;
+    // cell_sort clears the histogram it accumulates into; every other scratch
+    // word is written before it is read
+    return cell_sort(*g, n, pos_in, comp_in, ids_in, pos_out, comp_out, ids_out, ws, (cudaStream_t)stream);
 }
 
 extern "C" int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* pos_out, void* stream) {
