@@ -114,14 +114,20 @@ typedef struct {
  * Node (i,j,k) of an (nx,ny,nz) grid has index (i*ny + j)*nz + k, the
  * reference's ij layout.  Values are stored as snapshot PAIRS: record n of
  * pair p holds snapshot p and p+1 of node n side by side:
- *   F32 : 8 floats  {Ax,Ay,Az,Bx, By,Bz,0,0}        (32 B, one sector)
- *   BF16/F16: 8 halves {Ax,Ay,Az,Bx,By,Bz,0,0}      (16 B)
- * so one aligned load returns both bracketing snapshots of a node. */
+ *   F32 : 8 floats  {Ax,Ay,Bx,By, Az,Bz,0,0}        (32 B, one sector)
+ *   BF16/F16 (grid field): 16 halves, the z-PAIR of node (i,j,k) and its
+ *         z-successor (i,j,k1) -- k1 = (k+1) mod nz for periodic bounds,
+ *         min(k+1, nz-1) otherwise: {node k: Ax,Ay,Bx,By,Az,Bz, node k1:
+ *         Ax,Ay,Bx,By,Az,Bz, 0,0,0,0}                (32 B)
+ *   BF16/F16 (mesh, nearest fields): 8 halves {Ax,Ay,Bx,By,Az,Bz,0,0} (16 B)
+ * so one aligned 256-bit load returns both bracketing snapshots of a node
+ * (or of two z-neighbours), x,y components in register pairs. */
 typedef struct {
     int32_t nx, ny, nz;
     int32_t bounds_mode;   /* JT_GRID_*                                       */
     float origin[3];       /* grid_x[0], grid_y[0], grid_z[0]                 */
     float spacing[3];      /* float32(grid[1]-grid[0]), 1 when n == 1         */
+    float inv_spacing[3];  /* 1/spacing (used by the non-exact modes only)    */
     float valid_hi[3];     /* float32(min + (n-1)*d), the zero/nan validity edge */
     int32_t storage;       /* JT_STORE_*                                      */
     int32_t n_pairs;       /* number of snapshot pairs (>= 1)                  */

@@ -22,7 +22,10 @@ LIB_PATH = PKG_DIR / LIB_NAME
 OBJ_DIR = PKG_DIR / "_build"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+# -fmad=false: no multiply/add is ever contracted implicitly, so the exact
+# (NumPy-compatible) arithmetic holds for scalar and packed float32x2 code;
+# the fast paths ask for FMAs explicitly (fmaf, __ffma2_rn).
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-fmad=false",
               "-Xptxas", "-warn-spills"]
 
 
@@ -37,12 +40,13 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
-def _compile(src: Path, verbose: bool) -> Path:
-    obj = OBJ_DIR / (src.stem + ".o")
+def _compile(src: Path, verbose: bool, obj_dir: Path = OBJ_DIR, defines: tuple = ()) -> Path:
+    obj = obj_dir / (src.stem + ".o")
     deps = [src] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
     if obj.exists() and obj.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return obj
-    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc_path(), *ARCH, *NVCC_FLAGS, *[f"-D{d}" for d in defines], "-I", str(INCLUDE), "-c", str(src),
+           "-o", str(obj)]
     if src.suffix == ".cpp":
         cmd = [nvcc_path(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", str(INCLUDE),
                "-c", str(src), "-o", str(obj)]
@@ -56,24 +60,29 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> Path:
-    """Compile every translation unit and link ``libjaxtrace_gb300.so``."""
-    OBJ_DIR.mkdir(exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, defines: tuple = (), out: Path | None = None) -> Path:
+    """Compile every translation unit and link ``libjaxtrace_gb300.so``.
+
+    ``defines`` (e.g. ``("JT_TRACK_MIN_BLOCKS=3",)``) and ``out`` build a
+    tuning variant into another directory; the default build is in-tree."""
+    lib_path = Path(out) if out is not None else LIB_PATH
+    obj_dir = OBJ_DIR if out is None else lib_path.parent / "_build"
+    obj_dir.mkdir(parents=True, exist_ok=True)
     srcs = sources()
     jobs = jobs or min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
-        return LIB_PATH
-    tmp = LIB_PATH.with_suffix(".so.tmp")
+        objs = list(ex.map(lambda s: _compile(s, verbose, obj_dir, tuple(defines)), srcs))
+    if lib_path.exists() and lib_path.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
+        return lib_path
+    tmp = lib_path.with_suffix(".so.tmp")
     cmd = [nvcc_path(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -43,7 +43,7 @@ BLEND_DTYPE = np.dtype([("pair", "<i4"), ("form", "<i4"), ("wa", "<f4"), ("wb", 
 
 class GridField(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("bounds_mode", i32),
-                ("origin", f32 * 3), ("spacing", f32 * 3), ("valid_hi", f32 * 3),
+                ("origin", f32 * 3), ("spacing", f32 * 3), ("inv_spacing", f32 * 3), ("valid_hi", f32 * 3),
                 ("storage", i32), ("n_pairs", i32), ("pair_stride", i64), ("pairs", vp)]
 
 
@@ -110,7 +110,10 @@ _lib = None
 
 
 def library_path() -> Path:
-    return _build.LIB_PATH
+    """The in-tree library, or the file named by JAXTRACE_GB300_LIB (a tuning
+    variant built by ``_build.build(defines=..., out=...)``)."""
+    alt = os.environ.get("JAXTRACE_GB300_LIB")
+    return Path(alt) if alt else _build.LIB_PATH
 
 
 def load(build_if_missing: bool = True):

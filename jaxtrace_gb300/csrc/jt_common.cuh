@@ -13,6 +13,24 @@
 
 namespace jt {
 
+// Tuning switches.  JT_LERP_NOINLINE=1 moves the rarely taken extrapolation
+// blend out of line (measured 2x slower: the call forces a stack frame on the
+// hot path); JT_STAGE_UNROLL unrolls the RK stage loop (measured slower at the
+// default occupancy: more registers, more instruction-cache misses).
+#ifndef JT_LERP_NOINLINE
+#define JT_LERP_NOINLINE 0
+#endif
+#if JT_LERP_NOINLINE
+#define JT_LERP_INLINE __device__ __noinline__
+#else
+#define JT_LERP_INLINE __device__ __forceinline__
+#endif
+#ifndef JT_STAGE_UNROLL
+#define JT_STAGE_UNROLL 1
+#endif
+#define JT_PRAGMA(x) _Pragma(#x)
+#define JT_UNROLL(n) JT_PRAGMA(unroll n)
+
 // ---------------------------------------------------------------------------
 // Arithmetic policies.  Exact: every operation rounded to nearest on its own,
 // never contracted into an FMA -- the order and rounding of NumPy float32
@@ -77,61 +95,93 @@ struct V3 {
 // ---------------------------------------------------------------------------
 // Snapshot-pair records.
 // ---------------------------------------------------------------------------
+// Record layout (8 slots, float32 or 16-bit): {Ax, Ay, Bx, By, Az, Bz, 0, 0}
+// so that (Ax,Ay) and (Bx,By) arrive in aligned register pairs for the
+// packed float32x2 instructions.
 struct PairVal {
-    float ax, ay, az, bx, by, bz;
+    float2 axy, bxy;
+    float az, bz;
 };
 
 template <int STORE>
 __device__ __forceinline__ PairVal load_pair(const void* base, int64_t rec);
 
-template <>
-__device__ __forceinline__ PairVal load_pair<JT_STORE_F32>(const void* base, int64_t rec) {
-    const float4* p = reinterpret_cast<const float4*>(base) + 2 * rec;
-    float4 lo = __ldg(p);
-    float2 hi = __ldg(reinterpret_cast<const float2*>(p + 1));
-    return PairVal{lo.x, lo.y, lo.z, lo.w, hi.x, hi.y};
+// One 256-bit read-only load (a whole 32-byte record in one request).
+__device__ __forceinline__ void ldg256(const void* p, uint32_t (&w)[8]) {
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+        : "l"(p));
 }
 
 template <>
+__device__ __forceinline__ PairVal load_pair<JT_STORE_F32>(const void* base, int64_t rec) {
+    uint32_t w[8];
+    ldg256(reinterpret_cast<const float4*>(base) + 2 * rec, w);
+    return PairVal{make_float2(__uint_as_float(w[0]), __uint_as_float(w[1])),
+                   make_float2(__uint_as_float(w[2]), __uint_as_float(w[3])), __uint_as_float(w[4]),
+                   __uint_as_float(w[5])};
+}
+
+// bfloat16 -> float32 is exact: the 16 bits become the high half of the word.
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+template <int STORE>
+__device__ __forceinline__ PairVal decode3(uint32_t w0, uint32_t w1, uint32_t w2) {
+    if (STORE == JT_STORE_BF16) {
+        return PairVal{make_float2(bf16_lo(w0), bf16_hi(w0)), make_float2(bf16_lo(w1), bf16_hi(w1)), bf16_lo(w2),
+                       bf16_hi(w2)};
+    }
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&w0));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&w1));
+    const float2 z = __half22float2(*reinterpret_cast<const __half2*>(&w2));
+    return PairVal{a, b, z.x, z.y};
+}
+
+// 16-bit z-pair record of the grid field (32 B): node (i,j,k) in words 0-2
+// and its z-successor (i,j,k1) in words 3-5, k1 as the sampler computes it.
+template <int STORE>
+__device__ __forceinline__ void load_zpair(const void* base, int64_t rec, PairVal& p0, PairVal& p1) {
+    uint32_t w[8];
+    ldg256(reinterpret_cast<const uint4*>(base) + 2 * rec, w);
+    p0 = decode3<STORE>(w[0], w[1], w[2]);
+    p1 = decode3<STORE>(w[3], w[4], w[5]);
+}
+
+// 16-bit single-node record (16 B), used by the mesh and nearest fields.
+template <>
 __device__ __forceinline__ PairVal load_pair<JT_STORE_BF16>(const void* base, int64_t rec) {
-    uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
-    __nv_bfloat162 h0 = *reinterpret_cast<__nv_bfloat162*>(&r.x);
-    __nv_bfloat162 h1 = *reinterpret_cast<__nv_bfloat162*>(&r.y);
-    __nv_bfloat162 h2 = *reinterpret_cast<__nv_bfloat162*>(&r.z);
-    float2 f0 = __bfloat1622float2(h0), f1 = __bfloat1622float2(h1), f2 = __bfloat1622float2(h2);
-    return PairVal{f0.x, f0.y, f1.x, f1.y, f2.x, f2.y};
+    const uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
+    return decode3<JT_STORE_BF16>(r.x, r.y, r.z);
 }
 
 template <>
 __device__ __forceinline__ PairVal load_pair<JT_STORE_F16>(const void* base, int64_t rec) {
-    uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
-    __half2 h0 = *reinterpret_cast<__half2*>(&r.x);
-    __half2 h1 = *reinterpret_cast<__half2*>(&r.y);
-    __half2 h2 = *reinterpret_cast<__half2*>(&r.z);
-    float2 f0 = __half22float2(h0), f1 = __half22float2(h1), f2 = __half22float2(h2);
-    return PairVal{f0.x, f0.y, f1.x, f1.y, f2.x, f2.y};
+    const uint4 r = __ldg(reinterpret_cast<const uint4*>(base) + rec);
+    return decode3<JT_STORE_F16>(r.x, r.y, r.z);
 }
 
-// Blend of one snapshot pair at the time the schedule entry describes:
-// time_series.py:367  ((1-alpha)*V[il] + alpha*V[ir]).astype(float32)
-// time_series.py:336  V0 + alpha*(V1-V0)        (linear extrapolation, left)
-// time_series.py:352  V1 + alpha*(V1-V0)        (linear extrapolation, right)
+// a*wa + b*wb on (x,y) pairs.  The exact mode rounds every product and sum on
+// its own with scalar instructions (a packed multiply followed by a packed
+// add was measured to differ from separately rounded scalar operations in a
+// quarter of the results, so it cannot stand in for NumPy's arithmetic); the
+// fast modes use the packed FFMA2/FMUL2 instructions.
+template <bool EXACT>
+__device__ __forceinline__ float2 dot2p(float2 a, float2 wa, float2 b, float2 wb) {
+    if (EXACT) {
+        return make_float2(__fadd_rn(__fmul_rn(a.x, wa.x), __fmul_rn(b.x, wb.x)),
+                           __fadd_rn(__fmul_rn(a.y, wa.y), __fmul_rn(b.y, wb.y)));
+    }
+    return __ffma2_rn(a, wa, __fmul2_rn(b, wb));
+}
+
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+
+// Linear extrapolation outside the snapshot times (rarely taken).
 template <bool EXACT, int STORE>
-__device__ __forceinline__ V3 blend(const PairVal& p, const jt_blend& e) {
+JT_LERP_INLINE V3 blend_lerp(const PairVal& p, const jt_blend& e) {
     typedef Ar<EXACT> A;
-    if (e.form == JT_BLEND_WEIGHTED) {
-        return V3{A::dot2(p.ax, e.wa, p.bx, e.wb), A::dot2(p.ay, e.wa, p.by, e.wb),
-                  A::dot2(p.az, e.wa, p.bz, e.wb)};
-    }
-    if (e.form == JT_BLEND_SAME_A) {
-        return V3{A::dot2(p.ax, e.wa, p.ax, e.wb), A::dot2(p.ay, e.wa, p.ay, e.wb),
-                  A::dot2(p.az, e.wa, p.az, e.wb)};
-    }
-    if (e.form == JT_BLEND_SAME_B) {
-        return V3{A::dot2(p.bx, e.wa, p.bx, e.wb), A::dot2(p.by, e.wa, p.by, e.wb),
-                  A::dot2(p.bz, e.wa, p.bz, e.wb)};
-    }
-    float ax = p.ax, ay = p.ay, az = p.az, bx = p.bx, by = p.by, bz = p.bz;
+    float ax = p.axy.x, ay = p.axy.y, az = p.az, bx = p.bxy.x, by = p.bxy.y, bz = p.bz;
     if (STORE != JT_STORE_F32) {
         ax = A::mul(ax, e.sa); ay = A::mul(ay, e.sa); az = A::mul(az, e.sa);
         bx = A::mul(bx, e.sb); by = A::mul(by, e.sb); bz = A::mul(bz, e.sb);
@@ -142,6 +192,27 @@ __device__ __forceinline__ V3 blend(const PairVal& p, const jt_blend& e) {
     }
     return V3{A::axpy(bx, e.wb, A::sub(bx, ax)), A::axpy(by, e.wb, A::sub(by, ay)),
               A::axpy(bz, e.wb, A::sub(bz, az))};
+}
+
+// Blend of one snapshot pair at the time the schedule entry describes:
+// time_series.py:367  ((1-alpha)*V[il] + alpha*V[ir]).astype(float32)
+// time_series.py:336  V0 + alpha*(V1-V0)        (linear extrapolation, left)
+// time_series.py:352  V1 + alpha*(V1-V0)        (linear extrapolation, right)
+template <bool EXACT, int STORE>
+__device__ __forceinline__ V3 blend(const PairVal& p, const jt_blend& e) {
+    typedef Ar<EXACT> A;
+    if (e.form == JT_BLEND_WEIGHTED) {
+        const float2 xy = dot2p<EXACT>(p.axy, splat(e.wa), p.bxy, splat(e.wb));
+        return V3{xy.x, xy.y, A::dot2(p.az, e.wa, p.bz, e.wb)};
+    }
+    const float ax = p.axy.x, ay = p.axy.y, bx0 = p.bxy.x, by0 = p.bxy.y;
+    if (e.form == JT_BLEND_SAME_A) {
+        return V3{A::dot2(ax, e.wa, ax, e.wb), A::dot2(ay, e.wa, ay, e.wb), A::dot2(p.az, e.wa, p.az, e.wb)};
+    }
+    if (e.form == JT_BLEND_SAME_B) {
+        return V3{A::dot2(bx0, e.wa, bx0, e.wb), A::dot2(by0, e.wa, by0, e.wb), A::dot2(p.bz, e.wa, p.bz, e.wb)};
+    }
+    return blend_lerp<EXACT, STORE>(p, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,24 +352,35 @@ __device__ __forceinline__ void integrate(const Field& f, const jt_blend* s, con
     typedef Ar<EXACT> A;
     V3 inc;  // the increment added to x
     if (INTEG == JT_RK4) {
-        const jt_blend e0 = s[0], e1 = s[1], e2 = s[2];
-        V3 k1 = f(x, e0, flags);
-        V3 x2{A::axpy(x.x, k.dth, k1.x), A::axpy(x.y, k.dth, k1.y), A::axpy(x.z, k.dth, k1.z)};
-        V3 k2 = f(x2, e1, flags);
-        V3 x3{A::axpy(x.x, k.dth, k2.x), A::axpy(x.y, k.dth, k2.y), A::axpy(x.z, k.dth, k2.z)};
-        V3 k3 = f(x3, e1, flags);
-        V3 x4{A::axpy(x.x, k.dt, k3.x), A::axpy(x.y, k.dt, k3.y), A::axpy(x.z, k.dt, k3.z)};
-        V3 k4 = f(x4, e2, flags);
-        V3 sm{A::add(A::add(A::add(k1.x, A::mul(2.0f, k2.x)), A::mul(2.0f, k3.x)), k4.x),
-              A::add(A::add(A::add(k1.y, A::mul(2.0f, k2.y)), A::mul(2.0f, k3.y)), k4.y),
-              A::add(A::add(A::add(k1.z, A::mul(2.0f, k2.z)), A::mul(2.0f, k3.z)), k4.z)};
+        // One field-evaluation body, four trips: stage positions x + dth*k1,
+        // x + dth*k2, x + dt*k3 and the sum ((k1 + 2k2) + 2k3) + k4 in the
+        // reference's left-to-right order.
+        V3 sm{0.f, 0.f, 0.f}, xs = x;
+JT_UNROLL(JT_STAGE_UNROLL)
+        for (int st = 0; st < 4; ++st) {
+            const jt_blend e = s[st == 0 ? 0 : (st == 3 ? 2 : 1)];
+            const V3 kk = f(xs, e, flags);
+            if (st == 0) {
+                sm = kk;
+            } else if (st == 3) {
+                sm = V3{A::add(sm.x, kk.x), A::add(sm.y, kk.y), A::add(sm.z, kk.z)};
+            } else {
+                sm = V3{A::add(sm.x, A::mul(2.0f, kk.x)), A::add(sm.y, A::mul(2.0f, kk.y)),
+                        A::add(sm.z, A::mul(2.0f, kk.z))};
+            }
+            const float h = st < 2 ? k.dth : k.dt;
+            xs = V3{A::axpy(x.x, h, kk.x), A::axpy(x.y, h, kk.y), A::axpy(x.z, h, kk.z)};
+        }
         inc = V3{A::mul(k.dt6, sm.x), A::mul(k.dt6, sm.y), A::mul(k.dt6, sm.z)};
     } else if (INTEG == JT_RK2) {
-        const jt_blend e0 = s[0], e1 = s[1];
-        V3 v1 = f(x, e0, flags);
-        V3 xm{A::axpy(x.x, k.dth, v1.x), A::axpy(x.y, k.dth, v1.y), A::axpy(x.z, k.dth, v1.z)};
-        V3 v2 = f(xm, e1, flags);
-        inc = V3{A::mul(k.dt, v2.x), A::mul(k.dt, v2.y), A::mul(k.dt, v2.z)};
+        V3 xs = x, v{0.f, 0.f, 0.f};
+JT_UNROLL(JT_STAGE_UNROLL)
+        for (int st = 0; st < 2; ++st) {
+            const jt_blend e = s[st];
+            v = f(xs, e, flags);
+            xs = V3{A::axpy(x.x, k.dth, v.x), A::axpy(x.y, k.dth, v.y), A::axpy(x.z, k.dth, v.z)};
+        }
+        inc = V3{A::mul(k.dt, v.x), A::mul(k.dt, v.y), A::mul(k.dt, v.z)};
     } else {
         const jt_blend e0 = s[0];
         V3 v = f(x, e0, flags);

@@ -3,6 +3,10 @@
 // to TimeSeriesField.sample_at_time (fields/time_series.py:326-367): the
 // reference blends every node in time and then interpolates; here only the
 // eight gathered corners are blended, with identical float32 rounding.
+//
+// Throughput: x and y components travel as float32x2 pairs through packed
+// FMUL2/FADD2/FFMA2 instructions (each lane rounded like the scalar op, so
+// the exact mode stays bit-identical), z components pair up across corners.
 #pragma once
 
 #include "jt_common.cuh"
@@ -11,10 +15,11 @@ namespace jt {
 
 // Continuous index, cell and weight of one axis (structured.py:289-322).
 template <bool EXACT>
-__device__ __forceinline__ void grid_axis(float x, float org, float d, int n, int mode, float vhi,
+__device__ __forceinline__ void grid_axis(float x, float org, float d, float inv_d, int n, int mode, float vhi,
                                           int& i0, int& i1, float& w, bool& valid, int& flags) {
     typedef Ar<EXACT> A;
-    float f = A::div(A::sub(x, org), d);  // (x - x_min) / dx
+    // (x - x_min) / dx; the fast modes multiply by the reciprocal
+    float f = EXACT ? __fdiv_rn(__fsub_rn(x, org), d) : (x - org) * inv_d;
     if (mode == JT_GRID_PERIODIC) {
         const int nn = n > 1 ? n : 1;
         f = np_mod(f, (float)nn);          // np.mod(fx, max(Nx,1))
@@ -43,6 +48,23 @@ __device__ __forceinline__ void grid_axis(float x, float org, float d, int n, in
     }
 }
 
+// A corner value after the time blend: (x,y) packed, z apart.
+struct CV {
+    float2 xy;
+    float z;
+};
+
+template <bool EXACT, int STORE>
+__device__ __forceinline__ CV blend_cv(const PairVal& p, const jt_blend& e, float2 WA, float2 WB, bool weighted) {
+    if (weighted) {
+        // wa*A + wb*B per component
+        const float2 xy = dot2p<EXACT>(p.axy, WA, p.bxy, WB);
+        return CV{xy, Ar<EXACT>::dot2(p.az, WA.x, p.bz, WB.x)};
+    }
+    const V3 v = blend<EXACT, STORE>(p, e);
+    return CV{make_float2(v.x, v.y), v.z};
+}
+
 template <bool EXACT, int STORE>
 struct GridField {
     jt_grid_field F;
@@ -54,44 +76,59 @@ struct GridField {
         int i0, i1, j0, j1, k0, k1;
         float wx, wy, wz;
         bool vx, vy, vz;
-        grid_axis<EXACT>(p.x, F.origin[0], F.spacing[0], F.nx, F.bounds_mode, F.valid_hi[0], i0, i1, wx, vx, flags);
-        grid_axis<EXACT>(p.y, F.origin[1], F.spacing[1], F.ny, F.bounds_mode, F.valid_hi[1], j0, j1, wy, vy, flags);
-        grid_axis<EXACT>(p.z, F.origin[2], F.spacing[2], F.nz, F.bounds_mode, F.valid_hi[2], k0, k1, wz, vz, flags);
+        grid_axis<EXACT>(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode, F.valid_hi[0], i0,
+                         i1, wx, vx, flags);
+        grid_axis<EXACT>(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode, F.valid_hi[1], j0,
+                         j1, wy, vy, flags);
+        grid_axis<EXACT>(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode, F.valid_hi[2], k0,
+                         k1, wz, vz, flags);
 
         const int pr = min(max(e.pair, 0), F.n_pairs - 1);
         const int64_t base = (int64_t)pr * F.pair_stride;
         const int ny = F.ny, nz = F.nz;
-        const int64_t r00 = ((int64_t)i0 * ny + j0) * nz, r10 = ((int64_t)i1 * ny + j0) * nz;
-        const int64_t r01 = ((int64_t)i0 * ny + j1) * nz, r11 = ((int64_t)i1 * ny + j1) * nz;
-        // all eight gathers issued before any use
-        const PairVal p000 = load_pair<STORE>(F.pairs, base + r00 + k0);
-        const PairVal p100 = load_pair<STORE>(F.pairs, base + r10 + k0);
-        const PairVal p010 = load_pair<STORE>(F.pairs, base + r01 + k0);
-        const PairVal p110 = load_pair<STORE>(F.pairs, base + r11 + k0);
-        const PairVal p001 = load_pair<STORE>(F.pairs, base + r00 + k1);
-        const PairVal p101 = load_pair<STORE>(F.pairs, base + r10 + k1);
-        const PairVal p011 = load_pair<STORE>(F.pairs, base + r01 + k1);
-        const PairVal p111 = load_pair<STORE>(F.pairs, base + r11 + k1);
-        const V3 v000 = blend<EXACT, STORE>(p000, e), v100 = blend<EXACT, STORE>(p100, e);
-        const V3 v010 = blend<EXACT, STORE>(p010, e), v110 = blend<EXACT, STORE>(p110, e);
-        const V3 v001 = blend<EXACT, STORE>(p001, e), v101 = blend<EXACT, STORE>(p101, e);
-        const V3 v011 = blend<EXACT, STORE>(p011, e), v111 = blend<EXACT, STORE>(p111, e);
+        const int r00 = (i0 * ny + j0) * nz, r10 = (i1 * ny + j0) * nz;
+        const int r01 = (i0 * ny + j1) * nz, r11 = (i1 * ny + j1) * nz;
+        // all gathers issued before any use: eight 32-byte float32 node
+        // records, or four 32-byte 16-bit z-pair records (k0 and k1 together)
+        PairVal p000, p100, p010, p110, p001, p101, p011, p111;
+        if (STORE == JT_STORE_F32) {
+            p000 = load_pair<STORE>(F.pairs, base + (r00 + k0));
+            p100 = load_pair<STORE>(F.pairs, base + (r10 + k0));
+            p010 = load_pair<STORE>(F.pairs, base + (r01 + k0));
+            p110 = load_pair<STORE>(F.pairs, base + (r11 + k0));
+            p001 = load_pair<STORE>(F.pairs, base + (r00 + k1));
+            p101 = load_pair<STORE>(F.pairs, base + (r10 + k1));
+            p011 = load_pair<STORE>(F.pairs, base + (r01 + k1));
+            p111 = load_pair<STORE>(F.pairs, base + (r11 + k1));
+        } else {
+            load_zpair<STORE>(F.pairs, base + (r00 + k0), p000, p001);
+            load_zpair<STORE>(F.pairs, base + (r10 + k0), p100, p101);
+            load_zpair<STORE>(F.pairs, base + (r01 + k0), p010, p011);
+            load_zpair<STORE>(F.pairs, base + (r11 + k0), p110, p111);
+        }
+        const bool wgt = e.form == JT_BLEND_WEIGHTED;
+        const float2 WA = splat(e.wa), WB = splat(e.wb);
+        const CV v000 = blend_cv<EXACT, STORE>(p000, e, WA, WB, wgt), v100 = blend_cv<EXACT, STORE>(p100, e, WA, WB, wgt);
+        const CV v010 = blend_cv<EXACT, STORE>(p010, e, WA, WB, wgt), v110 = blend_cv<EXACT, STORE>(p110, e, WA, WB, wgt);
+        const CV v001 = blend_cv<EXACT, STORE>(p001, e, WA, WB, wgt), v101 = blend_cv<EXACT, STORE>(p101, e, WA, WB, wgt);
+        const CV v011 = blend_cv<EXACT, STORE>(p011, e, WA, WB, wgt), v111 = blend_cv<EXACT, STORE>(p111, e, WA, WB, wgt);
 
-        // structured.py:334-342: lerp in x, then y, then z
+        // structured.py:334-342: lerp in x, then y, then z; every product
+        // rounded before its sum in the exact mode
         const float ox = A::sub(1.0f, wx), oy = A::sub(1.0f, wy), oz = A::sub(1.0f, wz);
-        V3 r;
-#define JT_TRI(c)                                                      \
-    {                                                                  \
-        const float c00 = A::dot2(v000.c, ox, v100.c, wx);             \
-        const float c10 = A::dot2(v010.c, ox, v110.c, wx);             \
-        const float c01 = A::dot2(v001.c, ox, v101.c, wx);             \
-        const float c11 = A::dot2(v011.c, ox, v111.c, wx);             \
-        const float c0 = A::dot2(c00, oy, c10, wy);                    \
-        const float c1 = A::dot2(c01, oy, c11, wy);                    \
-        r.c = A::dot2(c0, oz, c1, wz);                                 \
-    }
-        JT_TRI(x) JT_TRI(y) JT_TRI(z)
-#undef JT_TRI
+        const float2 OX = splat(ox), WX = splat(wx), OY = splat(oy), WY = splat(wy), OZ = splat(oz), WZ = splat(wz);
+        const float2 c00 = dot2p<EXACT>(v000.xy, OX, v100.xy, WX);
+        const float2 c10 = dot2p<EXACT>(v010.xy, OX, v110.xy, WX);
+        const float2 c01 = dot2p<EXACT>(v001.xy, OX, v101.xy, WX);
+        const float2 c11 = dot2p<EXACT>(v011.xy, OX, v111.xy, WX);
+        const float2 c0 = dot2p<EXACT>(c00, OY, c10, WY);
+        const float2 c1 = dot2p<EXACT>(c01, OY, c11, WY);
+        const float2 rxy = dot2p<EXACT>(c0, OZ, c1, WZ);
+        // z: (c00z, c01z) and (c10z, c11z) as pairs, then (c0z, c1z)
+        const float2 cz0 = dot2p<EXACT>(make_float2(v000.z, v001.z), OX, make_float2(v100.z, v101.z), WX);
+        const float2 cz1 = dot2p<EXACT>(make_float2(v010.z, v011.z), OX, make_float2(v110.z, v111.z), WX);
+        const float2 cz = dot2p<EXACT>(cz0, OY, cz1, WY);
+        V3 r{rxy.x, rxy.y, A::dot2(cz.x, oz, cz.y, wz)};
         if (F.bounds_mode == JT_GRID_ZERO || F.bounds_mode == JT_GRID_NAN) {
             if (!(vx && vy && vz)) {
                 const float o = F.bounds_mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);

@@ -9,9 +9,16 @@ namespace jt {
 
 constexpr int kBlock = 256;
 
+// Resident blocks per SM the tracking kernels are compiled for (register cap
+// 65536 / (kBlock * JT_TRACK_MIN_BLOCKS)).  Measured on the precision
+// configuration: 3 beats 2 by 12-15 % and 4 (heavy spills) by 5-10 %.
+#ifndef JT_TRACK_MIN_BLOCKS
+#define JT_TRACK_MIN_BLOCKS 3
+#endif
+
 // Persistent tracking: tracker.py:236-242 (scan body) over [step_begin, step_end).
 template <bool EXACT, int INTEG, class Field>
-__global__ void __launch_bounds__(kBlock) k_track(Field f, jt_boundary B, jt_track_params P) {
+__global__ void __launch_bounds__(kBlock, JT_TRACK_MIN_BLOCKS) k_track(Field f, jt_boundary B, jt_track_params P) {
     track_body<EXACT, INTEG>(f, B, P);
 }
 

@@ -74,29 +74,50 @@ def snapshot_scales(data: np.ndarray, storage: int) -> np.ndarray:
     return np.exp2(np.ceil(np.log2(amax))).astype(F32)
 
 
-def build_pairs_device(data: np.ndarray, storage: int, device="cuda"):
-    """Upload (T,N,3) snapshots as (max(T-1,1), N, 8) pair records."""
+A_SLOTS, B_SLOTS = [0, 1, 4], [2, 3, 5]   # record {Ax,Ay,Bx,By,Az,Bz,0,0}
+
+
+def build_pairs_device(data: np.ndarray, storage: int, device="cuda", z_successor: np.ndarray | None = None):
+    """Upload (T,N,3) snapshots as (max(T-1,1), N, 8) pair records
+    {Ax,Ay,Bx,By,Az,Bz,0,0} (A = snapshot p, B = snapshot p+1).
+
+    With ``z_successor`` (16-bit grid fields) each record is a 16-slot z-pair:
+    node n in slots 0-5 and node z_successor[n] in slots 6-11."""
     torch = _torch_cuda()
     T, N, _ = data.shape
     P = max(T - 1, 1)
     scales = snapshot_scales(data, storage)
+    zp = z_successor is not None and storage != L.JT_STORE_F32
+    width = 16 if zp else 8
     if storage == L.JT_STORE_F32:
-        pairs = torch.zeros((P, N, 8), dtype=torch.float32, device=device)
+        pairs = torch.zeros((P, N, width), dtype=torch.float32, device=device)
     else:
         dt = torch.bfloat16 if storage == L.JT_STORE_BF16 else torch.float16
-        pairs = torch.zeros((P, N, 8), dtype=dt, device=device)
+        pairs = torch.zeros((P, N, width), dtype=dt, device=device)
+    a_idx = torch.tensor(A_SLOTS, device=device)
+    b_idx = torch.tensor(B_SLOTS, device=device)
+    a2_idx = a_idx + 6
+    b2_idx = b_idx + 6
+    succ = torch.from_numpy(np.asarray(z_successor, dtype=np.int64)).to(device) if zp else None
     prev = None
     for t in range(T):
         snap = torch.from_numpy(np.ascontiguousarray(data[t])).to(device)
         if storage != L.JT_STORE_F32:
             snap = (snap / float(scales[t])).to(pairs.dtype)
+        nxt = snap[succ] if zp else None
         if t < P:
-            pairs[t, :, 0:3] = snap
+            pairs[t].index_copy_(1, a_idx, snap)
+            if zp:
+                pairs[t].index_copy_(1, a2_idx, nxt)
         if t >= 1:
-            pairs[t - 1, :, 3:6] = snap
-        prev = snap
+            pairs[t - 1].index_copy_(1, b_idx, snap)
+            if zp:
+                pairs[t - 1].index_copy_(1, b2_idx, nxt)
+        prev = (snap, nxt)
     if T == 1:
-        pairs[0, :, 3:6] = prev
+        pairs[0].index_copy_(1, b_idx, prev[0])
+        if zp:
+            pairs[0].index_copy_(1, b2_idx, prev[1])
     return pairs, scales
 
 
@@ -198,8 +219,8 @@ class _DeviceField:
         torch = _torch_cuda()
         pairs = self._device_pairs()
         e = self.blend_at(t)[0]
-        A = pairs[int(e["pair"]), :, 0:3].float()
-        B = pairs[int(e["pair"]), :, 3:6].float()
+        A = pairs[int(e["pair"])][:, A_SLOTS].float()
+        B = pairs[int(e["pair"])][:, B_SLOTS].float()
         form = int(e["form"])
         if form == L.JT_BLEND_WEIGHTED:
             v = A * float(e["wa"]) + B * float(e["wb"])
@@ -289,10 +310,19 @@ class StructuredTimeSeriesField(_DeviceField):
         self.z_min, self.z_max = float(gz[0]), float(gz[-1])
         self._mode = codes[mode]
 
+    def _z_successor(self) -> np.ndarray:
+        """Node index of (i, j, k1) for every node (i, j, k), k1 as the sampler
+        computes it (structured.py:311-318)."""
+        nx, ny, nz = self.Nx, self.Ny, self.Nz
+        k = np.arange(nz)
+        k1 = (k + 1) % max(nz, 1) if self._mode == L.JT_GRID_PERIODIC else np.minimum(k + 1, max(nz - 1, 0))
+        col = np.arange(nx * ny, dtype=np.int64)[:, None] * nz
+        return (col + k1[None, :]).reshape(-1)
+
     def _device(self):
         if self._dev is not None:
             return
-        pairs, scales = build_pairs_device(self.data, self._storage)
+        pairs, scales = build_pairs_device(self.data, self._storage, z_successor=self._z_successor())
         self._scales = scales
         self._dev = {"pairs": pairs}
         g = L.GridField()
@@ -300,6 +330,7 @@ class StructuredTimeSeriesField(_DeviceField):
         g.bounds_mode = self._mode
         g.origin[:] = [F32(self.x_min), F32(self.y_min), F32(self.z_min)]
         g.spacing[:] = [F32(self.dx), F32(self.dy), F32(self.dz)]
+        g.inv_spacing[:] = [float(F32(1.0) / F32(v)) for v in (self.dx, self.dy, self.dz)]
         # structured.py:299-301: x <= x_min + (Nx-1)*dx, the Python float rounded to float32
         g.valid_hi[:] = [F32(self.x_min + (self.Nx - 1) * self.dx), F32(self.y_min + (self.Ny - 1) * self.dy),
                          F32(self.z_min + (self.Nz - 1) * self.dz)]

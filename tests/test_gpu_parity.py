@@ -196,6 +196,53 @@ def test_periodic_wrap_is_flagged():
     assert same(out, ref)
 
 
+# ---------------------------------------------------------------- 16-bit storage
+def _quantize(data, storage):
+    """The values 16-bit storage holds, as float32: round(v/s) * s per snapshot."""
+    import torch
+    from jaxtrace_gb300.fields import snapshot_scales
+    code = L.STORAGE_CODES[storage]
+    s = snapshot_scales(data, code)
+    dt = torch.bfloat16 if storage == "bf16" else torch.float16
+    q = np.stack([(torch.from_numpy(data[t]) / float(s[t])).to(dt).float().numpy() * s[t] for t in range(len(data))])
+    return q.astype(F32)
+
+
+@pytest.mark.parametrize("storage", ["bf16", "f16"])
+@pytest.mark.parametrize("mode", ["clamp", "periodic", "nan"])
+def test_16bit_sampler_matches_oracle_on_quantized_values(golden, storage, mode):
+    """BF16/FP16 snapshots (z-pair records) give the float32 result of the
+    quantized values up to the fast path's rounding: FMA contraction and the
+    cell coordinate taken as (x - x_min) * (1/dx), whose error grows with |fx|
+    (queries here reach several periods outside the box).  Tolerance: 1e-5
+    of the field's largest magnitude."""
+    g = golden("structured")
+    V, gx, gy, gz, q = (g[f"{mode}_{k}"] for k in ("V", "gx", "gy", "gz", "q"))
+    s = jt.StructuredGridSampler(V, gx, gy, gz, mode, storage=storage)
+    out = s.sample(q)
+    Vq = _quantize(V[None], storage)
+    ref, _ = oracle.sample(oracle.GridSpec(Vq, np.zeros(1, F32), gx, gy, gz, mode), q, 0.0)
+    assert np.allclose(out, ref, rtol=0, atol=1e-5 * float(np.abs(Vq).max()), equal_nan=True)
+
+
+@pytest.mark.parametrize("storage", ["bf16", "f16"])
+def test_16bit_tracking_matches_oracle_on_quantized_values(storage):
+    from jaxtrace_gb300 import workloads as W
+    c = W.precision_case(n=20, n_snap=6, seeds=(16, 16, 16), lattice=16, n_steps=25, dt=0.01)
+    g = c["grid"][0]
+    f = jt.StructuredTimeSeriesField(c["data"], c["times"], g, g, g, "clamp", storage=storage)
+    bc = jt.continuous_inlet_boundary_factory(W.UNIT, "x", "positive", "grid", c["concentrations"])
+    traj = jt.create_tracker("rk4", f, bc, record_final_only=True).track_particles(
+        c["x0"], c["time_span"], c["n_timesteps"], dt=c["dt"])
+    spec = oracle.GridSpec(_quantize(c["data"], storage), c["times"], g, g, g, "clamp")
+    lat = np.linspace(F32(0), F32(1), 16, dtype=F32)
+    times = np.linspace(0.0, 0.25, 26, dtype=F32)
+    ref, _, _ = oracle.track(spec, oracle.BoundarySpec(inlet_axis=0, inlet_positive=True, lattices=[lat, lat]),
+                             c["x0"], times, 0.01)
+    close = np.all(np.isclose(traj.positions[-1], ref, rtol=1e-4, atol=1e-5), axis=1)
+    assert close.mean() > 0.995  # an inlet snap can flip on a last-bit difference
+
+
 # ---------------------------------------------------------------- locality sort
 def test_cell_sort_is_a_permutation_in_morton_order():
     import ctypes as C
