@@ -38,6 +38,22 @@ UNIT = "particle-steps/s"
 BYTES_PER_PSTEP = {"f32": 4 * 2 * 8 * 12 + 24, "bf16": 4 * 2 * 8 * 6 + 24, "f16": 4 * 2 * 8 * 6 + 24}
 
 
+def traffic_per_pstep(storage):
+    """DRAM bytes per particle-step of k_track from the committed ncu summary
+    (profiles/k_track_precision.md, line 'dram_bytes_per_particle_step <storage> <value>')."""
+    f = ROOT / "profiles" / "k_track_precision.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.replace("|", " ").split()
+        if len(parts) >= 3 and parts[0] == "dram_bytes_per_particle_step" and parts[1] == storage:
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
 def args_parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -221,21 +237,17 @@ def main():
         comp = torch.zeros_like(x0_dev) if tr._arith() == L.JT_ARITH_COMPENSATED else None
         pos = torch.empty_like(x0_dev)
 
-        def one(ev=None):
+        def one(timers=None):
             pos.copy_(x0_dev)
             if comp is not None:
                 comp.zero_()
-            if ev is not None:
-                ev[0].record(stream)
-            tr.track_device(pos, times, case["dt"], status, comp, sched)
-            if ev is not None:
-                ev[1].record(stream)
+            return tr.track_device(pos, times, case["dt"], status, comp, sched, timers=timers)
 
         for _ in range(a.warmup):
             one()
         torch.cuda.synchronize()
         barrier(world)
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+        timers = []
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         headline = v == variants[0]
@@ -243,28 +255,33 @@ def main():
             clk.__enter__()
         torch.cuda.synchronize()
         t0.record(stream)
-        for k in range(a.steps):
-            one(evs[k])
+        counts = [one(timers) for _ in range(a.steps)]
         t1.record(stream)
         torch.cuda.synchronize()
         if headline:
             clk.__exit__()
         barrier(world)
         ms_total = max_over_ranks(world, t0.elapsed_time(t1))
-        kern_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+        launch_ms = [e[0].elapsed_time(e[1]) for e in timers]
+        per_launch_ms = float(np.mean(launch_ms))
+        n_track = sum(c["track_launches"] for c in counts)
         if headline:
-            launches = a.steps
+            launches = sum(c["kernels"] for c in counts)
         psteps = n * a.n_steps
         results[v] = {"value": world * psteps * a.steps / (ms_total / 1e3), "ms_per_step": ms_total / a.steps,
-                      "kernel_ms": kern_ms, "status": int(status.item()),
-                      "hbm_frac_algorithmic": None}
+                      "track_kernel_ms_per_step": float(np.sum(launch_ms)) / a.steps, "status": int(status.item())}
         bpp = BYTES_PER_PSTEP[v]
         from_peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         peak = float(from_peaks.get("hbm_gbs", 6800.0))
-        achieved = psteps * bpp / (kern_ms / 1e3) / 1e9
+        units_per_launch = psteps * a.steps / n_track          # particle-steps per k_track launch
+        achieved = units_per_launch * bpp / (per_launch_ms / 1e3) / 1e9
+        tb = traffic_per_pstep(v)
         results[v]["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                                  "frac": achieved / peak, "traffic": None,
-                                  "peak_source": "measured" if from_peaks else "fallback",
+                                  "frac": achieved / peak,
+                                  "traffic": (tb * units_per_launch if tb is not None else None),
+                                  "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if from_peaks else "fallback",
+                                  "kernel": "k_track (RK4, grid field, %s)" % v,
+                                  "launch_ms": per_launch_ms, "particle_steps_per_launch": units_per_launch,
                                   "bytes_per_particle_step": bpp}
         finals[v] = pos.cpu().numpy()
         del field
@@ -279,7 +296,7 @@ def main():
                        "steps_per_pass": a.n_steps,
                        "l2": f"inputs larger than L2 (positions {n * 12 / 1e6:.0f} MB, snapshot pairs "
                              f"{(len(case['times']) - 1) * g.size ** 3 * (32 if head == 'f32' else 16) / 1e9:.2f} GB)"},
-            "variants": {v: {k: r[k] for k in ("value", "ms_per_step", "kernel_ms", "status")} |
+            "variants": {v: {k: r[k] for k in ("value", "ms_per_step", "track_kernel_ms_per_step", "status")} |
                          {"roofline_frac": r["roofline"]["frac"]} for v, r in results.items()},
             "roofline": results[head]["roofline"], "gpu_launches": launches}
     if not a.profile and rank == 0:

@@ -286,14 +286,17 @@ class ParticleTracker:
         self.last_status = int(eng.status.item())
         return eng.launches
 
-    def track_device(self, pos, times, dt, status=None, comp=None, sched_dev=None):
+    def track_device(self, pos, times, dt, status=None, comp=None, sched_dev=None, timers=None):
         """Advance device positions (N,3) in place through every step of the
         float32 time grid ``times`` without recording (benchmark and ensemble
-        entry).  Returns the number of tracking-kernel launches."""
+        entry).  ``timers``: a list that receives a (start, end) CUDA-event
+        pair around every tracking-kernel launch.  Returns the number of
+        tracking launches and of all kernels this library launched."""
         eng = self._engine(pos, times, dt, sched_dev, status, comp)
+        eng.timers = timers
         eng.advance(0, len(times) - 1, None)
         eng.finish()
-        return eng.launches
+        return {"track_launches": eng.launches, "kernels": eng.kernels}
 
     # ------------------------------------------------------------------
     def validate_configuration(self) -> Dict[str, Any]:
@@ -350,7 +353,9 @@ class _Engine:
         self.status, self.sched = status, sched_dev
         self.n = pos.shape[0]
         self.sort_every = sort_every
-        self.launches = 0
+        self.launches = 0      # tracking-kernel launches
+        self.kernels = 0       # every kernel of this library
+        self.timers = None
         self.field_c = tracker._field.jt_field()
         self.bc_c = tracker._bc.jt_boundary()
         self.lib = L.load()
@@ -379,6 +384,7 @@ class _Engine:
         L.check(self.lib.jt_cell_sort(C.byref(self.grid), self.n, L.ptr(src_pos), L.ptr(self.comp), L.ptr(src_ids),
                                       L.ptr(dst_pos), L.ptr(comp_dst), L.ptr(dst_ids), L.ptr(self.ws),
                                       self.ws.numel(), self.stream))
+        self.kernels += 5      # keys, two scan levels, scan add, scatter
         if not first:
             self.pos, self.pos_alt = self.pos_alt, self.pos
             self.ids, self.ids_alt = self.ids_alt, self.ids
@@ -405,13 +411,22 @@ class _Engine:
                 p.record_every, p.record_compact, p.row_base, p.n_rows = k, int(compact), r0, nr
             else:
                 p.traj = p.vel = None
+            if self.timers is not None:
+                import torch
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                ev[0].record()
             L.check(self.lib.jt_track(C.byref(self.field_c), C.byref(self.bc_c), C.byref(p), self.stream))
+            if self.timers is not None:
+                ev[1].record()
+                self.timers.append(ev)
             self.launches += 1
+            self.kernels += 1
             s = stop
 
     def finish(self):
         if self.ids is not None:
             L.check(self.lib.jt_unpermute(self.n, L.ptr(self.pos), L.ptr(self.ids), L.ptr(self.out), self.stream))
+            self.kernels += 1
 
 
 def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:
