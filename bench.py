@@ -63,11 +63,15 @@ def args_parse():
     p.add_argument("--variants", default="bf16,f32,f16")
     p.add_argument("--seeds", type=int, default=256, help="lattice seeds per axis (256 -> 16,777,216)")
     p.add_argument("--n-steps", type=int, default=1000)
+    p.add_argument("--dt", type=float, default=0.002)
+    p.add_argument("--sort-every", type=int, default=None, help="locality re-sort interval (default: automatic)")
     p.add_argument("--grid", type=int, default=128)
     p.add_argument("--no-error", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--profile", action="store_true", help="only the timed kernel runs (for ncu)")
+    p.add_argument("--profile", action="store_true",
+                   help="first variant only, no error/e2e/CPU legs; the timed region is bracketed by "
+                        "cudaProfilerStart/Stop for ncu --profile-from-start off")
     return p.parse_args()
 
 
@@ -171,7 +175,7 @@ def run_reference(a, world, rank):
         return
     from jaxtrace_gb300 import workloads as W
     import oracle
-    case = W.precision_case(n=a.grid, seeds=(a.seeds,) * 3, n_steps=a.n_steps)
+    case = W.precision_case(n=a.grid, seeds=(a.seeds,) * 3, lattice=a.seeds, n_steps=a.n_steps, dt=a.dt)
     cores = os.cpu_count() or 1
     n = len(case["x0"])
     sample = min(n, 4096)
@@ -199,7 +203,7 @@ def run_reference(a, world, rank):
 def workload_name(a):
     return (f"precision: {a.grid}^3 clamp grid, 64 snapshots ABC+(1,0,0)+N(0,0.01^2) over [0,2], "
             f"{a.seeds ** 3} lattice seeds, continuous inlet x (lattice {a.seeds}x{a.seeds}), "
-            f"RK4 dt={2.0 / a.n_steps if a.n_steps != 1000 else 0.002}, {a.n_steps} steps")
+            f"RK4 dt={a.dt}, {a.n_steps} steps")
 
 
 def main():
@@ -215,7 +219,7 @@ def main():
     from jaxtrace_gb300 import workloads as W
 
     L.load()
-    dt = 0.002 if a.n_steps == 1000 else 2.0 / a.n_steps
+    dt = a.dt
     case = W.precision_case(n=a.grid, seeds=(a.seeds,) * 3, lattice=a.seeds, n_steps=a.n_steps, dt=dt)
     x0 = case["x0"]
     n = len(x0)
@@ -230,7 +234,7 @@ def main():
     clk = Clocks(local)
     for v in variants:
         field = jt.StructuredTimeSeriesField(case["data"], case["times"], g, g, g, "clamp", storage=v)
-        tr = jt.create_tracker("rk4", field, bc, record_final_only=True)
+        tr = jt.create_tracker("rk4", field, bc, record_final_only=True, sort_every=a.sort_every)
         trackers[v] = tr
         sched = torch.from_numpy(tr._schedule(times, case["dt"]).view(np.int32).reshape(-1, 8)).cuda()
         status = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -255,7 +259,11 @@ def main():
             clk.__enter__()
         torch.cuda.synchronize()
         t0.record(stream)
+        if a.profile:
+            torch.cuda.profiler.start()
         counts = [one(timers) for _ in range(a.steps)]
+        if a.profile:
+            torch.cuda.profiler.stop()
         t1.record(stream)
         torch.cuda.synchronize()
         if headline:

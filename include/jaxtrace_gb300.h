@@ -282,12 +282,16 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
                        float* x_out, int32_t n, int32_t* status, void* stream);
 
 /* ---- locality sort ------------------------------------------------------ */
-/* Morton cell grid of the sort: cell = clamp(floor((x-origin)*inv_cell), 0, 2^bits-1). */
+/* Cell grid of the sort: cell = clamp(floor((x-origin)*inv_cell), 0, 2^bits-1)
+ * per axis; cells ordered by Morton key (tracking locality) or row-major
+ * with x fastest (density passes: an x-run of cells is one particle range). */
+#define JT_ORDER_MORTON 0
+#define JT_ORDER_LINEAR 1
 typedef struct {
     float origin[3];
     float inv_cell[3];
     int32_t bits;            /* 1..7 bits per axis                           */
-    int32_t pad;
+    int32_t order;           /* JT_ORDER_*                                   */
 } jt_sort_grid;
 
 /* Bytes of device workspace jt_cell_sort needs (0 for invalid arguments). */
@@ -329,6 +333,68 @@ int jt_cell_sort_noalloc(const jt_sort_grid* g, int32_t n, const float* pos_in, 
 
 /* pos_out[ids[i]] = pos_sorted[i]: back to the caller's particle order. */
 int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* pos_out, void* stream);
+
+/* Counting sort of particles by Morton cell that also returns the cell list:
+ * cell_end[key] = one past the last sorted particle of Morton cell `key`
+ * (device, 2^(3*bits) entries; the cell starts at cell_end[key-1], or 0).
+ * Replaces HashGridNeighbors.__post_init__ (density/neighbors.py:61-104):
+ * cell keys, argsort, unique starts/counts.  Other arguments as jt_cell_sort. */
+int jt_cell_list(const jt_sort_grid* g, int32_t n, const float* pos_in, float* pos_out, int32_t* ids_out,
+                 uint32_t* cell_end, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- density passes ------------------------------------------------------ */
+#define JT_SPH_CUBIC 0    /* sph.py:227-236 */
+#define JT_SPH_WENDLAND 1 /* sph.py:238-246 */
+#define JT_SPH_GAUSSIAN 2 /* sph.py:248-255 */
+
+typedef struct {
+    int32_t dims;              /* 2 or 3 (2-D: z of particles and queries is 0) */
+    int32_t kernel;            /* JT_SPH_*                                    */
+    int32_t n_particles;
+    int32_t n_queries;
+    float radius;              /* neighbour cutoff (the NumPy path uses 3*mean(h), sph.py:284-285) */
+    float h_const;             /* smoothing length when h == NULL            */
+    jt_sort_grid grid;         /* cell grid of the particle cell list        */
+    int32_t reach[3];          /* cells searched on each side, per axis      */
+    int32_t pad;
+    const float* particles;    /* device (N,3) in cell order                 */
+    const float* masses;       /* device (N) in cell order, or NULL (unit masses) */
+    const float* h;            /* device (N) in cell order, or NULL (h_const) */
+    const uint32_t* cell_end;  /* device, from jt_cell_list                  */
+    const float* queries;      /* device (M,3)                               */
+    double* out;               /* device (M): sum_j m_j W(|q - p_j|, h_j)    */
+} jt_sph_params;
+
+/* SPH density at M query points: _evaluate_density (density/sph.py:269-292)
+ * summed exactly over every particle within `radius` (the NumPy brute-force
+ * semantics; no per-cell cap or nearest-512 truncation).  Each cell's terms
+ * are summed in float32 and the cells in float64.  Normalisation by N/volume
+ * (sph.py:365-378) is left to the caller. */
+int jt_sph_density(const jt_sph_params* p, void* stream);
+
+typedef struct {
+    int32_t dims;              /* 2 or 3                                      */
+    int32_t n_particles;
+    int32_t res[3];            /* grid points per axis (x, y, z; z = 1 in 2-D) */
+    float half_inv_h2;         /* 0.5 / h^2                                   */
+    float radius;              /* particles farther than this along an axis from every grid point of a tile are skipped */
+    jt_sort_grid grid;         /* cell grid of the particle cell list         */
+    const float* axis[3];      /* device float32 grid coordinates per axis    */
+    const float* particles;    /* device (N,3) in cell order                  */
+    const uint32_t* cell_end;  /* device, from jt_cell_list                   */
+    double* out;               /* device: grid (x index i, y index j, z index k) at (i*res_y + j)*res_z + k */
+} jt_kde_params;
+
+/* Gaussian KDE on a tensor grid: out = sum_j exp(-|g - p_j|^2 h^-2 / 2) at
+ * every grid point g (the float32 JAX / pure-NumPy formula of
+ * density/kde.py:249-282 without its constant factors, which the grid
+ * normalisation of kde.py:229-239 removes).  Separable per 8^3 (3-D) or
+ * 16^2 (2-D) tile; per-tile float32 chunks accumulated in float64. */
+int jt_kde_grid(const jt_kde_params* p, void* stream);
+
+/* The same sum at M arbitrary points (KDEEstimator.evaluate, kde.py:123-169):
+ * points device (M,3), out device (M).  p->axis and p->res are unused. */
+int jt_kde_points(const jt_kde_params* p, const float* points, int32_t m, double* out, void* stream);
 
 /* ---- octree build (host) ------------------------------------------------ */
 typedef struct {

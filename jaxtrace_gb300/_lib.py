@@ -91,7 +91,22 @@ class TrackParams(C.Structure):
 
 
 class SortGrid(C.Structure):
-    _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("bits", i32), ("pad", i32)]
+    _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("bits", i32), ("order", i32)]
+
+
+JT_ORDER_MORTON, JT_ORDER_LINEAR = 0, 1
+JT_SPH_CUBIC, JT_SPH_WENDLAND, JT_SPH_GAUSSIAN = 0, 1, 2
+
+
+class SphParams(C.Structure):
+    _fields_ = [("dims", i32), ("kernel", i32), ("n_particles", i32), ("n_queries", i32), ("radius", f32),
+                ("h_const", f32), ("grid", SortGrid), ("reach", i32 * 3), ("pad", i32), ("particles", vp),
+                ("masses", vp), ("h", vp), ("cell_end", vp), ("queries", vp), ("out", vp)]
+
+
+class KdeParams(C.Structure):
+    _fields_ = [("dims", i32), ("n_particles", i32), ("res", i32 * 3), ("half_inv_h2", f32), ("radius", f32),
+                ("grid", SortGrid), ("axis", vp * 3), ("particles", vp), ("cell_end", vp), ("out", vp)]
 
 
 class OctreeInfo(C.Structure):
@@ -143,6 +158,10 @@ def load(build_if_missing: bool = True):
         "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),
         "jt_unpermute": (i32, [i32, vp, vp, vp, vp]),
         "jt_cell_sort_noalloc": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp]),
+        "jt_cell_list": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, C.c_size_t, vp]),
+        "jt_sph_density": (i32, [P(SphParams), vp]),
+        "jt_kde_grid": (i32, [P(KdeParams), vp]),
+        "jt_kde_points": (i32, [P(KdeParams), vp, i32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -92,6 +92,19 @@ struct V3 {
     float x, y, z;
 };
 
+// Morton (Z-order) key of a cell: bit b of axis a goes to bit 3b+a.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000ff;
+    v = (v | (v << 8)) & 0x0300f00f;
+    v = (v | (v << 4)) & 0x030c30c3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+__device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
 // ---------------------------------------------------------------------------
 // Snapshot-pair records.
 // ---------------------------------------------------------------------------

@@ -1,0 +1,299 @@
+// Density passes over a Morton cell list: SPH summation (density/sph.py) and
+// Gaussian KDE on a grid or at points (density/kde.py).
+//
+// SPH: one query per thread; the query's neighbour cells are visited in a
+// fixed order, each cell's terms summed in float32 and the cell sums in
+// float64.  The sum runs over every particle within the cutoff -- the NumPy
+// brute-force semantics (sph.py:282-292), not the JAX hash grid's per-cell
+// cap and nearest-512 truncation (neighbors.py:145-159).
+//
+// KDE grid: exp(-|g-p|^2/2h^2) = ex * ey * ez factorises per axis, so a block
+// owning an 8x8x8 tile of grid points computes 24 exponentials per particle
+// (8 per axis) instead of 512 and forms the products from shared memory.
+// Particles more than `radius` from the tile along an axis lie in cells the
+// block never visits; their terms are below exp(-radius^2/2h^2).
+#include <stdint.h>
+
+#include "jt_internal.h"
+#include "jt_kernels.cuh"
+
+namespace jt {
+
+// Cell coordinate of x on one axis, clamped to [0, 2^bits - 1].
+__device__ __forceinline__ int cell_of(float x, float org, float inv, int lim) {
+    const float f = floorf((x - org) * inv);
+    return (f != f) ? 0 : (f < 0.0f ? 0 : (f > (float)lim ? lim : (int)f));
+}
+
+__device__ __forceinline__ uint32_t cell_begin(const uint32_t* __restrict__ end, uint32_t key) {
+    return key == 0 ? 0u : __ldg(end + key - 1);
+}
+
+// Row-major cell key (x fastest), the JT_ORDER_LINEAR order of the cell list:
+// the cells x0..x1 of one (y, z) row hold one contiguous particle range.
+__device__ __forceinline__ uint32_t row_key(int x, int y, int z, int bits) {
+    return (((uint32_t)z << bits | (uint32_t)y) << bits) | (uint32_t)x;
+}
+
+// Particle range [b, e) of the cells x0..x1 in row (y, z).
+__device__ __forceinline__ void row_range(const uint32_t* __restrict__ end, int x0, int x1, int y, int z, int bits,
+                                          uint32_t& b, uint32_t& e) {
+    b = cell_begin(end, row_key(x0, y, z, bits));
+    e = __ldg(end + row_key(x1, y, z, bits));
+}
+
+// Smoothing kernels of SPHDensityEstimator (sph.py:227-255).
+template <int DIM, int KERN>
+__device__ __forceinline__ float sph_w(float r, float h) {
+    const float hh = fmaxf(h, 1e-12f);
+    const float q = r / hh;
+    const float pi = 3.14159265358979f;
+    if (KERN == JT_SPH_CUBIC) {
+        const float sigma = DIM == 2 ? 10.0f / (7.0f * pi * hh * hh) : 1.0f / (pi * hh * hh * hh);
+        if (q <= 1.0f) return sigma * (1.0f - 1.5f * q * q + 0.75f * q * q * q);
+        if (q <= 2.0f) {
+            const float t = 2.0f - q;
+            return sigma * 0.25f * t * t * t;
+        }
+        return 0.0f;
+    } else if (KERN == JT_SPH_WENDLAND) {
+        const float sigma = DIM == 2 ? 7.0f / (pi * hh * hh) : 21.0f / (2.0f * pi * hh * hh * hh);
+        const float t = fmaxf(1.0f - q, 0.0f);
+        const float t2 = t * t;
+        return sigma * t2 * t2 * (1.0f + 4.0f * q);
+    } else {
+        const float ph2 = pi * hh * hh;
+        const float sigma = DIM == 2 ? 1.0f / ph2 : 1.0f / (ph2 * sqrtf(ph2));
+        return sigma * expf(-q * q);
+    }
+}
+
+template <int DIM, int KERN>
+__global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n_queries) return;
+    const float qx = P.queries[3 * (int64_t)i], qy = P.queries[3 * (int64_t)i + 1];
+    const float qz = DIM == 3 ? P.queries[3 * (int64_t)i + 2] : 0.0f;
+    const jt_sort_grid& g = P.grid;
+    const int lim = (1 << g.bits) - 1;
+    const int cx = cell_of(qx, g.origin[0], g.inv_cell[0], lim);
+    const int cy = cell_of(qy, g.origin[1], g.inv_cell[1], lim);
+    const int cz = DIM == 3 ? cell_of(qz, g.origin[2], g.inv_cell[2], lim) : 0;
+    const float r2max = P.radius * P.radius;
+    const int z0 = DIM == 3 ? max(cz - P.reach[2], 0) : 0, z1 = DIM == 3 ? min(cz + P.reach[2], lim) : 0;
+    const int y0 = max(cy - P.reach[1], 0), y1 = min(cy + P.reach[1], lim);
+    const int x0 = max(cx - P.reach[0], 0), x1 = min(cx + P.reach[0], lim);
+    double acc = 0.0;
+    for (int z = z0; z <= z1; ++z) {
+        for (int y = y0; y <= y1; ++y) {
+            uint32_t b, e;
+            row_range(P.cell_end, x0, x1, y, z, g.bits, b, e);
+            float part = 0.0f;
+            for (uint32_t j = b; j < e; ++j) {
+                const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
+                const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
+                const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 <= r2max) {
+                    const float h = P.h != nullptr ? __ldg(P.h + j) : P.h_const;
+                    const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
+                    part += m * sph_w<DIM, KERN>(sqrtf(d2), h);
+                }
+            }
+            acc += (double)part;
+        }
+    }
+    P.out[i] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// KDE on a grid.
+constexpr int kTile3 = 8;            // 8x8x8 grid points per block
+constexpr int kTile2 = 16;           // 16x16 in 2-D
+constexpr int kKdeThreads = 512;     // one grid point per thread (3-D), 256 used in 2-D
+// particles per shared-memory chunk: DIM*T factor rows of (chunk+1) floats
+// must fit the 48 KB of static shared memory (the +1 keeps rows on distinct banks)
+constexpr int kChunk3 = 480;         // 24 rows x 481 x 4 B = 46.2 KB
+constexpr int kChunk2 = 352;         // 32 rows x 353 x 4 B = 45.2 KB
+
+template <int DIM>
+__global__ void __launch_bounds__(kKdeThreads) k_kde_grid(jt_kde_params P) {
+    constexpr int T = DIM == 3 ? kTile3 : kTile2;
+    constexpr int NT = DIM == 3 ? T * T * T : T * T;  // threads that own a grid point
+    constexpr int CH = DIM == 3 ? kChunk3 : kChunk2;
+    __shared__ float fac[DIM * T][CH + 1];             // factors per axis value, per particle of the chunk
+    __shared__ float gcoord[3][T];
+    const int t = threadIdx.x;
+    const int tiles_x = (P.res[0] + T - 1) / T, tiles_y = (P.res[1] + T - 1) / T;
+    const int bx = blockIdx.x % tiles_x;
+    const int by = (blockIdx.x / tiles_x) % tiles_y;
+    const int bz = DIM == 3 ? blockIdx.x / (tiles_x * tiles_y) : 0;
+    const int base[3] = {bx * T, by * T, bz * T};
+    const int cnt[3] = {min(T, P.res[0] - base[0]), min(T, P.res[1] - base[1]),
+                        DIM == 3 ? min(T, P.res[2] - base[2]) : 1};
+    if (t < 3 * T) {
+        const int a = t / T, k = t % T;
+        gcoord[a][k] = (a < DIM && k < cnt[a]) ? __ldg(P.axis[a] + base[a] + k) : 0.0f;
+    }
+    __syncthreads();
+    // this thread's grid point inside the tile
+    int pa, pb, pc;
+    if (DIM == 3) { pa = t / (T * T); pb = (t / T) % T; pc = t % T; }
+    else { pa = t / T; pb = t % T; pc = 0; }
+    const bool owner = t < NT && pa < cnt[0] && pb < cnt[1] && pc < cnt[2];
+    // cell range covering the tile widened by the radius
+    const jt_sort_grid& g = P.grid;
+    const int lim = (1 << g.bits) - 1;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int a = 0; a < DIM; ++a) {
+        lo[a] = cell_of(gcoord[a][0] - P.radius, g.origin[a], g.inv_cell[a], lim);
+        hi[a] = cell_of(gcoord[a][cnt[a] - 1] + P.radius, g.origin[a], g.inv_cell[a], lim);
+    }
+    double acc = 0.0;
+    for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+            uint32_t b, e;
+            row_range(P.cell_end, lo[0], hi[0], cy, cz, g.bits, b, e);
+            {
+                for (uint32_t c0 = b; c0 < e; c0 += CH) {
+                    const int nchunk = (int)min((uint32_t)CH, e - c0);
+                    if (t < nchunk) {
+                        const int64_t j = c0 + t;
+                        const float p[3] = {__ldg(P.particles + 3 * j), __ldg(P.particles + 3 * j + 1),
+                                            __ldg(P.particles + 3 * j + 2)};
+#pragma unroll
+                        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+                            for (int k = 0; k < T; ++k) {
+                                const float d = gcoord[a][k] - p[a];
+                                fac[a * T + k][t] = __expf(-d * d * P.half_inv_h2);
+                            }
+                    }
+                    __syncthreads();
+                    if (owner) {
+                        float part = 0.0f;
+                        const float* fa = fac[pa];
+                        const float* fb = fac[T + pb];
+                        if (DIM == 3) {
+                            const float* fc = fac[2 * T + pc];
+                            for (int j = 0; j < nchunk; ++j) part = fmaf(fa[j] * fb[j], fc[j], part);
+                        } else {
+                            for (int j = 0; j < nchunk; ++j) part = fmaf(fa[j], fb[j], part);
+                        }
+                        acc += (double)part;
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+    if (owner) {
+        const int64_t gi = ((int64_t)(base[0] + pa) * P.res[1] + (base[1] + pb)) * (DIM == 3 ? P.res[2] : 1) +
+                           (DIM == 3 ? base[2] + pc : 0);
+        P.out[gi] = acc;
+    }
+}
+
+// KDE at arbitrary points: one point per thread over the cells within radius.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) k_kde_points(jt_kde_params P, const float* __restrict__ pts, int m,
+                                                       double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const float q[3] = {pts[3 * (int64_t)i], pts[3 * (int64_t)i + 1], DIM == 3 ? pts[3 * (int64_t)i + 2] : 0.0f};
+    const jt_sort_grid& g = P.grid;
+    const int lim = (1 << g.bits) - 1;
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int a = 0; a < DIM; ++a) {
+        lo[a] = cell_of(q[a] - P.radius, g.origin[a], g.inv_cell[a], lim);
+        hi[a] = cell_of(q[a] + P.radius, g.origin[a], g.inv_cell[a], lim);
+    }
+    double acc = 0.0;
+    for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+            {
+                uint32_t b, e;
+                row_range(P.cell_end, lo[0], hi[0], cy, cz, g.bits, b, e);
+                float part = 0.0f;
+                for (uint32_t j = b; j < e; ++j) {
+                    const float dx = q[0] - __ldg(P.particles + 3 * (int64_t)j);
+                    const float dy = q[1] - __ldg(P.particles + 3 * (int64_t)j + 1);
+                    const float dz = DIM == 3 ? q[2] - __ldg(P.particles + 3 * (int64_t)j + 2) : 0.0f;
+                    part += __expf(-(dx * dx + dy * dy + dz * dz) * P.half_inv_h2);
+                }
+                acc += (double)part;
+            }
+        }
+    out[i] = acc;
+}
+
+}  // namespace jt
+
+using namespace jt;
+
+extern "C" int jt_sph_density(const jt_sph_params* p, void* stream) {
+    if (p == nullptr) return set_error(JT_ERR_INVALID, "params is NULL");
+    if (p->dims != 2 && p->dims != 3) return set_error(JT_ERR_INVALID, "dims must be 2 or 3");
+    if (p->kernel < JT_SPH_CUBIC || p->kernel > JT_SPH_GAUSSIAN) return set_error(JT_ERR_INVALID, "unknown SPH kernel");
+    if (p->grid.bits < 1 || p->grid.bits > 7) return set_error(JT_ERR_INVALID, "grid bits must be 1..7");
+    if (p->n_queries < 0 || p->n_particles < 0) return set_error(JT_ERR_INVALID, "negative size");
+    if (p->n_queries == 0) return JT_OK;
+    if (p->queries == nullptr || p->out == nullptr || p->cell_end == nullptr || (p->n_particles > 0 && p->particles == nullptr))
+        return set_error(JT_ERR_INVALID, "queries, out, cell_end and particles are required");
+    for (int a = 0; a < 3; ++a)
+        if (p->reach[a] < 0 || p->reach[a] > 127) return set_error(JT_ERR_INVALID, "reach must be 0..127");
+    const unsigned gb = grid_blocks(p->n_queries);
+    cudaStream_t st = (cudaStream_t)stream;
+#define JT_SPH_LAUNCH(D, K) k_sph<D, K><<<gb, kBlock, 0, st>>>(*p)
+    if (p->dims == 3) {
+        if (p->kernel == JT_SPH_CUBIC) JT_SPH_LAUNCH(3, JT_SPH_CUBIC);
+        else if (p->kernel == JT_SPH_WENDLAND) JT_SPH_LAUNCH(3, JT_SPH_WENDLAND);
+        else JT_SPH_LAUNCH(3, JT_SPH_GAUSSIAN);
+    } else {
+        if (p->kernel == JT_SPH_CUBIC) JT_SPH_LAUNCH(2, JT_SPH_CUBIC);
+        else if (p->kernel == JT_SPH_WENDLAND) JT_SPH_LAUNCH(2, JT_SPH_WENDLAND);
+        else JT_SPH_LAUNCH(2, JT_SPH_GAUSSIAN);
+    }
+#undef JT_SPH_LAUNCH
+    return cuda_status(cudaGetLastError(), "SPH kernel launch");
+}
+
+static int check_kde(const jt_kde_params* p) {
+    if (p == nullptr) return set_error(JT_ERR_INVALID, "params is NULL");
+    if (p->dims != 2 && p->dims != 3) return set_error(JT_ERR_INVALID, "dims must be 2 or 3");
+    if (p->grid.bits < 1 || p->grid.bits > 7) return set_error(JT_ERR_INVALID, "grid bits must be 1..7");
+    if (p->n_particles < 0) return set_error(JT_ERR_INVALID, "negative size");
+    if (p->cell_end == nullptr || (p->n_particles > 0 && p->particles == nullptr))
+        return set_error(JT_ERR_INVALID, "cell_end and particles are required");
+    if (!(p->radius >= 0.0f) || !(p->half_inv_h2 > 0.0f)) return set_error(JT_ERR_INVALID, "bad radius or bandwidth");
+    return JT_OK;
+}
+
+extern "C" int jt_kde_grid(const jt_kde_params* p, void* stream) {
+    int rc;
+    if ((rc = check_kde(p))) return rc;
+    const int D = p->dims;
+    for (int a = 0; a < D; ++a)
+        if (p->res[a] < 1 || p->axis[a] == nullptr) return set_error(JT_ERR_INVALID, "grid axis %d is empty", a);
+    if (D == 2 && p->res[2] != 1) return set_error(JT_ERR_INVALID, "2-D grids have res[2] == 1");
+    if (p->out == nullptr) return set_error(JT_ERR_INVALID, "out is NULL");
+    const int T = D == 3 ? kTile3 : kTile2;
+    int64_t blocks = (int64_t)((p->res[0] + T - 1) / T) * ((p->res[1] + T - 1) / T);
+    if (D == 3) blocks *= (p->res[2] + T - 1) / T;
+    if (blocks > 0x7fffffff) return set_error(JT_ERR_INVALID, "grid too large");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (D == 3) k_kde_grid<3><<<(unsigned)blocks, kKdeThreads, 0, st>>>(*p);
+    else k_kde_grid<2><<<(unsigned)blocks, kKdeThreads, 0, st>>>(*p);
+    return cuda_status(cudaGetLastError(), "KDE grid kernel launch");
+}
+
+extern "C" int jt_kde_points(const jt_kde_params* p, const float* points, int32_t m, double* out, void* stream) {
+    int rc;
+    if ((rc = check_kde(p))) return rc;
+    if (m < 0) return set_error(JT_ERR_INVALID, "m must be >= 0");
+    if (m == 0) return JT_OK;
+    if (points == nullptr || out == nullptr) return set_error(JT_ERR_INVALID, "points and out are required");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p->dims == 3) k_kde_points<3><<<grid_blocks(m), kBlock, 0, st>>>(*p, points, m, out);
+    else k_kde_points<2><<<grid_blocks(m), kBlock, 0, st>>>(*p, points, m, out);
+    return cuda_status(cudaGetLastError(), "KDE points kernel launch");
+}

@@ -16,15 +16,6 @@ namespace jt {
 constexpr int kScanBlock = 1024;            // threads of the scan kernels
 constexpr int kScanItems = 2 * kScanBlock;  // bins per scan block
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-    v &= 0x3ff;
-    v = (v | (v << 16)) & 0x030000ff;
-    v = (v | (v << 8)) & 0x0300f00f;
-    v = (v | (v << 4)) & 0x030c30c3;
-    v = (v | (v << 2)) & 0x09249249;
-    return v;
-}
-
 __global__ void __launch_bounds__(kBlock) k_cell_keys(jt_sort_grid g, const float* __restrict__ pos, int n,
                                                       uint32_t* __restrict__ keys, uint32_t* __restrict__ hist) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -37,7 +28,8 @@ __global__ void __launch_bounds__(kBlock) k_cell_keys(jt_sort_grid g, const floa
         int ci = (f != f) ? 0 : (f < 0.0f ? 0 : (f > (float)lim ? lim : (int)f));
         c[a] = (uint32_t)ci;
     }
-    const uint32_t key = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+    const uint32_t key = g.order == JT_ORDER_LINEAR ? (((c[2] << g.bits) | c[1]) << g.bits) | c[0]
+                                                    : morton3(c[0], c[1], c[2]);
     keys[i] = key;
     atomicAdd(hist + key, 1u);
 }
@@ -165,6 +157,21 @@ extern "C" int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_i
         return set_error(JT_ERR_NOMEM, "workspace of %zu bytes < %zu needed", workspace_bytes,
                          sort_workspace_bytes(n, g->bits));
     return cell_sort(*g, n, pos_in, comp_in, ids_in, pos_out, comp_out, ids_out, workspace, (cudaStream_t)stream);
+}
+
+extern "C" int jt_cell_list(const jt_sort_grid* g, int32_t n, const float* pos_in, float* pos_out, int32_t* ids_out,
+                            uint32_t* cell_end, void* workspace, size_t workspace_bytes, void* stream) {
+    if (cell_end == nullptr) return set_error(JT_ERR_INVALID, "cell_end is required");
+    if (g == nullptr || g->bits < 1 || g->bits > 7) return set_error(JT_ERR_INVALID, "bits must be 1..7");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t bins = n_bins(g->bits);
+    if (n == 0) return cuda_status(cudaMemsetAsync(cell_end, 0, bins * 4, st), "cell list memset");
+    const int rc = jt_cell_sort(g, n, pos_in, nullptr, nullptr, pos_out, nullptr, ids_out, workspace, workspace_bytes,
+                                stream);
+    if (rc != JT_OK) return rc;
+    // after the scatter the histogram words hold each cell's end offset
+    return cuda_status(cudaMemcpyAsync(cell_end, workspace, bins * 4, cudaMemcpyDeviceToDevice, st),
+                       "cell list copy");
 }
 
 // ---------------------------------------------------------------------------

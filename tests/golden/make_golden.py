@@ -196,6 +196,32 @@ def phase_numpy(ref: str):
     traj = tr.track_particles(seeds, (0.0, 2.0), 101, dt=0.02)
     np.savez_compressed(HERE / "nearest.npz", nodes=nodes, D=Dn, st=stn, q=q, outs=outs, qn=qn, vort=vort, vt=vt,
                         seeds=seeds, quick_traj=traj.positions)
+    # A7: density passes (KDE pure-NumPy formula with SciPy switched off; SPH brute force)
+    from jaxtrace.density import kde as kde_mod
+    from jaxtrace.density.kde import KDEEstimator
+    from jaxtrace.density.sph import SPHDensityEstimator
+    kde_mod.SCIPY_AVAILABLE = False
+    drng = np.random.default_rng(99)
+    Pd = np.concatenate([drng.normal(0.5, 0.12, (900, 3)), drng.random((600, 3))]).astype(F32)
+    dens = {"P": Pd}
+    k3 = KDEEstimator(Pd, bandwidth_rule="scott", resolution=12)
+    X, Y, Z, D = k3.evaluate_3d()
+    dens.update(kde_h=np.float64(k3.h), kde3_X=X, kde3_Y=Y, kde3_Z=Z, kde3_D=D)
+    k2 = KDEEstimator(Pd, bandwidth_rule="silverman", resolution=20, plane="xz", slab_position=0.5, slab_thickness=0.3)
+    X2, Y2, Z2 = k2.evaluate_2d()
+    dens.update(kde2_h=np.float64(k2.h), kde2_X=X2, kde2_Y=Y2, kde2_Z=Z2)
+    qk = drng.uniform(-0.1, 1.1, (300, 3)).astype(F32)
+    dens.update(kde_q=qk, kde_pts=np.asarray(k3.evaluate(qk), dtype=F32))
+    for kern in ("cubic_spline", "wendland", "gaussian"):
+        s3 = SPHDensityEstimator(Pd, dimensions="3d", smoothing_length=0.08, kernel_type=kern)
+        dens[f"sph3_{kern}"] = np.asarray(s3.evaluate(Pd), dtype=F32)
+    s2 = SPHDensityEstimator(Pd, dimensions="2d", plane="xy", position=0.5, slab_thickness=0.4)
+    dens["sph2_default_h"] = np.float64(s2._mean_h)
+    dens["sph2_default"] = np.asarray(s2.evaluate(Pd), dtype=F32)
+    sa = SPHDensityEstimator(Pd[:400], dimensions="3d", adaptive=True, n_neighbors=16)
+    dens["sph3_adaptive_h"] = np.asarray(sa.smoothing_lengths, dtype=F32)
+    dens["sph3_adaptive"] = np.asarray(sa.evaluate(Pd[:400]), dtype=F32)
+    np.savez_compressed(HERE / "density.npz", **dens)
     print("phase numpy: done")
 
 
