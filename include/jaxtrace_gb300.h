@@ -281,6 +281,30 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
                        const float* dt_per_particle, const float* x_in,
                        float* x_out, int32_t n, int32_t* status, void* stream);
 
+/* ---- adjoint ------------------------------------------------------------- */
+/* No reference counterpart: JAXTrace has no gradients (no jax.grad on this
+ * path).  Reverse-mode RK4 for loss gradients with respect to the initial
+ * positions and the snapshot values, one checkpoint segment per call. */
+#define JT_ADJOINT_MAX_SEGMENT 64
+typedef struct {
+    int32_t n_particles;
+    int32_t step_begin, step_end;  /* the segment, at most JT_ADJOINT_MAX_SEGMENT steps */
+    float dt, dt_half, dt_sixth;   /* as jt_track_params                    */
+    int32_t pad;
+    const jt_blend* schedule;      /* as jt_track_params.schedule          */
+    const float* ckpt;             /* device (N,3): positions at step_begin (forward checkpoint) */
+    float* lambda;                 /* device (N,3): dL/dx at step_end on entry, at step_begin on exit */
+    float* grad;                   /* device, the field's pair-record layout in float32
+                                      (n_pairs, nodes, 8): += dL/dA in slots 0,1,4 and dL/dB
+                                      in slots 2,3,5 (A = snapshot p, B = snapshot p+1) */
+} jt_adjoint_params;
+
+/* One backward segment over a float32 regular-grid field with per-axis box
+ * boundaries: recomputes the segment from its checkpoint with the forward
+ * (exact) arithmetic, then propagates lambda back step by step and
+ * accumulates the snapshot gradient (vector atomics). */
+int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, const jt_adjoint_params* p, void* stream);
+
 /* ---- locality sort ------------------------------------------------------ */
 /* Cell grid of the sort: cell = clamp(floor((x-origin)*inv_cell), 0, 2^bits-1)
  * per axis; cells ordered by Morton key (tracking locality) or row-major

@@ -94,6 +94,11 @@ class SortGrid(C.Structure):
     _fields_ = [("origin", f32 * 3), ("inv_cell", f32 * 3), ("bits", i32), ("order", i32)]
 
 
+class AdjointParams(C.Structure):
+    _fields_ = [("n_particles", i32), ("step_begin", i32), ("step_end", i32), ("dt", f32), ("dt_half", f32),
+                ("dt_sixth", f32), ("pad", i32), ("schedule", vp), ("ckpt", vp), ("lambda_", vp), ("grad", vp)]
+
+
 JT_ORDER_MORTON, JT_ORDER_LINEAR = 0, 1
 JT_SPH_CUBIC, JT_SPH_WENDLAND, JT_SPH_GAUSSIAN = 0, 1, 2
 
@@ -162,6 +167,7 @@ def load(build_if_missing: bool = True):
         "jt_sph_density": (i32, [P(SphParams), vp]),
         "jt_kde_grid": (i32, [P(KdeParams), vp]),
         "jt_kde_points": (i32, [P(KdeParams), vp, i32, vp, vp]),
+        "jt_adjoint_rk4": (i32, [P(Field), P(Boundary), P(AdjointParams), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

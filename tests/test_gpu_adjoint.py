@@ -1,0 +1,133 @@
+"""The adjoint RK4 kernel against central finite differences of the float64
+oracle.  The trilinear field is C0 with derivative jumps on cell faces; a
+finite difference that straddles a face differs from the exact derivative,
+so agreement is required for a large majority of samples, not all of them:
+at least 85 % within 1e-3 relative and a median below 1e-4 (h = 1e-5 in
+float64, where round-off is ~1e-11 relative)."""
+import numpy as np
+import pytest
+
+import jaxtrace_gb300 as jt
+import oracle
+from jaxtrace_gb300 import workloads as W
+from jaxtrace_gb300.adjoint import AdjointRK4
+
+pytestmark = pytest.mark.gpu
+F32 = np.float32
+
+
+def _setup(n=16, n_snap=6, npart=256, seed=3):
+    g = (np.arange(n) / n).astype(F32)
+    st = np.linspace(0, 1, n_snap).astype(F32)
+    data = W.abc_snapshots(W.grid_nodes(g, g, g), st)
+    rng = np.random.default_rng(seed)
+    x0 = rng.random((npart, 3)).astype(F32)
+    y = rng.random((npart, 3)).astype(np.float64)
+    return g, st, data, x0, y
+
+
+def _oracle_final(spec, x0, times, dt):
+    out, _, _ = oracle.track(spec, oracle.BoundarySpec(kinds=("periodic",) * 3), x0, times, dt,
+                             precision=oracle.ORC_F64)
+    return out
+
+
+def _score(ad, fd):
+    rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
+    return float(np.mean(rel < 1e-3)), float(np.median(rel))
+
+
+def test_adjoint_gradients_match_finite_differences():
+    import torch
+    g, st, data, x0, y = _setup()
+    T, steps, dt = 31, 30, 0.01
+    solver = AdjointRK4(st, g, g, g, "periodic", jt.periodic_boundary(W.UNIT), checkpoint_every=8)
+    x0_t = torch.tensor(x0, device="cuda", requires_grad=True)
+    U_t = torch.tensor(data.reshape(len(st), 16, 16, 16, 3), device="cuda", requires_grad=True)
+    xT = solver(x0_t, U_t, (0.0, 0.3), T, dt=dt)
+    # the forward pass is the exact tracking path
+    f = jt.StructuredTimeSeriesField(data, st, g, g, g, "periodic")
+    ref = jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT), record_final_only=True).track_particles(
+        x0, (0.0, 0.3), T, dt=dt).positions[-1]
+    assert np.array_equal(xT.detach().cpu().numpy(), ref)
+    loss = ((xT.double() - torch.tensor(y, device="cuda")) ** 2).sum()
+    loss.backward()
+    gx = x0_t.grad.cpu().numpy().astype(np.float64)
+    gU = U_t.grad.cpu().numpy().reshape(len(st), -1, 3).astype(np.float64)
+
+    spec = oracle.GridSpec(data, st, g, g, g, "periodic")
+    times = np.linspace(0.0, 0.3, T, dtype=F32)
+    rng = np.random.default_rng(11)
+    h = 1e-5
+    # dL/dx0: each particle moves alone, so the difference of its own loss term suffices
+    picks = [(int(i), int(a)) for i, a in zip(rng.integers(0, len(x0), 48), rng.integers(0, 3, 48))]
+    ad, fd = [], []
+    for i, a in picks:
+        xs = np.repeat(x0[i:i + 1].astype(np.float64), 2, axis=0)
+        xs[0, a] += h
+        xs[1, a] -= h
+        xp, xm = np.float32(xs[0, a]), np.float32(xs[1, a])
+        pair = np.repeat(x0[i:i + 1], 2, axis=0)
+        pair[0, a], pair[1, a] = xp, xm
+        out = _oracle_final(spec, pair, times, dt)
+        lp = np.sum((out[0] - y[i]) ** 2)
+        lm = np.sum((out[1] - y[i]) ** 2)
+        fd.append((lp - lm) / (float(xp) - float(xm)))
+        ad.append(gx[i, a])
+    frac, med = _score(np.array(ad), np.array(fd))
+    assert frac >= 0.85 and med < 1e-4, (frac, med)
+
+    # dL/dU: perturb one snapshot value, rerun every particle
+    def full_loss(d):
+        s = oracle.GridSpec(d, st, g, g, g, "periodic")
+        return np.sum((_oracle_final(s, x0, times, dt) - y) ** 2)
+
+    upicks = [(int(t), int(nd), int(c)) for t, nd, c in zip(rng.integers(0, len(st), 24),
+                                                            rng.integers(0, data.shape[1], 24),
+                                                            rng.integers(0, 3, 24))]
+    # keep entries that some particle actually samples
+    ad, fd = [], []
+    for t, nd, c in upicks:
+        if gU[t, nd, c] == 0.0:
+            continue
+        dp, dm = data.copy(), data.copy()
+        hv = np.float32(1e-3)
+        dp[t, nd, c] += hv
+        dm[t, nd, c] -= hv
+        step = float(dp[t, nd, c]) - float(dm[t, nd, c])
+        fd.append((full_loss(dp) - full_loss(dm)) / step)
+        ad.append(gU[t, nd, c])
+    if ad:
+        frac, med = _score(np.array(ad), np.array(fd))
+        assert frac >= 0.85 and med < 1e-3, (frac, med)
+
+
+def test_adjoint_reflective_and_segments():
+    """Reflective walls (the cotangent flips sign on a fold) and a last segment
+    shorter than the checkpoint interval."""
+    import torch
+    g, st, data, x0, y = _setup(n=12, npart=128, seed=4)
+    g = np.linspace(0, 1, 12).astype(F32)
+    data = W.abc_snapshots(W.grid_nodes(g, g, g), st)
+    bc = jt.reflective_boundary(W.UNIT)
+    solver = AdjointRK4(st, g, g, g, "clamp", bc, checkpoint_every=7)
+    x0_t = torch.tensor(x0, device="cuda", requires_grad=True)
+    U_t = torch.tensor(data.reshape(len(st), 12, 12, 12, 3), device="cuda", requires_grad=True)
+    xT = solver(x0_t, U_t, (0.0, 0.2), 21, dt=0.01)
+    loss = ((xT.double() - torch.tensor(y, device="cuda")) ** 2).sum()
+    loss.backward()
+    gx = x0_t.grad.cpu().numpy().astype(np.float64)
+    spec = oracle.GridSpec(data, st, g, g, g, "clamp")
+    times = np.linspace(0.0, 0.2, 21, dtype=F32)
+    obc = oracle.BoundarySpec(kinds=("reflective",) * 3)
+    ad, fd = [], []
+    for i in range(0, 128, 4):
+        for a in range(3):
+            pair = np.repeat(x0[i:i + 1], 2, axis=0)
+            xp, xm = np.float32(float(x0[i, a]) + 1e-5), np.float32(float(x0[i, a]) - 1e-5)
+            pair[0, a], pair[1, a] = xp, xm
+            out, _, _ = oracle.track(spec, obc, pair, times, 0.01, precision=oracle.ORC_F64)
+            fd.append((np.sum((out[0] - y[i]) ** 2) - np.sum((out[1] - y[i]) ** 2)) / (float(xp) - float(xm)))
+            ad.append(gx[i, a])
+    frac, med = _score(np.array(ad), np.array(fd))
+    assert frac >= 0.85 and med < 1e-4, (frac, med)
