@@ -69,6 +69,13 @@ def args_parse():
     p.add_argument("--no-error", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-fem", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--fem-steps", type=int, default=1000)
+    p.add_argument("--leg", default=None, choices=["fem", "batch", "adjoint"],
+                   help="run one configuration leg alone and print its JSON (with --profile: the leg's timed "
+                        "region bracketed by cudaProfilerStart/Stop)")
     p.add_argument("--profile", action="store_true",
                    help="first variant only, no error/e2e/CPU legs; the timed region is bracketed by "
                         "cudaProfilerStart/Stop for ncu --profile-from-start off")
@@ -200,6 +207,275 @@ def run_reference(a, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_leg(a):
+    """Differentiation configuration: plain ABC field at 64^3 (16 snapshots,
+    periodic), 256x256x64 lattice seeds, RK4 dt=0.01, 500 steps, checkpoint
+    every 50; loss = sum |x_T - y|^2 with y ~ U[0,1)^3 (default_rng(3)).
+    Times the forward pass (with checkpoints) and the backward pass, and
+    checks dL/dx0 against float64 central differences on sampled particles."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    import oracle
+    from jaxtrace_gb300 import workloads as W
+    from jaxtrace_gb300.adjoint import AdjointRK4
+    c = W.plain_rk4(n_particles=1, n=64, n_snap=16)
+    g = c["grid"][0]
+    x0 = jt.uniform_grid_seeds((256, 256, 64), W.UNIT)
+    n = len(x0)
+    y = np.random.default_rng(3).uniform(size=(n, 3)).astype(np.float32)
+    solver = AdjointRK4(c["times"], g, g, g, "periodic", jt.periodic_boundary(W.UNIT), checkpoint_every=50)
+    x0_t = torch.tensor(x0, device="cuda", requires_grad=True)
+    U_t = torch.tensor(c["data"].reshape(16, 64, 64, 64, 3), device="cuda", requires_grad=True)
+    y_t = torch.tensor(y, device="cuda")
+    n_steps, dt = 500, 0.01
+    fwd_ms, bwd_ms = [], []
+    for it in range(a.warmup + a.steps):
+        x0_t.grad = None
+        U_t.grad = None
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record()
+        xT = solver(x0_t, U_t, (0.0, n_steps * dt), n_steps + 1, dt=dt)
+        e[1].record()
+        loss = ((xT - y_t) ** 2).sum()
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        if it >= a.warmup:
+            fwd_ms.append(e[0].elapsed_time(e[1]))
+            bwd_ms.append(e[1].elapsed_time(e[2]))
+    gx = x0_t.grad.cpu().numpy().astype(np.float64)
+    # float64 central differences of single particles (each particle's loss term is its own)
+    spec = oracle.GridSpec(c["data"], c["times"], g, g, g, "periodic")
+    obc = oracle.BoundarySpec(kinds=("periodic",) * 3)
+    rng = np.random.default_rng(17)
+    fd_stats = {}
+    for horizon in (50, 500):
+        if horizon != n_steps:
+            # a shorter horizon needs its own adjoint
+            xs = torch.tensor(x0[:4096], device="cuda", requires_grad=True)
+            xh = solver(xs, U_t.detach(), (0.0, horizon * dt), horizon + 1, dt=dt)
+            ((xh - y_t[:4096]) ** 2).sum().backward()
+            gref = xs.grad.cpu().numpy().astype(np.float64)
+            pool = 4096
+        else:
+            gref, pool = gx, n
+        times = np.linspace(0.0, horizon * dt, horizon + 1, dtype=np.float32)
+        picks = list(zip(rng.integers(0, pool, 96), rng.integers(0, 3, 96)))
+        for h in (1e-3, 1e-5):
+            ad, fd = [], []
+            for i, ax in picks:
+                pair = np.repeat(x0[i:i + 1], 2, axis=0)
+                xp, xm = np.float32(float(x0[i, ax]) + h), np.float32(float(x0[i, ax]) - h)
+                pair[0, ax], pair[1, ax] = xp, xm
+                out, _, _ = oracle.track(spec, obc, pair, times, dt, precision=oracle.ORC_F64)
+                fd.append((np.sum((out[0] - y[i]) ** 2) - np.sum((out[1] - y[i]) ** 2)) / (float(xp) - float(xm)))
+                ad.append(gref[i, ax])
+            ad, fd = np.array(ad), np.array(fd)
+            rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
+            fd_stats[f"{horizon}_steps_h{h:g}"] = {"frac_within_1e-3": float(np.mean(rel < 1e-3)),
+                                                  "median_rel": float(np.median(rel)), "samples": int(len(rel))}
+    # dL/dU of a 2048-particle subset's loss against float64 central differences
+    # (h = 1e-3 on one snapshot value; each difference reruns the subset in the oracle)
+    m = 2048
+    xs = torch.tensor(x0[:m], device="cuda")
+    Us = U_t.detach().clone().requires_grad_(True)
+    xh = solver(xs, Us, (0.0, n_steps * dt), n_steps + 1, dt=dt)
+    ((xh - y_t[:m]) ** 2).sum().backward()
+    gU = Us.grad.cpu().numpy().reshape(16, -1, 3).astype(np.float64)
+    nz = np.argwhere(gU != 0.0)
+    times = np.linspace(0.0, n_steps * dt, n_steps + 1, dtype=np.float32)
+
+    def sub_loss(d):
+        s = oracle.GridSpec(d, c["times"], g, g, g, "periodic")
+        o, _, _ = oracle.track(s, obc, x0[:m], times, dt, precision=oracle.ORC_F64)
+        return float(np.sum((o - y[:m]) ** 2))
+
+    ad, fd = [], []
+    for t, nd, cc in nz[rng.choice(len(nz), size=min(24, len(nz)), replace=False)]:
+        dp, dm = c["data"].copy(), c["data"].copy()
+        dp[t, nd, cc] += np.float32(1e-3)
+        dm[t, nd, cc] -= np.float32(1e-3)
+        fd.append((sub_loss(dp) - sub_loss(dm)) / (float(dp[t, nd, cc]) - float(dm[t, nd, cc])))
+        ad.append(gU[t, nd, cc])
+    ad, fd = np.array(ad), np.array(fd)
+    rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
+    fd_U = {"frac_within_1e-3": float(np.mean(rel < 1e-3)), "median_rel": float(np.median(rel)),
+            "samples": int(len(rel)), "subset_particles": m, "h": 1e-3}
+    f, b = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
+    return {"fd_check_dL_dU": fd_U,
+            "workload": "differentiation: 64^3 periodic ABC, 16 snapshots, 4,194,304 lattice seeds, RK4 dt=0.01, "
+                        "500 steps, checkpoint every 50, loss sum|x_T - y|^2",
+            "forward_ms": f, "backward_ms": b, "backward_over_forward": b / f,
+            "forward_particle_steps_per_s": n * n_steps / (f / 1e3),
+            "adjoint_particle_steps_per_s": n * n_steps / (b / 1e3),
+            "fd_check_dL_dx0": fd_stats,
+            "fd_note": "float64 central differences of single particles at h=1e-3 and h=1e-5 on x0; trilinear "
+                       "cell faces make the exact derivative jump, so the wider step and the longer horizon "
+                       "have more samples whose difference straddles a face"}
+
+
+def _mesh_oracle_spec(c, f):
+    import oracle
+    m = f.octree_mesh
+    return oracle.MeshSpec(c["data"], c["times"], c["points"], c["tets"], m.element_bounds, m.nodes_min,
+                           m.nodes_max, m.nodes_elements, m.nodes_children, m.nodes_is_leaf,
+                           max_depth=m.max_depth)
+
+
+def _timed(fn, reps):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def fem_leg(a, profile=False):
+    """Unstructured FEM configuration: 64^3 hexes split into 6 jittered Kuhn
+    tets (1,572,864 tets), 32 FP32 snapshots, octree location + P1, 1M
+    particles, x/z periodic and y reflective, RK4 dt=0.005, 1000 steps.
+    Parity: every 1000th particle against the float32 oracle (bit-exact
+    count) and the float64 oracle (relative error)."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    import oracle
+    from jaxtrace_gb300 import _lib as L
+    from jaxtrace_gb300 import workloads as W
+    n_steps = a.fem_steps
+    c = W.fem_case(n_steps=n_steps)
+    f = jt.OctreeFEMTimeSeriesFieldOptimized(c["data"], c["times"], c["points"], c["tets"])
+    bc = jt.mixed_boundary(W.UNIT, c["conditions"])
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
+    times = np.linspace(c["time_span"][0], c["time_span"][1], c["n_timesteps"], dtype=np.float32)
+    x0 = torch.from_numpy(c["x0"]).cuda()
+    pos = torch.empty_like(x0)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sched = torch.from_numpy(tr._schedule(times, c["dt"]).view(np.int32).reshape(-1, 8)).cuda()
+    timers = []
+
+    def one(t=None):
+        pos.copy_(x0)
+        return tr.track_device(pos, times, c["dt"], status, None, sched, timers=t)
+
+    for _ in range(1 if profile else 2):
+        one()
+    torch.cuda.synchronize()
+    if profile:
+        torch.cuda.profiler.start()
+    ms = _timed(lambda: one(timers), 1 if profile else 2)
+    if profile:
+        torch.cuda.profiler.stop()
+        return {}
+    n = len(c["x0"])
+    launch_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in timers]))
+    n_launch = len(timers) / 2
+    bpp = 4 * (16 + 4 * 12 + 2 * 4 * 12) + 24      # connectivity + vertices + two snapshots' values
+    units = n * n_steps / n_launch
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    final = pos.cpu().numpy()
+    sub = np.arange(0, n, 1000)
+    spec = _mesh_oracle_spec(c, f)
+    obc = oracle.BoundarySpec(kinds=("periodic", "reflective", "periodic"))
+    t0 = time.perf_counter()
+    o32, _, info = oracle.track(spec, obc, c["x0"][sub], times, c["dt"])
+    cpu_s = time.perf_counter() - t0
+    o64, _, _ = oracle.track(spec, obc, c["x0"][sub], times, c["dt"], precision=oracle.ORC_F64)
+    same = np.all(final[sub].view(np.uint32) == o32.view(np.uint32), axis=1)
+    rel = np.linalg.norm(final[sub] - o64, axis=1) / np.maximum(np.linalg.norm(o64, axis=1), 1e-30)
+    return {"workload": "unstructured FEM: 64^3 hexes x 6 jittered tets (1,572,864), 32 FP32 snapshots, octree + "
+                        f"P1, 1,000,000 particles, x/z periodic y reflective, RK4 dt=0.005, {n_steps} steps",
+            "value": n * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "status": int(status.item()),
+            "roofline": {"bound": "hbm", "achieved": units * bpp / (launch_ms / 1e3) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": units * bpp / (launch_ms / 1e3) / 1e9 / peak,
+                         "kernel": "k_track (RK4, octree mesh field, f32)", "bytes_per_particle_step": bpp,
+                         "note": "P1 bytes exclude the octree search"},
+            "parity_f32_oracle": {"bit_exact_fraction": float(np.mean(same)), "particles": len(sub),
+                                  "oracle_fallbacks": info["fallback_count"]},
+            "error_vs_fp64": {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)),
+                              "max": float(rel.max())},
+            "cpu_baseline": {"value": len(sub) * n_steps / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1,
+                             "kind": "port", "sample": f"{len(sub)} particles (every 1000th) x {n_steps} steps, "
+                                                       "float32 C restatement of the octree/P1 path, OpenMP"}}
+
+
+def batch_leg(a, profile=False):
+    """Batching + density configuration: 256 ensembles of round(10^U(3,6))
+    particles (default_rng(7); 36,800,084 in all) released at U(0,0.5) on the
+    FEM mesh, 400 RK4 steps of dt=0.005 each from its own release time, in
+    one tracking pass (autotuned, captured in a CUDA graph); then cubic-spline
+    SPH (h=0.02, 3-D) at, and a Scott-bandwidth Gaussian KDE on the 100^3
+    grid of, the first 16,000,000 final positions."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    import oracle
+    from jaxtrace_gb300 import workloads as W
+    c = W.fem_case(n_particles=1)
+    f = jt.OctreeFEMTimeSeriesFieldOptimized(c["data"], c["times"], c["points"], c["tets"])
+    bc = jt.mixed_boundary(W.UNIT, c["conditions"])
+    sizes, release, xs = W.ensembles()
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
+    b = tr.ensemble_batch(xs, release, 401, dt=0.005)
+    tune = jt.Autotuner(cache_path="").tune_batch(b)
+    b.capture()
+    b.run()
+    torch.cuda.synchronize()
+    if profile:
+        torch.cuda.profiler.start()
+    ms = _timed(b.run, 1 if profile else 2)
+    if profile:
+        torch.cuda.profiler.stop()
+        return {}
+    n = b.n
+    status = b.check_status()
+    # eager pass for comparison: the graph saves the host launch overhead only
+    eager = tr.ensemble_batch(xs, release, 401, dt=0.005)
+    eager.run()
+    ms_eager = _timed(eager.run, 1)
+    # parity: a few ensembles' first particles against the float32 oracle
+    spec = _mesh_oracle_spec(c, f)
+    obc = oracle.BoundarySpec(kinds=("periodic", "reflective", "periodic"))
+    fin = b.pos.cpu().numpy()
+    del eager
+    exact, tot = 0, 0
+    for e in range(0, 256, 16):
+        lo = int(b.offsets[e])
+        k = min(64, int(sizes[e]))
+        o, _, _ = oracle.track(spec, obc, xs[e][:k], b.times[e], b.dt)
+        exact += int(np.sum(np.all(fin[lo:lo + k].view(np.uint32) == o.view(np.uint32), axis=1)))
+        tot += k
+    out = {"workload": "batching: 256 ensembles (sizes round(10^U(3,6)), default_rng(7)), "
+                       f"{n:,} particles, release U(0,0.5), FEM mesh, 400 RK4 steps dt=0.005 each",
+           "value": n * 400 / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "ms_per_pass_eager": ms_eager,
+           "cuda_graph": True, "status": status,
+           "autotune": {"block_size": tune.block_size, "sort_every": tune.sort_every, "sort_bits": tune.sort_bits,
+                        "trials": len(tune.trials)},
+           "parity_f32_oracle": {"bit_exact_fraction": exact / max(tot, 1), "particles": tot}}
+    # density passes on the first 16,000,000 final positions
+    P = b.pos[:16_000_000].contiguous()
+    del b
+    torch.cuda.empty_cache()
+    from jaxtrace_gb300.density import KDEEstimator, SPHDensityEstimator
+    sph = SPHDensityEstimator(P, dimensions="3d", smoothing_length=0.02, kernel_type="cubic_spline")
+    sph.evaluate(P[:1024])
+    sph_ms = _timed(lambda: sph._density_sum(P), 1)
+    kde = KDEEstimator(P, bandwidth_rule="scott")
+    kde.evaluate_3d()
+    kde_ms = _timed(kde.evaluate_3d, 1)
+    out["density"] = {"particles": int(P.shape[0]), "sph_ms": sph_ms, "sph_queries_per_s": P.shape[0] / (sph_ms / 1e3),
+                      "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3",
+                      "kde_particles_per_s": P.shape[0] / (kde_ms / 1e3)}
+    return out
+
+
 def workload_name(a):
     return (f"precision: {a.grid}^3 clamp grid, 64 snapshots ABC+(1,0,0)+N(0,0.01^2) over [0,2], "
             f"{a.seeds ** 3} lattice seeds, continuous inlet x (lattice {a.seeds}x{a.seeds}), "
@@ -213,6 +489,17 @@ def main():
         run_reference(a, world, rank)
         return
     import torch
+    if a.leg is not None:
+        # one configuration leg alone (rank 0 of a single process)
+        from jaxtrace_gb300 import _lib as L
+        L.load()
+        if a.leg == "adjoint":
+            out = {} if a.profile else adjoint_leg(a)
+        else:
+            out = {"fem": fem_leg, "batch": batch_leg}[a.leg](a, profile=a.profile)
+        if rank == 0:
+            print(json.dumps({"leg": a.leg} | out), flush=True)
+        return
 
     import jaxtrace_gb300 as jt
     from jaxtrace_gb300 import _lib as L
@@ -347,6 +634,15 @@ def main():
                        "api": "create_tracker('rk4', field, continuous_inlet, record_final_only=True)"
                               ".track_particles(pinned host x0)"}
     line["clocks"] = clk.summary()
+    if not a.profile and rank == 0:
+        del trackers
+        torch.cuda.empty_cache()
+        if not a.no_adjoint:
+            line["adjoint"] = adjoint_leg(a)
+        if not a.no_fem:
+            line["fem"] = fem_leg(a)
+        if not a.no_batch:
+            line["batching"] = batch_leg(a)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

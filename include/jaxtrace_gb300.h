@@ -46,7 +46,8 @@ extern "C" {
 /* ---- device status bits (OR-ed by kernels into *status) --------------- */
 #define JT_STATUS_INDEX_WRAPPED 0x1 /* periodic cell index hit N (the reference raises IndexError there) */
 #define JT_STATUS_NONFINITE 0x2     /* a non-finite position was produced          */
-#define JT_STATUS_OCTREE_FALLBACK 0x4 /* at least one P1 lookup used the nearest-vertex fallback */
+#define JT_STATUS_OCTREE_FALLBACK 0x4 /* at least one mesh lookup found no containing tet and used
+                                         the nearest-vertex / nearest-node fallback */
 
 /* ---- enums ------------------------------------------------------------- */
 /* snapshot value storage */
@@ -178,9 +179,30 @@ typedef struct {
     const void* pairs;      /* device value pairs indexed by ORIGINAL node id */
 } jt_nearest_field;
 
+/* Tetrahedral mesh field with the hash-grid point location of
+ * FEMTimeSeriesField (fields/fem_time_series.py:16-110,
+ * fields/fem_interpolator.py:36-328): the query's cell of a uniform grid
+ * over the node bounding box (float32 (q - grid_min) / cell_size, floored,
+ * clipped), the cell's elements in ascending order, the first whose box and
+ * barycentric test hold the query gives P1; otherwise the nearest node of
+ * the whole mesh (searched through the embedded nearest-node cell list). */
+typedef struct {
+    jt_nearest_field nearest; /* nodes, nearest-node cell list and the
+                                 snapshot value pairs (indexed by node id)  */
+    int32_t n_tets;
+    int32_t grid_size[3];   /* hash cells per axis; cell id (i*gy + j)*gz + k */
+    float grid_min[3];      /* float32 node bounding-box minimum              */
+    float cell_size[3];     /* float32 cell edges of the lookup               */
+    const float* tet_box;   /* device (n_tets,8): min xyz,0, max xyz,0        */
+    const float* tet_geom;  /* device (n_tets,16) as jt_mesh_field            */
+    const int32_t* cell_start; /* device (cells+1) CSR offsets                 */
+    const int32_t* cell_elems; /* device element ids, ascending within a cell */
+} jt_fem_field;
+
 #define JT_FIELD_GRID 1
 #define JT_FIELD_MESH 2
 #define JT_FIELD_NEAREST 3
+#define JT_FIELD_FEM 4
 
 typedef struct {
     int32_t kind;           /* JT_FIELD_*                                     */
@@ -188,6 +210,7 @@ typedef struct {
     const jt_grid_field* grid;
     const jt_mesh_field* mesh;
     const jt_nearest_field* nearest;
+    const jt_fem_field* fem;
 } jt_field;
 
 /* ---- boundary descriptor ------------------------------------------------ */
@@ -225,9 +248,12 @@ typedef struct {
     int64_t schedule_stride;/* entries between ensembles (0: one schedule)    */
     const int32_t* ens_offsets; /* device (n_ens+1) particle offsets or NULL:
                                    particles [ens_offsets[e], ens_offsets[e+1])
-                                   use schedule + e*schedule_stride        */
+                                   use schedule + e*schedule_stride; the
+                                   particle of slot i is ids[i] when ids is
+                                   set (after a locality sort), else i     */
     int32_t n_ens;
-    int32_t pad_e;
+    int32_t block_size;     /* threads per block of the tracking launch:
+                               0 (256), 64, 128 or 256                     */
     float* pos;             /* device (N,3) in/out                            */
     float* comp;            /* device (N,3) Kahan compensation (COMPENSATED) or NULL */
     float* traj;            /* device (rows,N,3) or NULL                      */

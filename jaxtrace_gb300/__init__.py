@@ -8,12 +8,13 @@ kernels through the C ABI in ``include/jaxtrace_gb300.h``.
 from .boundary import (absorbing_boundary_factory, clamping_boundary, continuous_inlet_boundary_factory,
                        mixed_boundary, no_boundary, periodic_boundary, reflective_boundary, unit_box_periodic,
                        unit_box_reflective)
-from .fields import (OctreeFEMTimeSeriesFieldOptimized, OctreeMesh, StructuredGridSampler,
+from .fields import (FEMTimeSeriesField, FemHashGrid, OctreeFEMTimeSeriesFieldOptimized, OctreeMesh, StructuredGridSampler,
                      StructuredTimeSeriesField, TimeSeriesField)
 from .integrators import euler_step, rk2_step, rk4_step
 from .particles import Trajectory
 from .seeding import random_seeds, uniform_grid_seeds
-from .tracker import ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
+from .tracker import EnsembleBatch, ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
+from .autotune import Autotuner
 
 __version__ = "0.1.0"
 
@@ -23,4 +24,5 @@ __all__ = [
     "create_tracker", "track_particles_simple", "random_seeds", "uniform_grid_seeds", "periodic_boundary",
     "reflective_boundary", "clamping_boundary", "absorbing_boundary_factory", "mixed_boundary",
     "continuous_inlet_boundary_factory", "no_boundary", "unit_box_periodic", "unit_box_reflective",
+    "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid",
 ]

@@ -25,7 +25,7 @@ JT_EULER, JT_RK2, JT_RK4 = 0, 1, 2
 JT_BC_NONE, JT_BC_PERIODIC, JT_BC_REFLECTIVE, JT_BC_CLAMP, JT_BC_ABSORBING = 0, 1, 2, 3, 4
 JT_INLET_OFF, JT_INLET_GRID = 0, 1
 JT_ARITH_EXACT, JT_ARITH_COMPENSATED = 0, 1
-JT_FIELD_GRID, JT_FIELD_MESH, JT_FIELD_NEAREST = 1, 2, 3
+JT_FIELD_GRID, JT_FIELD_MESH, JT_FIELD_NEAREST, JT_FIELD_FEM = 1, 2, 3, 4
 
 STORAGE_CODES = {"f32": JT_STORE_F32, "float32": JT_STORE_F32, "bf16": JT_STORE_BF16,
                  "bfloat16": JT_STORE_BF16, "f16": JT_STORE_F16, "float16": JT_STORE_F16}
@@ -69,9 +69,14 @@ class NearestField(C.Structure):
                 ("points", vp), ("point_ids", vp), ("cell_start", vp), ("pairs", vp)]
 
 
+class FemField(C.Structure):
+    _fields_ = [("nearest", NearestField), ("n_tets", i32), ("grid_size", i32 * 3), ("grid_min", f32 * 3),
+                ("cell_size", f32 * 3), ("tet_box", vp), ("tet_geom", vp), ("cell_start", vp), ("cell_elems", vp)]
+
+
 class Field(C.Structure):
     _fields_ = [("kind", i32), ("pad", i32), ("grid", C.POINTER(GridField)),
-                ("mesh", C.POINTER(MeshField)), ("nearest", C.POINTER(NearestField))]
+                ("mesh", C.POINTER(MeshField)), ("nearest", C.POINTER(NearestField)), ("fem", C.POINTER(FemField))]
 
 
 class Boundary(C.Structure):
@@ -85,7 +90,7 @@ class TrackParams(C.Structure):
     _fields_ = [("integrator", i32), ("arith", i32), ("n_particles", i32), ("step_begin", i32),
                 ("step_end", i32), ("dt", f32), ("dt_half", f32), ("dt_sixth", f32),
                 ("schedule", vp), ("schedule_stride", i64), ("ens_offsets", vp), ("n_ens", i32),
-                ("pad_e", i32), ("pos", vp), ("comp", vp), ("traj", vp), ("vel", vp),
+                ("block_size", i32), ("pos", vp), ("comp", vp), ("traj", vp), ("vel", vp),
                 ("record_every", i32), ("record_compact", i32), ("row_base", i32), ("n_rows", i32),
                 ("status", vp), ("ids", vp)]
 
@@ -119,7 +124,8 @@ class OctreeInfo(C.Structure):
                 ("n_leaves", i32), ("pad", i32)]
 
 
-STRUCTS = [Blend, GridField, OctreeNode, MeshField, NearestField, Field, Boundary, TrackParams, SortGrid]
+STRUCTS = [Blend, GridField, OctreeNode, MeshField, NearestField, Field, Boundary, TrackParams, SortGrid, SphParams,
+           KdeParams, AdjointParams, OctreeInfo, FemField]
 
 
 class JTError(RuntimeError):

@@ -43,6 +43,17 @@ static int check_storage(int s) {
     return JT_OK;
 }
 
+static int check_nearest(const jt_nearest_field* q) {
+    if (q == nullptr) return set_error(JT_ERR_INVALID, "nearest field descriptor is NULL");
+    if (q->n_points < 1 || q->cells[0] < 1 || q->cells[1] < 1 || q->cells[2] < 1)
+        return set_error(JT_ERR_INVALID, "nearest field needs points and a positive cell grid");
+    if (q->points == nullptr || q->point_ids == nullptr || q->cell_start == nullptr || q->pairs == nullptr ||
+        q->n_pairs < 1)
+        return set_error(JT_ERR_INVALID, "nearest field has a NULL array");
+    if (q->pair_stride < q->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
+    return check_storage(q->storage);
+}
+
 static int check_field(const jt_field* f) {
     if (f == nullptr) return set_error(JT_ERR_INVALID, "field is NULL");
     switch (f->kind) {
@@ -70,16 +81,16 @@ static int check_field(const jt_field* f) {
             if (m->pair_stride < m->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
             return check_storage(m->storage);
         }
-        case JT_FIELD_NEAREST: {
-            const jt_nearest_field* q = f->nearest;
-            if (q == nullptr) return set_error(JT_ERR_INVALID, "nearest field descriptor is NULL");
-            if (q->n_points < 1 || q->cells[0] < 1 || q->cells[1] < 1 || q->cells[2] < 1)
-                return set_error(JT_ERR_INVALID, "nearest field needs points and a positive cell grid");
-            if (q->points == nullptr || q->point_ids == nullptr || q->cell_start == nullptr || q->pairs == nullptr ||
-                q->n_pairs < 1)
-                return set_error(JT_ERR_INVALID, "nearest field has a NULL array");
-            if (q->pair_stride < q->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
-            return check_storage(q->storage);
+        case JT_FIELD_NEAREST: return check_nearest(f->nearest);
+        case JT_FIELD_FEM: {
+            const jt_fem_field* h = f->fem;
+            if (h == nullptr) return set_error(JT_ERR_INVALID, "FEM field descriptor is NULL");
+            if (h->n_tets < 1 || h->grid_size[0] < 1 || h->grid_size[1] < 1 || h->grid_size[2] < 1)
+                return set_error(JT_ERR_INVALID, "FEM field needs tetrahedra and a positive hash grid");
+            if (h->tet_box == nullptr || h->tet_geom == nullptr || h->cell_start == nullptr ||
+                h->cell_elems == nullptr)
+                return set_error(JT_ERR_INVALID, "FEM field has a NULL array");
+            return check_nearest(&h->nearest);
         }
         default:
             return set_error(JT_ERR_INVALID, "unknown field kind %d", f->kind);
@@ -125,7 +136,9 @@ extern "C" int jt_struct_sizes(int64_t* out, int32_t n) {
                          (int64_t)sizeof(jt_octree_node),   (int64_t)sizeof(jt_mesh_field),
                          (int64_t)sizeof(jt_nearest_field), (int64_t)sizeof(jt_field),
                          (int64_t)sizeof(jt_boundary),      (int64_t)sizeof(jt_track_params),
-                         (int64_t)sizeof(jt_sort_grid)};
+                         (int64_t)sizeof(jt_sort_grid),     (int64_t)sizeof(jt_sph_params),
+                         (int64_t)sizeof(jt_kde_params),    (int64_t)sizeof(jt_adjoint_params),
+                         (int64_t)sizeof(jt_octree_info),   (int64_t)sizeof(jt_fem_field)};
     const int k = (int)(sizeof(s) / sizeof(s[0]));
     if (out == nullptr || n < k) return set_error(JT_ERR_INVALID, "jt_struct_sizes needs room for %d values", k);
     for (int i = 0; i < k; ++i) out[i] = s[i];
@@ -146,12 +159,15 @@ extern "C" int jt_track(const jt_field* field, const jt_boundary* bc, const jt_t
         return set_error(JT_ERR_INVALID, "recording needs record_every >= 1 and n_rows >= 0");
     if (p->vel != nullptr && p->traj == nullptr)
         return set_error(JT_ERR_INVALID, "velocity recording needs a trajectory buffer");
+    if (p->block_size != 0 && p->block_size != 64 && p->block_size != 128 && p->block_size != 256)
+        return set_error(JT_ERR_INVALID, "block_size must be 0, 64, 128 or 256, got %d", p->block_size);
     if (p->ens_offsets != nullptr && (p->n_ens < 1 || p->schedule_stride < 4LL * p->step_end))
         return set_error(JT_ERR_INVALID, "ensembles need n_ens >= 1 and schedule_stride >= 4*step_end");
     cudaStream_t s = (cudaStream_t)stream;
     switch (field->kind) {
         case JT_FIELD_GRID: return grid_track(*field->grid, *bc, *p, s);
         case JT_FIELD_MESH: return mesh_track(*field->mesh, *bc, *p, s);
+        case JT_FIELD_FEM: return fem_track(*field->fem, *bc, *p, s);
         default: return nearest_track(*field->nearest, *bc, *p, s);
     }
 }
@@ -168,6 +184,7 @@ extern "C" int jt_field_sample(const jt_field* field, const jt_blend* blend, int
     switch (field->kind) {
         case JT_FIELD_GRID: return grid_sample(*field->grid, arith, *blend, pos, out, m, status, s);
         case JT_FIELD_MESH: return mesh_sample(*field->mesh, arith, *blend, pos, out, m, status, s);
+        case JT_FIELD_FEM: return fem_sample(*field->fem, arith, *blend, pos, out, m, status, s);
         default: return nearest_sample(*field->nearest, arith, *blend, pos, out, m, status, s);
     }
 }
@@ -200,6 +217,7 @@ extern "C" int jt_integrator_step(const jt_field* field, const jt_blend* stage_b
     switch (field->kind) {
         case JT_FIELD_GRID: return grid_step(*field->grid, arith, sb, integrator, k, dt_per_particle, x_in, x_out, n, status, s);
         case JT_FIELD_MESH: return mesh_step(*field->mesh, arith, sb, integrator, k, dt_per_particle, x_in, x_out, n, status, s);
+        case JT_FIELD_FEM: return fem_step(*field->fem, arith, sb, integrator, k, dt_per_particle, x_in, x_out, n, status, s);
         default: return nearest_step(*field->nearest, arith, sb, integrator, k, dt_per_particle, x_in, x_out, n, status, s);
     }
 }

@@ -441,7 +441,8 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
     const bool comp = (P.arith == JT_ARITH_COMPENSATED) && P.comp != nullptr;
     const jt_blend* sched = P.schedule;
     if (P.ens_offsets != nullptr && P.n_ens > 0) {
-        sched += (int64_t)find_ensemble(P.ens_offsets, P.n_ens, i) * P.schedule_stride;
+        const int pid = P.ids != nullptr ? __ldg(P.ids + i) : i;
+        sched += (int64_t)find_ensemble(P.ens_offsets, P.n_ens, pid) * P.schedule_stride;
     }
     float* pp = P.pos + 3 * (int64_t)i;
     V3 x{pp[0], pp[1], pp[2]};

@@ -1,0 +1,23 @@
+// Kernel instances for the hash-grid FEM field (FEMTimeSeriesField,
+// fem_time_series.py / fem_interpolator.py).
+#include "jt_fem.cuh"
+#include "jt_kernels.cuh"
+
+namespace jt {
+typedef Launcher<FemField, jt_fem_field, float> FemL;
+
+float nearest_min_cell_edge(const jt_nearest_field& f);
+
+int fem_track(const jt_fem_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
+    return FemL::track(f, nearest_min_cell_edge(f.nearest), f.nearest.storage, b, p, s);
+}
+int fem_step(const jt_fem_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+             const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s) {
+    return FemL::step(f, nearest_min_cell_edge(f.nearest), f.nearest.storage, arith, sb, integ, k, dtpp, xin, xout,
+                      n, status, s);
+}
+int fem_sample(const jt_fem_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+               int m, int32_t* status, cudaStream_t s) {
+    return FemL::sample(f, nearest_min_cell_edge(f.nearest), f.nearest.storage, arith, e, pos, out, m, status, s);
+}
+}  // namespace jt

@@ -81,11 +81,13 @@ struct Launcher {
     static cudaError_t track_s(const Desc& d, const Extra& x, const jt_boundary& B,
                                const jt_track_params& P, cudaStream_t st) {
         const FT<EXACT, STORE> f = make<EXACT, STORE>(d, x);
-        const unsigned g = grid_blocks(P.n_particles);
+        // block_size was validated to 0, 64, 128 or 256 (<= kBlock, the launch bound)
+        const int bs = P.block_size > 0 ? P.block_size : kBlock;
+        const unsigned g = (unsigned)((P.n_particles + bs - 1) / bs);
         switch (P.integrator) {
-            case JT_EULER: k_track<EXACT, JT_EULER><<<g, kBlock, 0, st>>>(f, B, P); break;
-            case JT_RK2: k_track<EXACT, JT_RK2><<<g, kBlock, 0, st>>>(f, B, P); break;
-            default: k_track<EXACT, JT_RK4><<<g, kBlock, 0, st>>>(f, B, P); break;
+            case JT_EULER: k_track<EXACT, JT_EULER><<<g, bs, 0, st>>>(f, B, P); break;
+            case JT_RK2: k_track<EXACT, JT_RK2><<<g, bs, 0, st>>>(f, B, P); break;
+            default: k_track<EXACT, JT_RK4><<<g, bs, 0, st>>>(f, B, P); break;
         }
         return cudaGetLastError();
     }

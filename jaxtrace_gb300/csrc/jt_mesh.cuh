@@ -26,6 +26,45 @@ __device__ __forceinline__ float det3(const V3& c0, const V3& c1, const V3& c2) 
     return A::sub(A::sub(A::sub(A::add(A::add(t1, t2), t3), t4), t5), t6);
 }
 
+// Barycentric test of tetrahedron t (point_in_tetrahedron_fast,
+// …optimized.py:218-250, and point_in_tetrahedron, fem_interpolator.py:146-207,
+// which compute the same thing): true when the query's box test and the
+// tolerance test pass; b receives (b0..b3) and cn the vertex ids.
+template <bool EXACT>
+__device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, const float* tet_geom, int t,
+                                         float b[4], int4& cn) {
+    typedef Ar<EXACT> A;
+    const float4* bx = reinterpret_cast<const float4*>(tet_box) + 2 * (int64_t)t;
+    const float4 mn = __ldg(bx), mx = __ldg(bx + 1);
+    if (!(q.x >= mn.x && q.y >= mn.y && q.z >= mn.z && q.x <= mx.x && q.y <= mx.y && q.z <= mx.z)) return false;
+    const float4* g = reinterpret_cast<const float4*>(tet_geom) + 4 * (int64_t)t;
+    const float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
+    const V3 v0{g0.x, g0.y, g0.z};
+    const V3 v01{g0.w, g1.x, g1.y}, v02{g1.z, g1.w, g2.x}, v03{g2.y, g2.z, g2.w};
+    const V3 v0p{A::sub(q.x, v0.x), A::sub(q.y, v0.y), A::sub(q.z, v0.z)};
+    float det = det3<EXACT>(v01, v02, v03);
+    if (fabsf(det) < 1e-10f) det = 1.0f;
+    b[1] = A::div(det3<EXACT>(v0p, v02, v03), det);
+    b[2] = A::div(det3<EXACT>(v01, v0p, v03), det);
+    b[3] = A::div(det3<EXACT>(v01, v02, v0p), det);
+    b[0] = A::sub(A::sub(A::sub(1.0f, b[1]), b[2]), b[3]);
+    const float lo = -1e-6f, hi = 0.999999f;  // tol and 1 + tol as float32
+    if (!(b[0] >= lo && b[1] >= lo && b[2] >= lo && b[3] >= lo && b[0] <= hi && b[1] <= hi && b[2] <= hi &&
+          b[3] <= hi))
+        return false;
+    cn = __ldg(reinterpret_cast<const int4*>(g + 3));
+    return true;
+}
+
+// jnp.dot(bary, node_values): terms accumulated in vertex order.
+template <bool EXACT>
+__device__ __forceinline__ V3 p1_combine(const float b[4], const V3& n0, const V3& n1, const V3& n2, const V3& n3) {
+    typedef Ar<EXACT> A;
+    return V3{A::add(A::add(A::add(A::mul(b[0], n0.x), A::mul(b[1], n1.x)), A::mul(b[2], n2.x)), A::mul(b[3], n3.x)),
+              A::add(A::add(A::add(A::mul(b[0], n0.y), A::mul(b[1], n1.y)), A::mul(b[2], n2.y)), A::mul(b[3], n3.y)),
+              A::add(A::add(A::add(A::mul(b[0], n0.z), A::mul(b[1], n1.z)), A::mul(b[2], n2.z)), A::mul(b[3], n3.z))};
+}
+
 template <bool EXACT, int STORE>
 struct MeshField {
     jt_mesh_field F;
@@ -57,33 +96,11 @@ struct MeshField {
         // candidate scan (…optimized.py:309-360): first candidate whose box
         // holds the query and whose barycentrics pass the tolerance test
         for (int s = 0; s < cnt; ++s) {
-            const int t = __ldg(L + s);
-            const float4* bx = reinterpret_cast<const float4*>(F.tet_box) + 2 * (int64_t)t;
-            const float4 mn = __ldg(bx), mx = __ldg(bx + 1);
-            if (!(q.x >= mn.x && q.y >= mn.y && q.z >= mn.z && q.x <= mx.x && q.y <= mx.y && q.z <= mx.z))
-                continue;
-            const float4* g = reinterpret_cast<const float4*>(F.tet_geom) + 4 * (int64_t)t;
-            const float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
-            const int4 cn = __ldg(reinterpret_cast<const int4*>(g + 3));
-            const V3 v0{g0.x, g0.y, g0.z};
-            const V3 v01{g0.w, g1.x, g1.y}, v02{g1.z, g1.w, g2.x}, v03{g2.y, g2.z, g2.w};
-            const V3 v0p{A::sub(q.x, v0.x), A::sub(q.y, v0.y), A::sub(q.z, v0.z)};
-            float det = det3<EXACT>(v01, v02, v03);
-            if (fabsf(det) < 1e-10f) det = 1.0f;
-            const float b1 = A::div(det3<EXACT>(v0p, v02, v03), det);
-            const float b2 = A::div(det3<EXACT>(v01, v0p, v03), det);
-            const float b3 = A::div(det3<EXACT>(v01, v02, v0p), det);
-            const float b0 = A::sub(A::sub(A::sub(1.0f, b1), b2), b3);
-            const float lo = -1e-6f, hi = 0.999999f;  // tol and 1 + tol as float32
-            const bool inside = b0 >= lo && b1 >= lo && b2 >= lo && b3 >= lo && b0 <= hi && b1 <= hi &&
-                                b2 <= hi && b3 <= hi;
-            if (!inside) continue;
-            const V3 n0 = node_value(cn.x, e), n1 = node_value(cn.y, e);
-            const V3 n2 = node_value(cn.z, e), n3 = node_value(cn.w, e);
-            // jnp.dot(bary, node_values), terms accumulated in vertex order
-            return V3{A::add(A::add(A::add(A::mul(b0, n0.x), A::mul(b1, n1.x)), A::mul(b2, n2.x)), A::mul(b3, n3.x)),
-                      A::add(A::add(A::add(A::mul(b0, n0.y), A::mul(b1, n1.y)), A::mul(b2, n2.y)), A::mul(b3, n3.y)),
-                      A::add(A::add(A::add(A::mul(b0, n0.z), A::mul(b1, n1.z)), A::mul(b2, n2.z)), A::mul(b3, n3.z))};
+            float b[4];
+            int4 cn;
+            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(L + s), b, cn)) continue;
+            return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
+                                     node_value(cn.w, e));
         }
         // cheap fallback (…optimized.py:364-376): nearest of the four vertices
         // of the first candidate; an empty list reads slot -1, which indexes

@@ -469,6 +469,126 @@ class TimeSeriesField(_DeviceField):
 
 
 # ---------------------------------------------------------------------------
+class FemHashGrid:
+    """Spatial hash grid of build_tetrahedral_mesh (fem_interpolator.py:36-143),
+    built with array operations instead of the per-element loop but with the
+    same arithmetic: float32 node bounding box; cells per axis
+    ``max(1, ceil(aspect * R))`` with float32 aspect ratios and R the cube
+    root of grid_resolution^3 as a Python float; float64 cell edges for the
+    element-to-cell assignment (float32 box offsets divided by them, floored,
+    clipped) and their float32 copy for lookups; an element is listed in
+    every cell its box overlaps, in ascending element order.
+
+    Stored as CSR (``cell_start``, ``cell_elems``) plus the per-tet box and
+    geometry records the device kernels read; ``cell_to_elements()`` gives
+    the reference's -1-padded table.
+    """
+
+    def __init__(self, points, connectivity, grid_resolution: int = 32):
+        P = np.asarray(points, dtype=F32)
+        T4 = np.asarray(connectivity, dtype=np.int32)
+        if P.ndim != 2 or P.shape[1] != 3:
+            raise ValueError("points must be (N,3)")
+        if T4.ndim != 2 or T4.shape[1] != 4:
+            raise ValueError("connectivity must be (M,4)")
+        if T4.size and (T4.min() < 0 or T4.max() >= len(P)):
+            raise ValueError("connectivity indexes outside the points array")
+        self.points, self.connectivity = P, T4
+        bmin, bmax = P.min(axis=0), P.max(axis=0)
+        size = bmax - bmin
+        aspect = size / size.max()
+        gsf = aspect * (int(grid_resolution) ** 3) ** (1 / 3)
+        gs = np.maximum(1, np.ceil(gsf).astype(int))
+        self.grid_size = tuple(int(v) for v in gs)
+        cell64 = size / np.array(self.grid_size)
+        self.grid_min = bmin.astype(F32)
+        self.cell_size64 = cell64
+        self.grid_cell_size = cell64.astype(F32)
+        V = P[T4]                                           # (M,4,3)
+        emin, emax = V.min(axis=1), V.max(axis=1)
+        self.element_bounds = np.stack([emin, emax], axis=1)
+        hi = np.array(self.grid_size) - 1
+        cmin = np.clip(np.floor((emin - bmin) / cell64).astype(int), 0, hi)
+        cmax = np.clip(np.floor((emax - bmin) / cell64).astype(int), 0, hi)
+        ext = cmax - cmin + 1
+        count = ext.prod(axis=1)
+        elem = np.repeat(np.arange(len(T4), dtype=np.int64), count)
+        first = np.repeat(np.cumsum(count) - count, count)
+        r = np.arange(len(elem), dtype=np.int64) - first
+        ez, ey = np.repeat(ext[:, 2], count), np.repeat(ext[:, 1], count)
+        k = np.repeat(cmin[:, 2], count) + r % ez
+        j = np.repeat(cmin[:, 1], count) + (r // ez) % ey
+        i = np.repeat(cmin[:, 0], count) + r // (ez * ey)
+        cell = (i * self.grid_size[1] + j) * self.grid_size[2] + k
+        order = np.argsort(cell, kind="stable")             # keeps ascending elements per cell
+        n_cells = int(np.prod(self.grid_size))
+        counts = np.bincount(cell, minlength=n_cells)
+        self.cell_elem_counts = counts.astype(np.int32)
+        self.cell_start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        self.cell_elems = elem[order].astype(np.int32)
+        self.max_elems_per_cell = int(counts.max()) if n_cells else 0
+        # device records: box (min xyz,0,max xyz,0) and geometry (v0, v1-v0, v2-v0, v3-v0, ids)
+        M = len(T4)
+        self.tet_box = np.zeros((M, 8), dtype=F32)
+        self.tet_box[:, 0:3], self.tet_box[:, 4:7] = emin, emax
+        self.tet_geom = np.zeros((M, 16), dtype=F32)
+        v0 = V[:, 0]
+        self.tet_geom[:, 0:3] = v0
+        self.tet_geom[:, 3:6] = V[:, 1] - v0
+        self.tet_geom[:, 6:9] = V[:, 2] - v0
+        self.tet_geom[:, 9:12] = V[:, 3] - v0
+        self.tet_geom[:, 12:16] = T4.view(F32)
+
+    def cell_to_elements(self) -> np.ndarray:
+        """The reference's (cells, max_per_cell) table, -1 padded."""
+        n = len(self.cell_elem_counts)
+        out = np.full((n, max(self.max_elems_per_cell, 1)), -1, dtype=np.int32)
+        slot = np.arange(len(self.cell_elems)) - np.repeat(self.cell_start[:-1], self.cell_elem_counts)
+        out[np.repeat(np.arange(n), self.cell_elem_counts), slot] = self.cell_elems
+        return out
+
+
+class FEMTimeSeriesField(TimeSeriesField):
+    """fem_time_series.py:16-110: TimeSeriesField whose spatial sampling is
+    hash-grid point location + P1 over a tetrahedral mesh, the nearest node
+    of the whole mesh where no tetrahedron holds the query; float32 (JAX)
+    time blend."""
+
+    def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
+                 extrapolation: str = "constant", _source_info: Optional[dict] = None,
+                 fem_grid_resolution: int = 32, *, storage: str = "f32"):
+        super().__init__(data, times, positions, interpolation, extrapolation, _source_info, storage=storage,
+                         time_semantics="jax")
+        self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution)
+
+    def _device(self):
+        if self._dev is not None:
+            return
+        torch = _torch_cuda()
+        super()._device()
+        h = self.fem_mesh
+        d = self._dev
+        d["tet_box"] = torch.from_numpy(h.tet_box).cuda()
+        d["tet_geom"] = torch.from_numpy(h.tet_geom).cuda()
+        d["cell_start"] = torch.from_numpy(h.cell_start).cuda()
+        d["cell_elems"] = torch.from_numpy(h.cell_elems if len(h.cell_elems) else np.zeros(1, np.int32)).cuda()
+        f = L.FemField()
+        f.nearest = self._cnear
+        f.n_tets = len(h.connectivity)
+        f.grid_size[:] = list(h.grid_size)
+        f.grid_min[:] = [float(v) for v in h.grid_min]
+        f.cell_size[:] = [float(v) for v in h.grid_cell_size]
+        f.tet_box, f.tet_geom = d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
+        f.cell_start, f.cell_elems = d["cell_start"].data_ptr(), d["cell_elems"].data_ptr()
+        self._cfem = f
+        self._cfield = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(f))
+
+    def __repr__(self) -> str:
+        return (f"FEMTimeSeriesField(data={self.data.shape}, times={self.times.shape}, "
+                f"positions={self.positions.shape}, elements={self.fem_mesh.connectivity.shape[0]}, "
+                f"interpolation='{self.interpolation}', extrapolation='{self.extrapolation}')")
+
+
 class OctreeMesh:
     """Host copy of the octree in the reference's array layout
     (OctreeMeshOptimized, octree_fem_interpolator_optimized.py:18-38)."""

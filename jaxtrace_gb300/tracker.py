@@ -50,6 +50,13 @@ class TrackerOptions:
     time_chunk         steps per kernel launch (None: as many as fit)
     sort_every         re-sort particles by cell every k steps for gather
                        locality (None: 100 from 2^18 particles up, 0: never)
+    sort_bits          cells per axis of that sort, as a power of two
+                       (None: 2^7)
+    block_size         threads per block of the tracking kernel (0: 256)
+    autotune           pick sort_every / sort_bits / block_size by timing a
+                       short sample of the run (``autotune.Autotuner``)
+    cuda_graph         capture the whole tracking pass of ``track_ensembles``
+                       in a CUDA graph and replay it
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -76,6 +83,10 @@ class TrackerOptions:
     device_memory_gb: float = 32.0
     time_chunk: Optional[int] = None
     sort_every: Optional[int] = None
+    sort_bits: Optional[int] = None
+    block_size: int = 0
+    autotune: bool = False
+    cuda_graph: bool = False
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
         """tracker.py:142-153."""
@@ -225,6 +236,7 @@ class ParticleTracker:
         p.comp = comp.data_ptr() if comp is not None else None
         p.status = status.data_ptr()
         p.record_every = 1
+        p.block_size = int(self.options.block_size)
         return p
 
     def _sort_every(self, n: int) -> int:
@@ -233,7 +245,11 @@ class ParticleTracker:
             return 100 if n >= (1 << 18) else 0
         return max(int(se), 0)
 
-    def _engine(self, pos, times, dt, sched_dev=None, status=None, comp=None):
+    def _sort_bits(self) -> int:
+        b = self.options.sort_bits
+        return 7 if b is None else int(b)
+
+    def _engine(self, pos, times, dt, sched_dev=None, status=None, comp=None, ens=None):
         import torch
         if sched_dev is None:
             sched_dev = torch.from_numpy(self._schedule(times, dt).view(np.int32).reshape(-1, 8)).cuda()
@@ -241,7 +257,8 @@ class ParticleTracker:
             status = torch.zeros(1, dtype=torch.int32, device="cuda")
         if comp is None and self._arith() == L.JT_ARITH_COMPENSATED:
             comp = torch.zeros_like(pos)
-        return _Engine(self, pos, len(times) - 1, dt, sched_dev, status, comp, self._sort_every(pos.shape[0]))
+        return _Engine(self, pos, len(times) - 1, dt, sched_dev, status, comp, self._sort_every(pos.shape[0]),
+                       ens=ens)
 
     def _run(self, pos, times, dt, k, compact, n_rows, positions, velocities) -> int:
         """Advance ``pos`` (device, (N,3)) through all steps, filling rows 1.. of the outputs."""
@@ -298,6 +315,30 @@ class ParticleTracker:
         eng.finish()
         return {"track_launches": eng.launches, "kernels": eng.kernels}
 
+    def ensemble_batch(self, ensembles, release_times, n_timesteps: int, dt: Optional[float] = None,
+                       duration: Optional[float] = None) -> "EnsembleBatch":
+        """Device buffers and per-ensemble schedules of a batched run (see
+        ``EnsembleBatch``); ``run()`` advances it, ``capture()`` records it
+        in a CUDA graph."""
+        return EnsembleBatch(self, ensembles, release_times, n_timesteps, dt, duration)
+
+    def track_ensembles(self, ensembles, release_times, n_timesteps: int, dt: Optional[float] = None,
+                        duration: Optional[float] = None, return_device: bool = False):
+        """Final positions of many ensembles of uneven size and release time,
+        advanced together.  Ensemble e gives what
+        ``track_particles(x_e, (t_e, t_e + duration), n_timesteps, dt=dt)``
+        gives in its last row (``duration`` defaults to (n_timesteps-1)*dt).
+        Returns a list of (n_e, 3) float32 arrays, or the concatenated device
+        tensor with ``return_device=True``."""
+        b = self.ensemble_batch(ensembles, release_times, n_timesteps, dt, duration)
+        if self.options.autotune:
+            from .autotune import Autotuner
+            Autotuner.shared().tune_batch(b)
+        if self.options.cuda_graph:
+            b.capture()
+        b.run()
+        return b.pos if return_device else b.finals()
+
     # ------------------------------------------------------------------
     def validate_configuration(self) -> Dict[str, Any]:
         """tracker.py:720-787 on a one-particle probe."""
@@ -347,7 +388,7 @@ class _Engine:
     """Buffers of one run: positions in slot order, optional Kahan terms, the
     slot -> particle map of the locality sort and the sort workspace."""
 
-    def __init__(self, tracker, pos, n_steps, dt, sched_dev, status, comp, sort_every):
+    def __init__(self, tracker, pos, n_steps, dt, sched_dev, status, comp, sort_every, ens=None):
         import torch
         self.t, self.out, self.n_steps = tracker, pos, n_steps
         self.status, self.sched = status, sched_dev
@@ -362,7 +403,7 @@ class _Engine:
         self.stream = L.stream_ptr()
         self.pos, self.comp, self.ids = pos, comp, None
         if sort_every > 0 and self.n > 0:
-            self.grid = tracker._field.sort_grid()
+            self.grid = tracker._field.sort_grid(bits=tracker._sort_bits())
             self.pos = torch.empty_like(pos)
             self.pos_alt = torch.empty_like(pos)
             self.comp_alt = torch.empty_like(comp) if comp is not None else None
@@ -372,6 +413,9 @@ class _Engine:
             self.ws = torch.empty(ws, dtype=torch.uint8, device=pos.device)
             self._sort(first=True)
         self.p = tracker.make_params(self.pos, dt, n_steps, sched_dev, status, self.comp)
+        if ens is not None:       # (device offsets (E+1,) int32, E, schedule entries per ensemble)
+            self.ens = ens
+            self.p.ens_offsets, self.p.n_ens, self.p.schedule_stride = ens[0].data_ptr(), ens[1], ens[2]
 
     def _sort(self, first=False):
         src_pos = self.out if first else self.pos
@@ -427,6 +471,114 @@ class _Engine:
         if self.ids is not None:
             L.check(self.lib.jt_unpermute(self.n, L.ptr(self.pos), L.ptr(self.ids), L.ptr(self.out), self.stream))
             self.kernels += 1
+
+
+class EnsembleBatch:
+    """Ensembles of uneven size and release time in one tracking pass.
+
+    All ensembles take the same number of steps; ensemble e steps on its own
+    float32 time grid ``linspace(t_e, t_e + duration, n_timesteps)`` (the
+    grid ``track_particles`` builds for time_span (t_e, t_e + duration)).
+    The particles of all ensembles sit in one (sum n_e, 3) device array in
+    ensemble order; one tracking launch per time chunk advances them all,
+    each thread reading its ensemble's row of a stacked schedule through the
+    (E+1) offset table.  ``capture()`` records the whole pass (initial copy,
+    locality sorts, tracking launches, unpermute) in a CUDA graph that
+    ``run()`` then replays.
+    """
+
+    def __init__(self, tracker: ParticleTracker, ensembles, release_times, n_timesteps: int,
+                 dt: Optional[float] = None, duration: Optional[float] = None):
+        import torch
+        self.tracker = tracker
+        xs = [ensure_positions_shape(x) for x in ensembles]
+        rel = np.asarray(release_times, dtype=np.float64).reshape(-1)
+        if len(xs) != len(rel):
+            raise ValueError(f"{len(xs)} ensembles but {len(rel)} release times")
+        if len(xs) == 0:
+            raise ValueError("no ensembles")
+        T = int(n_timesteps)
+        if T < 2:
+            raise ValueError("n_timesteps must be >= 2")
+        if duration is None:
+            if dt is None:
+                raise ValueError("give dt or duration")
+            duration = (T - 1) * float(dt)
+        self.times = [np.linspace(float(t), float(t) + float(duration), T, dtype=np.float32) for t in rel]
+        if dt is None:
+            steps = {float(tm[1] - tm[0]) for tm in self.times}
+            if len(steps) != 1:
+                raise ValueError("with dt=None every ensemble's float32 step must agree; pass dt")
+            dt = steps.pop()
+        self.dt = float(dt)
+        self.n_steps = T - 1
+        self.sizes = np.array([len(x) for x in xs], dtype=np.int64)
+        off = np.zeros(len(xs) + 1, dtype=np.int64)
+        np.cumsum(self.sizes, out=off[1:])
+        if off[-1] >= 2 ** 31:
+            raise ValueError("at most 2^31-1 particles per batch")
+        self.offsets = off
+        self.n = int(off[-1])
+        if not torch.cuda.is_available():
+            raise RuntimeError("ensemble tracking runs on a CUDA GPU; none is visible")
+        host = torch.empty((self.n, 3), dtype=torch.float32).pin_memory()
+        hv = host.numpy()
+        for x, a in zip(xs, off[:-1]):
+            hv[a:a + len(x)] = x
+        self.x0 = host.to("cuda", non_blocking=True)
+        self.pos = torch.empty_like(self.x0)
+        sched = np.stack([tracker._schedule(tm, self.dt) for tm in self.times])
+        self.stride = sched.shape[1]
+        self.sched_dev = torch.from_numpy(sched.view(np.int32).reshape(-1, 8)).cuda()
+        self.off_dev = torch.from_numpy(off.astype(np.int32)).cuda()
+        self.status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.comp = torch.zeros_like(self.pos) if tracker._arith() == L.JT_ARITH_COMPENSATED else None
+        self.graph = None
+        self._graph_engine = None
+        self.launches = 0
+        self.kernels = 0
+
+    def _pass(self):
+        """One tracking pass on the current stream: x0 -> pos."""
+        self.pos.copy_(self.x0)
+        if self.comp is not None:
+            self.comp.zero_()
+        eng = self.tracker._engine(self.pos, self.times[0], self.dt, self.sched_dev, self.status, self.comp,
+                                   ens=(self.off_dev, len(self.sizes), self.stride))
+        eng.advance(0, self.n_steps, None)
+        eng.finish()
+        self.launches, self.kernels = eng.launches, eng.kernels
+        return eng
+
+    def capture(self):
+        """Record one pass in a CUDA graph (after one eager pass that loads
+        the library and sets kernel attributes outside the capture)."""
+        import torch
+        self._pass()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._graph_engine = self._pass()
+        self.graph = g
+        return self
+
+    def run(self):
+        """Advance every ensemble from its initial positions to its last step."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._pass()
+        return self
+
+    def check_status(self) -> int:
+        st = int(self.status.item())
+        self.tracker.last_status = st
+        return st
+
+    def finals(self) -> List[np.ndarray]:
+        out = self.pos.cpu().numpy()
+        self.check_status()
+        return [out[a:b] for a, b in zip(self.offsets[:-1], self.offsets[1:])]
 
 
 def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:

@@ -35,7 +35,7 @@ EX = {"constant": 0, "linear": 1, "zero": 2, "nan": 3}
 GRID = {"clamp": 0, "zero": 1, "nan": 2, "periodic": 3}
 INTEG = {"euler": 0, "rk2": 1, "rk4": 2}
 BC = {"none": 0, "periodic": 1, "reflective": 2, "clamping": 3, "clamp": 3, "absorbing": 4}
-FIELD_GRID, FIELD_MESH = 1, 2
+FIELD_GRID, FIELD_MESH, FIELD_FEM = 1, 2, 4
 SEM = {"numpy": 0, "jax": 1}
 
 vp, i32, i64, f32, f64 = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_double
@@ -46,7 +46,9 @@ class OrcField(C.Structure):
                 ("semantics", i32), ("kind", i32), ("nx", i32), ("ny", i32), ("nz", i32), ("bounds_mode", i32),
                 ("gx", vp), ("gy", vp), ("gz", vp), ("points", vp), ("conn", vp), ("n_tets", i32),
                 ("elem_bounds", vp), ("nodes_min", vp), ("nodes_max", vp), ("nodes_elements", vp),
-                ("max_elems", i32), ("nodes_children", vp), ("nodes_is_leaf", vp), ("max_depth", i32)]
+                ("max_elems", i32), ("nodes_children", vp), ("nodes_is_leaf", vp), ("max_depth", i32),
+                ("fem_grid_size", i32 * 3), ("fem_grid_min", f32 * 3), ("fem_cell_size", f32 * 3),
+                ("fem_cell_elements", vp), ("fem_max_per_cell", i32)]
 
 
 class OrcBoundary(C.Structure):
@@ -194,6 +196,39 @@ class BoundarySpec:
                 b.lattice[q] = lat.ctypes.data
                 b.inlet_res[q] = len(lat)
         self.c = b
+
+
+class FemSpec:
+    """Hash-grid FEM time-series field (fem_time_series.py:16-110) in the
+    reference layout: grid_size, grid_min, float32 grid_cell_size, the
+    (cells, max_per_cell) -1-padded cell_to_elements table and element_bounds
+    as build_tetrahedral_mesh returns them."""
+
+    def __init__(self, data, times, points, conn, grid_size, grid_min, grid_cell_size, cell_to_elements,
+                 element_bounds, extrapolation="constant"):
+        arrs = dict(
+            data=np.ascontiguousarray(np.asarray(data, np.float32).reshape(len(times), -1, 3)),
+            times=np.ascontiguousarray(np.asarray(times, np.float32)),
+            points=np.ascontiguousarray(np.asarray(points, np.float32)),
+            conn=np.ascontiguousarray(np.asarray(conn, np.int32)),
+            eb=np.ascontiguousarray(np.asarray(element_bounds, np.float32)),
+            cells=np.ascontiguousarray(np.asarray(cell_to_elements, np.int32)))
+        self.keep = arrs
+        f = OrcField()
+        f.n_snap = len(times)
+        f.snap_times, f.data = _p(arrs["times"]), _p(arrs["data"])
+        f.n_nodes = arrs["points"].shape[0]
+        f.extrapolation = EX[extrapolation]
+        f.semantics = SEM["jax"]
+        f.kind = FIELD_FEM
+        f.points, f.conn, f.n_tets = _p(arrs["points"]), _p(arrs["conn"]), arrs["conn"].shape[0]
+        f.elem_bounds = _p(arrs["eb"])
+        f.fem_grid_size[:] = [int(v) for v in grid_size]
+        f.fem_grid_min[:] = [float(v) for v in np.asarray(grid_min, np.float32)]
+        f.fem_cell_size[:] = [float(v) for v in np.asarray(grid_cell_size, np.float32)]
+        f.fem_cell_elements = _p(arrs["cells"])
+        f.fem_max_per_cell = arrs["cells"].shape[1]
+        self.c = f
 
 
 def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F32, n_threads=0,

@@ -32,7 +32,7 @@ enum { GRID_CLAMP = 0, GRID_ZERO = 1, GRID_NAN = 2, GRID_PERIODIC = 3 };
 enum { EX_CONSTANT = 0, EX_LINEAR = 1, EX_ZERO = 2, EX_NAN = 3 };
 enum { IN_EULER = 0, IN_RK2 = 1, IN_RK4 = 2 };
 enum { BC_NONE = 0, BC_PERIODIC = 1, BC_REFLECTIVE = 2, BC_CLAMP = 3, BC_ABSORBING = 4 };
-enum { FIELD_GRID = 1, FIELD_MESH = 2 };
+enum { FIELD_GRID = 1, FIELD_MESH = 2, FIELD_FEM = 4 };
 enum { SEM_NUMPY = 0, SEM_JAX = 1 };
 
 typedef struct {
@@ -59,6 +59,12 @@ typedef struct {
     const int32_t* nodes_children; /* (K,8) */
     const uint8_t* nodes_is_leaf;  /* (K) */
     int max_depth;
+    /* hash grid (fem_interpolator.py:18-143) in the reference layout */
+    int fem_grid_size[3];
+    float fem_grid_min[3];
+    float fem_cell_size[3];            /* float32 copy used by the lookup */
+    const int32_t* fem_cell_elements;  /* (cells, fem_max_per_cell) -1 padded */
+    int fem_max_per_cell;
 } orc_field;
 
 typedef struct {
@@ -463,6 +469,104 @@ static void mesh_eval_d(const orc_field* F, const blend_t* b, const double* q, d
 }
 
 /* ------------------------------------------------------------------------ */
+/* Hash-grid lookup + P1, fem_interpolator.py:146-328.                      */
+static int nearest_node(const orc_field* F, const float* q);
+
+/* floor(v).astype(int32) then clip(0, n-1), with XLA's saturating float ->
+ * int conversion (NaN -> 0). */
+static int fem_cell_coord(float v, int n) {
+    float f = floorf(v);
+    if (f != f) return 0;
+    if (f < 0.0f) return 0;
+    if (f > (float)(n - 1)) return n - 1;
+    return (int)f;
+}
+
+static int fem_cell(const orc_field* F, const float* q) {
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        const float u = q[a] - F->fem_grid_min[a];
+        c[a] = fem_cell_coord(u / F->fem_cell_size[a], F->fem_grid_size[a]);
+    }
+    return (c[0] * F->fem_grid_size[1] + c[1]) * F->fem_grid_size[2] + c[2];
+}
+
+static void fem_eval_f(const orc_field* F, const blend_t* b, const float* q, float* out, int64_t* fb) {
+    const int32_t* cand = F->fem_cell_elements + (size_t)fem_cell(F, q) * F->fem_max_per_cell;
+    /* lax.scan over the padded row keeps the first element found */
+    for (int s = 0; s < F->fem_max_per_cell; ++s) {
+        const int e = cand[s];
+        if (e < 0) continue;
+        const float* eb = F->elem_bounds + 6 * (size_t)e;
+        if (!(q[0] >= eb[0] && q[1] >= eb[1] && q[2] >= eb[2] && q[0] <= eb[3] && q[1] <= eb[4] && q[2] <= eb[5]))
+            continue;
+        const int32_t* cv = F->conn + 4 * (size_t)e;
+        const float* v0 = F->points + 3 * (size_t)cv[0];
+        float v0p[3], v01[3], v02[3], v03[3];
+        for (int a = 0; a < 3; ++a) {
+            v0p[a] = q[a] - v0[a];
+            v01[a] = F->points[3 * (size_t)cv[1] + a] - v0[a];
+            v02[a] = F->points[3 * (size_t)cv[2] + a] - v0[a];
+            v03[a] = F->points[3 * (size_t)cv[3] + a] - v0[a];
+        }
+        float det = det3_f(v01, v02, v03);
+        if (fabsf(det) < 1e-10f) det = 1.0f;
+        const float b1 = det3_f(v0p, v02, v03) / det;
+        const float b2 = det3_f(v01, v0p, v03) / det;
+        const float b3 = det3_f(v01, v02, v0p) / det;
+        float b0 = 1.0f - b1; b0 = b0 - b2; b0 = b0 - b3;
+        const float lo = -1e-6f, hi = 0.999999f;
+        if (!(b0 >= lo && b1 >= lo && b2 >= lo && b3 >= lo && b0 <= hi && b1 <= hi && b2 <= hi && b3 <= hi)) continue;
+        float n[4][3];
+        for (int k = 0; k < 4; ++k) node_f(F, b, cv[k], n[k]);
+        for (int c = 0; c < 3; ++c) {
+            float r = b0 * n[0][c];
+            r = r + b1 * n[1][c];
+            r = r + b2 * n[2][c];
+            r = r + b3 * n[3][c];
+            out[c] = r;
+        }
+        return;
+    }
+    /* not found: the nearest node of the whole mesh (fem_interpolator.py:311-316) */
+    if (fb) (*fb)++;
+    node_f(F, b, nearest_node(F, q), out);
+}
+
+static void fem_eval_d(const orc_field* F, const blend_t* b, const double* q, double* out, int64_t* fb) {
+    const float qf[3] = {(float)q[0], (float)q[1], (float)q[2]};
+    const int32_t* cand = F->fem_cell_elements + (size_t)fem_cell(F, qf) * F->fem_max_per_cell;
+    for (int s = 0; s < F->fem_max_per_cell; ++s) {
+        const int e = cand[s];
+        if (e < 0) continue;
+        const float* eb = F->elem_bounds + 6 * (size_t)e;
+        if (!(q[0] >= eb[0] && q[1] >= eb[1] && q[2] >= eb[2] && q[0] <= eb[3] && q[1] <= eb[4] && q[2] <= eb[5]))
+            continue;
+        const int32_t* cv = F->conn + 4 * (size_t)e;
+        double v0p[3], v01[3], v02[3], v03[3];
+        for (int a = 0; a < 3; ++a) {
+            const double v0 = F->points[3 * (size_t)cv[0] + a];
+            v0p[a] = q[a] - v0;
+            v01[a] = F->points[3 * (size_t)cv[1] + a] - v0;
+            v02[a] = F->points[3 * (size_t)cv[2] + a] - v0;
+            v03[a] = F->points[3 * (size_t)cv[3] + a] - v0;
+        }
+        double det = det3_d(v01, v02, v03);
+        if (fabs(det) < 1e-10) det = 1.0;
+        const double b1 = det3_d(v0p, v02, v03) / det, b2 = det3_d(v01, v0p, v03) / det;
+        const double b3 = det3_d(v01, v02, v0p) / det, b0 = 1.0 - b1 - b2 - b3;
+        const double lo = -1e-6, hi = 1.0 - 1e-6;
+        if (!(b0 >= lo && b1 >= lo && b2 >= lo && b3 >= lo && b0 <= hi && b1 <= hi && b2 <= hi && b3 <= hi)) continue;
+        double n[4][3];
+        for (int k = 0; k < 4; ++k) node_d(F, b, cv[k], n[k]);
+        for (int c = 0; c < 3; ++c) out[c] = b0 * n[0][c] + b1 * n[1][c] + b2 * n[2][c] + b3 * n[3][c];
+        return;
+    }
+    if (fb) (*fb)++;
+    node_d(F, b, nearest_node(F, qf), out);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Boundaries, boundary.py:101-210, :377-438, :1517-1599.                  */
 static float bc_axis_f(int kind, float x, float lo, float hi, float outside) {
     float width = hi - lo; width = width > 0.0f ? width : 0.0f;
@@ -606,6 +710,7 @@ static void field_f(const orc_field* F, stime s, const float* p, float* v, int64
     const blend_t b = blend_at(F, s);
     if (F->kind == FIELD_GRID) grid_eval_f(F, &b, p, v, wr);
     else if (F->kind == FIELD_MESH) mesh_eval_f(F, &b, p, v, fb);
+    else if (F->kind == FIELD_FEM) fem_eval_f(F, &b, p, v, fb);
     else node_f(F, &b, nearest_node(F, p), v);
 }
 static void field_d(const orc_field* F, stime s, const double* p, double* v, int64_t* fb) {
@@ -614,6 +719,7 @@ static void field_d(const orc_field* F, stime s, const double* p, double* v, int
     else b = blend_numpy(F, s.t);
     if (F->kind == FIELD_GRID) grid_eval_d(F, &b, p, v);
     else if (F->kind == FIELD_MESH) mesh_eval_d(F, &b, p, v, fb);
+    else if (F->kind == FIELD_FEM) fem_eval_d(F, &b, p, v, fb);
     else {
         const float pf[3] = {(float)p[0], (float)p[1], (float)p[2]};
         node_d(F, &b, nearest_node(F, pf), v);

@@ -269,11 +269,62 @@ def phase_octree(ref: str):
     print("phase octree: done")
 
 
+def phase_fem(ref: str):
+    """Hash-grid FEM interpolation (fields/fem_interpolator.py,
+    fields/fem_time_series.py) under the NumPy stand-in for jax."""
+    sys.path.insert(0, str(REPO / "oracle" / "jaxshim"))
+    sys.path.insert(1, ref)
+    import contextlib
+    import io
+    import warnings
+    warnings.simplefilter("ignore")
+    from jaxtrace.fields import fem_interpolator as fi
+    from jaxtrace.fields.fem_time_series import FEMTimeSeriesField
+    from jaxtrace.tracking import boundary as bnd
+    from jaxtrace.tracking.tracker import create_tracker
+
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    # C0: the module's own example (fem_interpolator.py:385-413): two tets, a
+    # query outside both, answered by the nearest node
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1], [1, 0, 1], [1, 1, 0], [0, 1, 1]], F32)
+    conn = np.array([[0, 1, 2, 3], [4, 5, 6, 7]], np.int32)
+    with quiet:
+        m = fi.build_tetrahedral_mesh(pts, conn, grid_resolution=4)
+        ka = np.asarray(fi.create_fem_interpolator(m)(np.array([[0.5, 0.5, 0.5], [0.1, 0.1, 0.1]], F32), pts))
+    out = {"ka_pts": pts, "ka_conn": conn, "ka_out": ka}
+    # C1-C3: jittered Kuhn mesh, squashed to half height in z so the hash
+    # grid's aspect-ratio adjustment gives unequal cells per axis
+    P, T4 = kuhn_mesh(6, 0.2, 1)
+    P = (P * np.array([1.0, 1.0, 0.5], F32)).astype(F32)
+    st = np.linspace(0, 1, 5).astype(F32)
+    D = np.stack([abc(P, float(t)) for t in st]).astype(F32)
+    with quiet:
+        f = FEMTimeSeriesField(D, st, P, T4, fem_grid_resolution=8)
+    M = f.fem_mesh
+    out.update(grid_size=np.array(M.grid_size, np.int64), grid_min=np.asarray(M.grid_min),
+               grid_cell_size=np.asarray(M.grid_cell_size), cell_to_elements=np.asarray(M.cell_to_elements),
+               cell_elem_counts=np.asarray(M.cell_elem_counts), element_bounds=np.asarray(M.element_bounds))
+    rng = np.random.default_rng(8)
+    q = np.concatenate([rng.random((300, 3)) * np.array([1, 1, 0.5]), rng.uniform(-0.1, 1.1, (60, 3))]).astype(F32)
+    out.update(P=P, T4=T4, st=st, D=D, q=q)
+    out["sample_t03"] = np.asarray(f.sample_at_positions(q, np.float32(0.3)), dtype=F32)
+    out["sample_t10"] = np.asarray(f.sample_at_positions(q, np.float32(1.0)), dtype=F32)
+    x0 = (rng.random((40, 3)) * np.array([1, 1, 0.5])).astype(F32)
+    bc = bnd.mixed_boundary(((0, 0, 0), (1, 1, 0.5)), {"x": "periodic", "y": "reflective", "z": "periodic"})
+    tr = create_tracker("rk4", f, bc, use_jax_jit=False, progress_style="none")
+    traj = tr.track_particles(x0, (0.0, 0.08), 9, dt=0.01)
+    out.update(x0=x0, traj=traj.positions)
+    np.savez_compressed(HERE / "fem.npz", **out)
+    print("phase fem: done")
+
+
+PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem}
+
 if __name__ == "__main__":
-    if len(sys.argv) >= 3 and sys.argv[1] in ("numpy", "octree"):
-        {"numpy": phase_numpy, "octree": phase_octree}[sys.argv[1]](sys.argv[2])
+    if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
+        PHASES[sys.argv[1]](sys.argv[2])
         sys.exit(0)
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
-    for phase in ("numpy", "octree"):
+    for phase in PHASES:
         subprocess.run([sys.executable, __file__, phase, ref], check=True, env=env)

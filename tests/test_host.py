@@ -18,7 +18,7 @@ F32 = np.float32
 def header_functions():
     text = (ROOT / "include" / "jaxtrace_gb300.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(jt_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|const char\*)\s+(jt_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_library_exports_every_header_symbol():

@@ -1,0 +1,95 @@
+"""Host logic of ensemble batching and of the autotuner (no GPU)."""
+import json
+
+import numpy as np
+import pytest
+
+import jaxtrace_gb300 as jt
+from jaxtrace_gb300 import autotune as A
+from jaxtrace_gb300 import workloads as W
+
+F32 = np.float32
+
+
+def _tracker():
+    g = (np.arange(8) / 8).astype(F32)
+    st = np.linspace(0, 1, 3).astype(F32)
+    f = jt.StructuredTimeSeriesField(W.abc_snapshots(W.grid_nodes(g, g, g), st), st, g, g, g, "periodic")
+    return jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT))
+
+
+def test_ensemble_batch_validates_before_touching_the_device():
+    tr = _tracker()
+    x = np.zeros((4, 3), F32)
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([x, x], [0.0], 11, dt=0.01)          # one release time short
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([], [], 11, dt=0.01)
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([x], [0.0], 1, dt=0.01)              # no step
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([x], [0.0], 11)                      # neither dt nor duration
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([np.zeros((4, 4), F32)], [0.0], 11, dt=0.01)
+    # dt=None needs one float32 step shared by all ensembles' grids
+    with pytest.raises(ValueError):
+        tr.ensemble_batch([x, x], [0.0, 0.3], 11, duration=0.1)
+
+
+def test_ensemble_schedules_follow_each_release_time():
+    from jaxtrace_gb300 import _lib as L
+    from jaxtrace_gb300.schedule import build_schedule, single_blend
+    st = np.linspace(0, 1, 32).astype(F32)
+    rel = np.random.default_rng(7).uniform(0, 0.5, 4)
+    rows = []
+    for t0 in rel:
+        times = np.linspace(t0, t0 + 400 * 0.005, 401, dtype=F32)
+        s = build_schedule(times, 0.005, L.JT_RK4, st, semantics="jax")
+        assert s.shape[0] == 4 * 400
+        # stage 1 of step 0 blends the snapshots bracketing the ensemble's own t0
+        b = single_blend(st, F32(times[0]), semantics="jax")[0]
+        assert s[0]["pair"] == b["pair"] and s[0]["wa"] == b["wa"] and s[0]["wb"] == b["wb"]
+        rows.append(s)
+    assert not np.array_equal(rows[0], rows[1])
+
+
+class _Opts:
+    block_size, sort_every, sort_bits = 0, None, None
+
+
+class _FakeTracker:
+    options = _Opts()
+
+
+def test_autotuner_coordinate_descent_picks_fastest():
+    cost = {128: 3.0, 256: 2.0, 64: 4.0}
+    every = {0: 5.0, 20: 1.5, 50: 1.0, 100: 1.2}
+    bits = {7: 1.0, 6: 0.5, 5: 0.8}
+    tr = _FakeTracker()
+
+    def sample():
+        o = tr.options
+        return cost[o.block_size] * every[o.sort_every] * (bits[o.sort_bits] if o.sort_every else 1.0)
+
+    res = A.Autotuner(cache_path="").search(tr, sample)
+    assert (res.block_size, res.sort_every, res.sort_bits) == (256, 50, 6)
+    assert res.ms == pytest.approx(2.0 * 1.0 * 0.5)
+    assert len(res.trials) == len(A.BLOCK_SIZES) + len(A.SORT_EVERY) + len(A.SORT_BITS)
+    # the tracker's own options are restored after the search
+    assert (tr.options.block_size, tr.options.sort_every, tr.options.sort_bits) == (0, None, None)
+
+
+def test_autotuner_skips_cell_size_without_sorting(tmp_path):
+    tr = _FakeTracker()
+    res = A.Autotuner(cache_path="").search(tr, lambda: 1.0 + 0.1 * (tr.options.sort_every or 0))
+    assert res.sort_every == 0
+    assert len(res.trials) == len(A.BLOCK_SIZES) + len(A.SORT_EVERY)
+
+
+def test_autotuner_cache_file_roundtrip(tmp_path):
+    p = tmp_path / "t.json"
+    t = A.Autotuner(cache_path=str(p))
+    t.cache["k"] = {"block_size": 128, "sort_every": 50, "sort_bits": 6, "ms": 1.0}
+    t._save()
+    assert json.loads(p.read_text())["k"]["sort_bits"] == 6
+    assert A.Autotuner(cache_path=str(p)).cache["k"]["block_size"] == 128

@@ -136,3 +136,34 @@ def test_octree_tracking(golden):
     times = np.linspace(0.0, 0.1, 11, dtype=F32)
     out, traj, _ = oracle.track(spec, bc, g["x0"], times, 0.01, "rk4", record=True)
     assert np.allclose(traj, g["traj"], rtol=1e-5, atol=1e-6)
+
+
+# ---------------------------------------------------------------- FEM hash grid
+def fem_spec(g):
+    return oracle.FemSpec(g["D"], g["st"], g["P"], g["T4"], g["grid_size"], g["grid_min"], g["grid_cell_size"],
+                          g["cell_to_elements"], g["element_bounds"])
+
+
+def test_fem_known_answer(golden):
+    g = golden("fem")
+    # (0.5,0.5,0.5) lies in neither tet: the nearest node, first of 8 ties (node 0)
+    assert np.allclose(g["ka_out"], [[0.0, 0.0, 0.0], [0.1, 0.1, 0.1]])
+
+
+def test_fem_sampling(golden):
+    g = golden("fem")
+    spec = fem_spec(g)
+    for key, t in (("sample_t03", 0.3), ("sample_t10", 1.0)):
+        out, fb = oracle.sample(spec, g["q"], float(F32(t)), t_is_f32=True)
+        ref = g[key]
+        assert np.allclose(out, ref, rtol=1e-5, atol=1e-6), np.abs(out - ref).max()
+        assert fb > 0  # queries outside the mesh take the global nearest node
+
+
+def test_fem_tracking(golden):
+    g = golden("fem")
+    spec = fem_spec(g)
+    bc = oracle.BoundarySpec(kinds=("periodic", "reflective", "periodic"), bounds=((0, 0, 0), (1, 1, 0.5)))
+    times = np.linspace(0.0, 0.08, 9, dtype=F32)
+    out, traj, _ = oracle.track(spec, bc, g["x0"], times, 0.01, "rk4", record=True)
+    assert np.allclose(traj, g["traj"], rtol=1e-5, atol=1e-6), np.abs(traj - g["traj"]).max()
