@@ -390,8 +390,10 @@ def fem_leg(a, profile=False):
     o64, _, _ = oracle.track(spec, obc, c["x0"][sub], times, c["dt"], precision=oracle.ORC_F64)
     same = np.all(final[sub].view(np.uint32) == o32.view(np.uint32), axis=1)
     rel = np.linalg.norm(final[sub] - o64, axis=1) / np.maximum(np.linalg.norm(o64, axis=1), 1e-30)
+    hash_grid = {} if profile else fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc)
     return {"workload": "unstructured FEM: 64^3 hexes x 6 jittered tets (1,572,864), 32 FP32 snapshots, octree + "
                         f"P1, 1,000,000 particles, x/z periodic y reflective, RK4 dt=0.005, {n_steps} steps",
+            "hash_grid_variant": hash_grid,
             "value": n * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "status": int(status.item()),
             "roofline": {"bound": "hbm", "achieved": units * bpp / (launch_ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": units * bpp / (launch_ms / 1e3) / 1e9 / peak,
@@ -404,6 +406,38 @@ def fem_leg(a, profile=False):
             "cpu_baseline": {"value": len(sub) * n_steps / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1,
                              "kind": "port", "sample": f"{len(sub)} particles (every 1000th) x {n_steps} steps, "
                                                        "float32 C restatement of the octree/P1 path, OpenMP"}}
+
+
+def fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc):
+    """The same run through the hash-grid FEM field (FEMTimeSeriesField,
+    32^3 cells, global nearest-node fallback)."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    import oracle
+    f = jt.FEMTimeSeriesField(c["data"], c["times"], c["points"], c["tets"])
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
+    pos = torch.empty_like(x0)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sched = torch.from_numpy(tr._schedule(times, c["dt"]).view(np.int32).reshape(-1, 8)).cuda()
+
+    def one():
+        pos.copy_(x0)
+        tr.track_device(pos, times, c["dt"], status, None, sched)
+
+    one()
+    ms = _timed(one, 2)
+    n = x0.shape[0]
+    final = pos.cpu().numpy()
+    h = f.fem_mesh
+    spec = oracle.FemSpec(c["data"], c["times"], c["points"], c["tets"], h.grid_size, h.grid_min, h.grid_cell_size,
+                          h.cell_to_elements(), h.element_bounds)
+    o32, _, info = oracle.track(spec, obc, c["x0"][sub], times, c["dt"])
+    same = np.all(final[sub].view(np.uint32) == o32.view(np.uint32), axis=1)
+    return {"value": n * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "status": int(status.item()),
+            "hash_grid": list(h.grid_size), "max_elements_per_cell": h.max_elems_per_cell,
+            "parity_f32_oracle": {"bit_exact_fraction": float(np.mean(same)), "particles": len(sub),
+                                  "oracle_fallbacks": info["fallback_count"]}}
 
 
 def batch_leg(a, profile=False):

@@ -322,13 +322,24 @@ typedef struct {
     float* lambda;                 /* device (N,3): dL/dx at step_end on entry, at step_begin on exit */
     float* grad;                   /* device, the field's pair-record layout in float32
                                       (n_pairs, nodes, 8): += dL/dA in slots 0,1,4 and dL/dB
-                                      in slots 2,3,5 (A = snapshot p, B = snapshot p+1) */
+                                      in slots 2,3,5 (A = snapshot p, B = snapshot p+1);
+                                      NULL: dL/dx only                          */
+    void* work;                    /* device workspace (16-byte aligned) of at least
+                                      jt_adjoint_workspace_bytes(nodes, steps) bytes when
+                                      grad is set; zeroed by the call           */
+    int64_t work_bytes;
 } jt_adjoint_params;
+
+/* Workspace of one backward segment of n_steps steps over n_nodes grid
+ * nodes: three float4 snapshot-gradient accumulators per step and node. */
+size_t jt_adjoint_workspace_bytes(int64_t n_nodes, int32_t n_steps);
 
 /* One backward segment over a float32 regular-grid field with per-axis box
  * boundaries: recomputes the segment from its checkpoint with the forward
- * (exact) arithmetic, then propagates lambda back step by step and
- * accumulates the snapshot gradient (vector atomics). */
+ * (exact) arithmetic, keeping every step's stage positions, then propagates
+ * lambda back step by step.  The snapshot gradient of each stage time is
+ * accumulated per node (vector atomics into the workspace) and folded into
+ * grad with the stage's blend coefficients by a second kernel. */
 int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, const jt_adjoint_params* p, void* stream);
 
 /* ---- locality sort ------------------------------------------------------ */

@@ -101,7 +101,8 @@ class SortGrid(C.Structure):
 
 class AdjointParams(C.Structure):
     _fields_ = [("n_particles", i32), ("step_begin", i32), ("step_end", i32), ("dt", f32), ("dt_half", f32),
-                ("dt_sixth", f32), ("pad", i32), ("schedule", vp), ("ckpt", vp), ("lambda_", vp), ("grad", vp)]
+                ("dt_sixth", f32), ("pad", i32), ("schedule", vp), ("ckpt", vp), ("lambda_", vp), ("grad", vp),
+                ("work", vp), ("work_bytes", i64)]
 
 
 JT_ORDER_MORTON, JT_ORDER_LINEAR = 0, 1
@@ -174,6 +175,7 @@ def load(build_if_missing: bool = True):
         "jt_kde_grid": (i32, [P(KdeParams), vp]),
         "jt_kde_points": (i32, [P(KdeParams), vp, i32, vp, vp]),
         "jt_adjoint_rk4": (i32, [P(Field), P(Boundary), P(AdjointParams), vp]),
+        "jt_adjoint_workspace_bytes": (C.c_size_t, [i64, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

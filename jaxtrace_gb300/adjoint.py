@@ -43,7 +43,7 @@ class AdjointRK4:
 
     def __init__(self, times, grid_x, grid_y, grid_z, bounds_handling: str = "periodic",
                  boundary: Optional[BoundaryDescriptor] = None, checkpoint_every: int = 50,
-                 time_semantics: str = "numpy"):
+                 time_semantics: str = "numpy", sort_bits: int = 6, sort_min_particles: int = 1 << 16):
         from .fields import StructuredTimeSeriesField
         self.times = np.asarray(times, dtype=F32)
         self.gx, self.gy, self.gz = (np.asarray(g, dtype=F32) for g in (grid_x, grid_y, grid_z))
@@ -59,6 +59,12 @@ class AdjointRK4:
         if not 1 <= k <= 64:
             raise ValueError("checkpoint_every must be in 1..64")
         self.k = k
+        # particles are re-sorted by cell (2^sort_bits per axis over the grid)
+        # at every checkpoint for gather and scatter locality; 0 disables it
+        if not 0 <= int(sort_bits) <= 7:
+            raise ValueError("sort_bits must be in 0..7")
+        self.sort_bits = int(sort_bits)
+        self.sort_min_particles = int(sort_min_particles)
 
     def _field(self, pairs):
         t = self._tmpl
@@ -119,51 +125,89 @@ def _make_function():
             pairs = solver.pairs_from(U.detach())
             gfield, field = solver._field(pairs)
             bc = solver.bc.jt_boundary()
-            pos = x0.detach().float().contiguous().clone()
-            n = pos.shape[0]
+            n = x0.shape[0]
             k = solver.k
             n_seg = (n_steps + k - 1) // k
-            ckpt = torch.empty((max(n_seg, 1), n, 3), dtype=torch.float32, device=pos.device)
-            status = torch.zeros(1, dtype=torch.int32, device=pos.device)
+            dev = x0.device
+            ckpt = torch.empty((max(n_seg, 1), n, 3), dtype=torch.float32, device=dev)
+            status = torch.zeros(1, dtype=torch.int32, device=dev)
+            stream = L.stream_ptr()
+            sort = solver.sort_bits > 0 and n >= solver.sort_min_particles
+            pos = x0.detach().float().contiguous().clone()
+            ids_all = None
+            if sort:
+                grid = solver._tmpl.sort_grid(bits=solver.sort_bits)
+                ids_all = torch.empty((max(n_seg, 1), n), dtype=torch.int32, device=dev)
+                ws = torch.empty(int(lib.jt_cell_sort_workspace_bytes(n, grid.bits)), dtype=torch.uint8, device=dev)
             p = L.TrackParams()
             p.integrator, p.arith, p.n_particles = L.JT_RK4, L.JT_ARITH_EXACT, n
             dtf, dth, dt6 = step_constants(dt)
             p.dt, p.dt_half, p.dt_sixth = float(dtf), float(dth), float(dt6)
             p.schedule, p.pos, p.status, p.record_every = sched_dev.data_ptr(), pos.data_ptr(), status.data_ptr(), 1
-            stream = L.stream_ptr()
             for sgi in range(n_seg):
-                ckpt[sgi].copy_(pos)
+                if sort:
+                    # particles in cell order at every checkpoint: ids_all[s][j] is the
+                    # particle in slot j during segment s
+                    src_ids = ids_all[sgi - 1] if sgi > 0 else None
+                    L.check(lib.jt_cell_sort(C.byref(grid), n, L.ptr(pos), None, L.ptr(src_ids), L.ptr(ckpt[sgi]),
+                                             None, L.ptr(ids_all[sgi]), L.ptr(ws), ws.numel(), stream))
+                    pos.copy_(ckpt[sgi])
+                else:
+                    ckpt[sgi].copy_(pos)
                 p.step_begin, p.step_end = sgi * k, min((sgi + 1) * k, n_steps)
                 L.check(lib.jt_track(C.byref(field), C.byref(bc), C.byref(p), stream))
+            out = pos
+            if sort and n_seg > 0:
+                out = torch.empty_like(pos)
+                L.check(lib.jt_unpermute(n, L.ptr(pos), L.ptr(ids_all[n_seg - 1]), L.ptr(out), stream))
             ctx.solver, ctx.sched, ctx.n_steps, ctx.dt = solver, sched_dev, n_steps, dt
             ctx.T = U.shape[0]
-            ctx.save_for_backward(ckpt, pairs)
+            ctx.save_for_backward(ckpt, pairs, ids_all)
             ctx.keep = (gfield, field, bc)
-            return pos
+            ctx.status = status
+            return out
 
         @staticmethod
         def backward(ctx, g_xT):
-            ckpt, pairs = ctx.saved_tensors
+            ckpt, pairs, ids_all = ctx.saved_tensors
             solver, k = ctx.solver, ctx.solver.k
             lib = L.load()
             gfield, field, bc = ctx.keep
-            lam = g_xT.detach().float().contiguous().clone()
-            grad = torch.zeros_like(pairs)
+            lam = g_xT.detach().float().contiguous().clone()          # particle order
+            want_u = ctx.needs_input_grad[1]
+            grad = torch.zeros_like(pairs) if want_u else None
             n = lam.shape[0]
+            n_seg = ckpt.shape[0]
             a = L.AdjointParams()
             a.n_particles = n
             dtf, dth, dt6 = step_constants(ctx.dt)
             a.dt, a.dt_half, a.dt_sixth = float(dtf), float(dth), float(dt6)
-            a.schedule, a.lambda_, a.grad = ctx.sched.data_ptr(), lam.data_ptr(), grad.data_ptr()
+            a.schedule = ctx.sched.data_ptr()
+            a.grad = grad.data_ptr() if grad is not None else None
+            work = None
+            if want_u:
+                wb = int(lib.jt_adjoint_workspace_bytes(solver.nodes, k))
+                work = torch.empty(wb // 4, dtype=torch.float32, device=lam.device)
+                a.work, a.work_bytes = work.data_ptr(), wb
             stream = L.stream_ptr()
-            n_seg = ckpt.shape[0]
             for sgi in reversed(range(n_seg)):
                 a.step_begin, a.step_end = sgi * k, min((sgi + 1) * k, ctx.n_steps)
                 a.ckpt = ckpt[sgi].data_ptr()
-                L.check(lib.jt_adjoint_rk4(C.byref(field), C.byref(bc), C.byref(a), stream))
-            dU = solver.pairs_grad_to_U(grad, ctx.T)
-            shape = (ctx.T,) + tuple(len(g) for g in (solver.gx, solver.gy, solver.gz)) + (3,)
-            return lam, dU.reshape(shape), None, None, None, None
+                if ids_all is not None:
+                    idx = ids_all[sgi].long()
+                    lam_s = lam.index_select(0, idx).contiguous()    # slot order of the segment
+                    a.lambda_ = lam_s.data_ptr()
+                    L.check(lib.jt_adjoint_rk4(C.byref(field), C.byref(bc), C.byref(a), stream))
+                    lam.index_copy_(0, idx, lam_s)
+                else:
+                    a.lambda_ = lam.data_ptr()
+                    L.check(lib.jt_adjoint_rk4(C.byref(field), C.byref(bc), C.byref(a), stream))
+            dU = None
+            if want_u:
+                dU = solver.pairs_grad_to_U(grad, ctx.T)
+                shape = (ctx.T,) + tuple(len(g) for g in (solver.gx, solver.gy, solver.gz)) + (3,)
+                dU = dU.reshape(shape)
+            return lam, dU, None, None, None, None
 
     return AdjointFunction
 

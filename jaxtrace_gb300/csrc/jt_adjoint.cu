@@ -3,14 +3,15 @@
 // Gradients of a loss of the final positions with respect to the initial
 // positions and to the snapshot values.  The forward pass stores positions
 // every K steps (the tracking kernel's recording); this kernel walks one
-// segment backwards: it recomputes the segment's states from its checkpoint
-// with the forward arithmetic into a per-thread array, then for every step
-// recomputes the four stage positions and runs the RK4 reverse sweep
+// segment backwards: it recomputes the segment from its checkpoint with the
+// forward arithmetic, keeping every step's stage positions in a per-thread
+// array, then runs the RK4 reverse sweep
 //     x' = B(x + h/6 (k1 + 2k2 + 2k3 + k4)),   k_i = v(x_i, t_i)
 // with vector-Jacobian products of the trilinear, time-blended field
-//     v(x) = sum_c w_c(x) (wa A_c + wb B_c).
-// J^T g uses dw_c/dx; dL/dA_c += wa w_c g and dL/dB_c += wb w_c g go to a
-// gradient buffer with the snapshot-pair record layout through vector atomics.
+//     v(x) = sum_c w_c(x) (ca A_c + cb B_c).
+// J^T g uses dw_c/dx.  The snapshot gradient dL/dA_c += ca w_c g,
+// dL/dB_c += cb w_c g is gathered as w_c g per stage time and node (one
+// vector atomic per corner) and folded with (ca, cb) afterwards.
 #include <stdint.h>
 
 #include "jt_grid.cuh"
@@ -34,9 +35,6 @@ __device__ __forceinline__ void red_v4(float* p, float a, float b, float c, floa
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
                  : "memory");
 }
-__device__ __forceinline__ void red_v2(float* p, float a, float b) {
-    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
-}
 
 // Axis data of the adjoint: cell, weight, and d(weight)/dx (0 where the
 // clamp mode clipped the coordinate).
@@ -59,9 +57,12 @@ __device__ __forceinline__ AxisD axis_d(float x, float org, float d, float inv_d
     return r;
 }
 
-// J^T g at p for entry e, scattering the snapshot gradient.
+// J^T g at p for entry e.  With acc set, the snapshot gradient of this
+// stage, w_c * g per corner node c, is added to acc (one float4 record per
+// node: x, y, z, unused); the blend coefficients of A and B are applied when
+// the accumulators are folded into the pair-record gradient.
 __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, const jt_blend& e, const V3& g,
-                                       float* __restrict__ grad) {
+                                       float4* __restrict__ acc) {
     const AxisD ax = axis_d(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode);
     const AxisD ay = axis_d(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode);
     const AxisD az = axis_d(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode);
@@ -75,8 +76,8 @@ __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, cons
         const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
         const int i = bx ? ax.i1 : ax.i0, j = by ? ay.i1 : ay.i0, k = bz ? az.i1 : az.i0;
         const float wx = bx ? ax.w : 1.0f - ax.w, wy = by ? ay.w : 1.0f - ay.w, wz = bz ? az.w : 1.0f - az.w;
-        const int64_t rec = base + ((int64_t)(i * F.ny + j) * F.nz + k);
-        const PairVal pv = load_pair<JT_STORE_F32>(F.pairs, rec);
+        const int64_t node = (int64_t)(i * F.ny + j) * F.nz + k;
+        const PairVal pv = load_pair<JT_STORE_F32>(F.pairs, base + node);
         // blended corner value dotted with g
         const float vx = ca * pv.axy.x + cb * pv.bxy.x, vy = ca * pv.axy.y + cb * pv.bxy.y;
         const float vz = ca * pv.az + cb * pv.bz;
@@ -85,11 +86,10 @@ __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, cons
         jtg.x += sx * ax.dfdx * wy * wz * vg;
         jtg.y += sy * ay.dfdx * wx * wz * vg;
         jtg.z += sz * az.dfdx * wx * wy * vg;
-        const float w = wx * wy * wz;
-        const float wa = w * ca, wb = w * cb;
-        float* r = grad + 8 * rec;  // {Ax, Ay, Bx, By, Az, Bz, -, -}
-        red_v4(r, wa * g.x, wa * g.y, wb * g.x, wb * g.y);
-        red_v2(r + 4, wa * g.z, wb * g.z);
+        if (acc != nullptr) {
+            const float w = wx * wy * wz;
+            red_v4(reinterpret_cast<float*>(acc + node), w * g.x, w * g.y, w * g.z, 0.0f);
+        }
     }
     return jtg;
 }
@@ -111,63 +111,84 @@ __device__ __forceinline__ float bc_deriv(int kind, float x, float lo, float hi)
     }
 }
 
-// One backward segment [s0, s1): lambda holds dL/dx_{s1} on entry, dL/dx_{s0} on exit.
-__global__ void __launch_bounds__(kBlock) k_adjoint_rk4(jt_grid_field F, jt_boundary B, jt_adjoint_params P) {
+// Per recomputed step: the RK4 stage positions x0, x2 = x0 + h/2 k1,
+// x3 = x0 + h/2 k2, x4 = x0 + h k3 and the pre-boundary end point, with the
+// forward pass's exact arithmetic (integrate<true, JT_RK4>).
+struct StepRec {
+    float v[15];
+};
+
+#ifndef JT_ADJOINT_MIN_BLOCKS
+#define JT_ADJOINT_MIN_BLOCKS 3
+#endif
+
+// One backward segment [s0, s1): lambda holds dL/dx_{s1} on entry, dL/dx_{s0}
+// on exit; acc (or NULL) receives the per-stage snapshot gradients, three
+// records per step (stage times t, t + h/2, t + h), (3*nseg, nodes) float4.
+__global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
+    k_adjoint_rk4(jt_grid_field F, jt_boundary B, jt_adjoint_params P, float4* __restrict__ acc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n_particles) return;
     typedef GridField<true, JT_STORE_F32> Fw;
     const Fw f{F};
     typedef Ar<true> A;
     const int nseg = P.step_end - P.step_begin;
-    float xs[JT_ADJOINT_MAX_SEGMENT][3];
+    const int64_t nodes = F.pair_stride;
+    StepRec rec[JT_ADJOINT_MAX_SEGMENT];
     V3 x{P.ckpt[3 * (int64_t)i], P.ckpt[3 * (int64_t)i + 1], P.ckpt[3 * (int64_t)i + 2]};
     const StepConst k{P.dt, P.dt_half, P.dt_sixth};
     int flags = 0;
-    V3 cz{0.f, 0.f, 0.f};
-    for (int s = 0; s < nseg; ++s) {  // recompute the segment's states
-        xs[s][0] = x.x; xs[s][1] = x.y; xs[s][2] = x.z;
-        integrate<true, JT_RK4, false>(f, P.schedule + 4 * (int64_t)(P.step_begin + s), k, x, cz, flags);
+    for (int s = 0; s < nseg; ++s) {  // recompute the segment, keeping the stage positions
+        const jt_blend* e = P.schedule + 4 * (int64_t)(P.step_begin + s);
+        float* r = rec[s].v;
+        V3 sm{0.f, 0.f, 0.f}, xs = x;
+#pragma unroll 1
+        for (int st = 0; st < 4; ++st) {
+            r[3 * st] = xs.x; r[3 * st + 1] = xs.y; r[3 * st + 2] = xs.z;
+            const jt_blend es = e[st == 0 ? 0 : (st == 3 ? 2 : 1)];
+            const V3 kk = f(xs, es, flags);
+            if (st == 0) {
+                sm = kk;
+            } else if (st == 3) {
+                sm = V3{A::add(sm.x, kk.x), A::add(sm.y, kk.y), A::add(sm.z, kk.z)};
+            } else {
+                sm = V3{A::add(sm.x, A::mul(2.0f, kk.x)), A::add(sm.y, A::mul(2.0f, kk.y)),
+                        A::add(sm.z, A::mul(2.0f, kk.z))};
+            }
+            const float h = st < 2 ? k.dth : k.dt;
+            xs = V3{A::axpy(x.x, h, kk.x), A::axpy(x.y, h, kk.y), A::axpy(x.z, h, kk.z)};
+        }
+        x = V3{A::add(x.x, A::mul(k.dt6, sm.x)), A::add(x.y, A::mul(k.dt6, sm.y)),
+               A::add(x.z, A::mul(k.dt6, sm.z))};
+        r[12] = x.x; r[13] = x.y; r[14] = x.z;
         apply_boundary<true>(B, x.x, x.y, x.z);
     }
     V3 lam{P.lambda[3 * (int64_t)i], P.lambda[3 * (int64_t)i + 1], P.lambda[3 * (int64_t)i + 2]};
     for (int s = nseg - 1; s >= 0; --s) {
         const jt_blend* e = P.schedule + 4 * (int64_t)(P.step_begin + s);
         const jt_blend e0 = e[0], e1 = e[1], e2 = e[2];
-        const V3 x0{xs[s][0], xs[s][1], xs[s][2]};
-        // forward stages (same arithmetic as the forward pass)
-        const V3 k1 = f(x0, e0, flags);
-        const V3 x2{A::axpy(x0.x, k.dth, k1.x), A::axpy(x0.y, k.dth, k1.y), A::axpy(x0.z, k.dth, k1.z)};
-        const V3 k2 = f(x2, e1, flags);
-        const V3 x3{A::axpy(x0.x, k.dth, k2.x), A::axpy(x0.y, k.dth, k2.y), A::axpy(x0.z, k.dth, k2.z)};
-        const V3 k3 = f(x3, e1, flags);
-        const V3 x4{A::axpy(x0.x, k.dt, k3.x), A::axpy(x0.y, k.dt, k3.y), A::axpy(x0.z, k.dt, k3.z)};
-        // through the boundary: pre-boundary position of this step
-        if (B.inlet_mode == JT_INLET_OFF && !B.absorbing_joint) {
-            const V3 k4 = f(x4, e2, flags);
-            const float pre[3] = {x0.x + k.dt6 * (k1.x + 2.0f * k2.x + 2.0f * k3.x + k4.x),
-                                  x0.y + k.dt6 * (k1.y + 2.0f * k2.y + 2.0f * k3.y + k4.y),
-                                  x0.z + k.dt6 * (k1.z + 2.0f * k2.z + 2.0f * k3.z + k4.z)};
-            lam.x *= bc_deriv(B.axis_kind[0], pre[0], B.lo[0], B.hi[0]);
-            lam.y *= bc_deriv(B.axis_kind[1], pre[1], B.lo[1], B.hi[1]);
-            lam.z *= bc_deriv(B.axis_kind[2], pre[2], B.lo[2], B.hi[2]);
-        }
+        const float* r = rec[s].v;
+        const V3 x0{r[0], r[1], r[2]}, x2{r[3], r[4], r[5]}, x3{r[6], r[7], r[8]}, x4{r[9], r[10], r[11]};
+        // through the boundary at the pre-boundary end point
+        lam.x *= bc_deriv(B.axis_kind[0], r[12], B.lo[0], B.hi[0]);
+        lam.y *= bc_deriv(B.axis_kind[1], r[13], B.lo[1], B.hi[1]);
+        lam.z *= bc_deriv(B.axis_kind[2], r[14], B.lo[2], B.hi[2]);
+        float4* a0 = acc != nullptr ? acc + (int64_t)(3 * s) * nodes : nullptr;
+        float4* a1 = acc != nullptr ? a0 + nodes : nullptr;
+        float4* a2 = acc != nullptr ? a1 + nodes : nullptr;
         // reverse sweep
         const float c6 = k.dt6, c3 = 2.0f * k.dt6;
-        V3 g4{c6 * lam.x, c6 * lam.y, c6 * lam.z};
-        V3 g3{c3 * lam.x, c3 * lam.y, c3 * lam.z};
-        V3 g2{c3 * lam.x, c3 * lam.y, c3 * lam.z};
-        V3 g1{c6 * lam.x, c6 * lam.y, c6 * lam.z};
         V3 lx = lam;
-        const V3 d4 = grid_vjp(F, x4, e2, g4, P.grad);          // k4 = v(x4)
+        const V3 d4 = grid_vjp(F, x4, e2, V3{c6 * lam.x, c6 * lam.y, c6 * lam.z}, a2);   // k4 = v(x4)
         lx = V3{lx.x + d4.x, lx.y + d4.y, lx.z + d4.z};
-        g3 = V3{g3.x + k.dt * d4.x, g3.y + k.dt * d4.y, g3.z + k.dt * d4.z};
-        const V3 d3 = grid_vjp(F, x3, e1, g3, P.grad);          // k3 = v(x3)
+        const V3 g3{c3 * lam.x + k.dt * d4.x, c3 * lam.y + k.dt * d4.y, c3 * lam.z + k.dt * d4.z};
+        const V3 d3 = grid_vjp(F, x3, e1, g3, a1);                                          // k3 = v(x3)
         lx = V3{lx.x + d3.x, lx.y + d3.y, lx.z + d3.z};
-        g2 = V3{g2.x + k.dth * d3.x, g2.y + k.dth * d3.y, g2.z + k.dth * d3.z};
-        const V3 d2 = grid_vjp(F, x2, e1, g2, P.grad);          // k2 = v(x2)
+        const V3 g2{c3 * lam.x + k.dth * d3.x, c3 * lam.y + k.dth * d3.y, c3 * lam.z + k.dth * d3.z};
+        const V3 d2 = grid_vjp(F, x2, e1, g2, a1);                                          // k2 = v(x2)
         lx = V3{lx.x + d2.x, lx.y + d2.y, lx.z + d2.z};
-        g1 = V3{g1.x + k.dth * d2.x, g1.y + k.dth * d2.y, g1.z + k.dth * d2.z};
-        const V3 d1 = grid_vjp(F, x0, e0, g1, P.grad);          // k1 = v(x0)
+        const V3 g1{c6 * lam.x + k.dth * d2.x, c6 * lam.y + k.dth * d2.y, c6 * lam.z + k.dth * d2.z};
+        const V3 d1 = grid_vjp(F, x0, e0, g1, a0);                                          // k1 = v(x0)
         lam = V3{lx.x + d1.x, lx.y + d1.y, lx.z + d1.z};
     }
     P.lambda[3 * (int64_t)i] = lam.x;
@@ -175,9 +196,49 @@ __global__ void __launch_bounds__(kBlock) k_adjoint_rk4(jt_grid_field F, jt_boun
     P.lambda[3 * (int64_t)i + 2] = lam.z;
 }
 
+// Fold the per-stage accumulators of a segment into the pair-record gradient:
+// dL/dA += ca * G, dL/dB += cb * G with (ca, cb) the stage's blend
+// coefficients.  One thread per node walks the stages in order, so no two
+// threads touch one record.
+__global__ void __launch_bounds__(kBlock) k_adjoint_fold(jt_grid_field F, const jt_blend* __restrict__ sched,
+                                                          int nseg, const float4* __restrict__ acc,
+                                                          float* __restrict__ grad) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nodes = F.pair_stride;
+    if (node >= nodes) return;
+    int cur = -1;
+    float sa[3] = {0.f, 0.f, 0.f}, sb[3] = {0.f, 0.f, 0.f};
+    for (int j = 0; j < 3 * nseg; ++j) {
+        const jt_blend e = sched[4 * (j / 3) + (j % 3)];
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        if (pr != cur) {
+            if (cur >= 0) {
+                float* r = grad + 8 * ((int64_t)cur * F.pair_stride + node);
+                r[0] += sa[0]; r[1] += sa[1]; r[2] += sb[0]; r[3] += sb[1]; r[4] += sa[2]; r[5] += sb[2];
+            }
+            cur = pr;
+            sa[0] = sa[1] = sa[2] = sb[0] = sb[1] = sb[2] = 0.f;
+        }
+        float ca, cb;
+        blend_coefs(e, ca, cb);
+        const float4 g = acc[(int64_t)j * nodes + node];
+        sa[0] += ca * g.x; sa[1] += ca * g.y; sa[2] += ca * g.z;
+        sb[0] += cb * g.x; sb[1] += cb * g.y; sb[2] += cb * g.z;
+    }
+    if (cur >= 0) {
+        float* r = grad + 8 * ((int64_t)cur * F.pair_stride + node);
+        r[0] += sa[0]; r[1] += sa[1]; r[2] += sb[0]; r[3] += sb[1]; r[4] += sa[2]; r[5] += sb[2];
+    }
+}
+
 }  // namespace jt
 
 using namespace jt;
+
+extern "C" size_t jt_adjoint_workspace_bytes(int64_t n_nodes, int32_t n_steps) {
+    if (n_nodes < 0 || n_steps < 0 || n_steps > JT_ADJOINT_MAX_SEGMENT) return 0;
+    return (size_t)3 * (size_t)n_steps * (size_t)n_nodes * sizeof(float4);
+}
 
 extern "C" int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, const jt_adjoint_params* p, void* stream) {
     if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
@@ -194,8 +255,23 @@ extern "C" int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, cons
         return set_error(JT_ERR_INVALID, "segment [%d,%d) must hold 0..%d steps", p->step_begin, p->step_end,
                          JT_ADJOINT_MAX_SEGMENT);
     if (p->n_particles == 0 || nseg == 0) return JT_OK;
-    if (p->schedule == nullptr || p->ckpt == nullptr || p->lambda == nullptr || p->grad == nullptr)
-        return set_error(JT_ERR_INVALID, "schedule, ckpt, lambda and grad are required");
-    k_adjoint_rk4<<<grid_blocks(p->n_particles), kBlock, 0, (cudaStream_t)stream>>>(F, *bc, *p);
-    return cuda_status(cudaGetLastError(), "adjoint kernel launch");
+    if (p->schedule == nullptr || p->ckpt == nullptr || p->lambda == nullptr)
+        return set_error(JT_ERR_INVALID, "schedule, ckpt and lambda are required");
+    const size_t need = jt_adjoint_workspace_bytes(F.pair_stride, nseg);
+    if (p->grad != nullptr && (p->work == nullptr || p->work_bytes < (int64_t)need))
+        return set_error(JT_ERR_INVALID, "the snapshot gradient needs a workspace of %zu bytes", need);
+    if (p->grad != nullptr && ((uintptr_t)p->work & 15u) != 0)
+        return set_error(JT_ERR_INVALID, "the adjoint workspace must be 16-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    float4* acc = p->grad != nullptr ? reinterpret_cast<float4*>(p->work) : nullptr;
+    if (acc != nullptr) {
+        const cudaError_t e = cudaMemsetAsync(acc, 0, need, s);
+        if (e != cudaSuccess) return cuda_status(e, "adjoint workspace memset");
+    }
+    k_adjoint_rk4<<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
+    int rc = cuda_status(cudaGetLastError(), "adjoint kernel launch");
+    if (rc != JT_OK || acc == nullptr) return rc;
+    k_adjoint_fold<<<grid_blocks(F.pair_stride), kBlock, 0, s>>>(F, p->schedule + 4 * (int64_t)p->step_begin, nseg,
+                                                                  acc, p->grad);
+    return cuda_status(cudaGetLastError(), "adjoint fold launch");
 }

@@ -295,44 +295,50 @@ __device__ __forceinline__ float nearest_lattice(const float* g, int n, float c)
 
 // Continuous inlet with grid-preserving replacement (boundary.py:1517-1599).
 template <bool EXACT>
-__device__ __forceinline__ void bc_inlet(const jt_boundary& B, float* r) {
+__device__ __forceinline__ void bc_inlet(const jt_boundary& B, float& x, float& y, float& z) {
     typedef Ar<EXACT> A;
+    // The flow axis a and the two others o0 < o1, picked with selects so that
+    // nothing is indexed by a run-time axis (no local-memory copy of B).
     const int a = B.inlet_axis;
-    const int o0 = (a == 0) ? 1 : 0;
-    const int o1 = (a == 2) ? 1 : 2;
-    const float amin = B.lo[a], amax = B.hi[a];
-    bool exited = B.inlet_positive ? (r[a] > amax) : (r[a] < amin);
+    float fa = a == 0 ? x : (a == 1 ? y : z);
+    float u0 = a == 0 ? y : x;  // axis o0 = (a == 0 ? 1 : 0)
+    float u1 = a == 2 ? y : z;  // axis o1 = (a == 2 ? 1 : 2)
+    const float amin = a == 0 ? B.lo[0] : (a == 1 ? B.lo[1] : B.lo[2]);
+    const float amax = a == 0 ? B.hi[0] : (a == 1 ? B.hi[1] : B.hi[2]);
+    const float lo0 = a == 0 ? B.lo[1] : B.lo[0], hi0 = a == 0 ? B.hi[1] : B.hi[0];
+    const float lo1 = a == 2 ? B.lo[1] : B.lo[2], hi1 = a == 2 ? B.hi[1] : B.hi[2];
+    const bool exited = B.inlet_positive ? (fa > amax) : (fa < amin);
     if (exited && B.inlet_mode == JT_INLET_GRID) {
-        float g0 = nearest_lattice(B.inlet_coords[0], B.inlet_res[0], r[o0]);
-        float g1 = nearest_lattice(B.inlet_coords[1], B.inlet_res[1], r[o1]);
-        r[a] = B.inlet_positive ? amin : amax;
-        r[o0] = g0;
-        r[o1] = g1;
+        const float g0 = nearest_lattice(B.inlet_coords[0], B.inlet_res[0], u0);
+        const float g1 = nearest_lattice(B.inlet_coords[1], B.inlet_res[1], u1);
+        fa = B.inlet_positive ? amin : amax;
+        u0 = g0;
+        u1 = g1;
     }
     // boundary.py:1580-1587  backward crossings are nudged inside
     if (B.inlet_positive) {
-        if (r[a] < amin) r[a] = B.inlet_nudge;
+        if (fa < amin) fa = B.inlet_nudge;
     } else {
-        if (r[a] > amax) r[a] = B.inlet_nudge;
+        if (fa > amax) fa = B.inlet_nudge;
     }
     // boundary.py:1590-1597  one mirror on the other axes
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int o = q == 0 ? o0 : o1;
-        const float lo = B.lo[o], hi = B.hi[o];
-        float v = r[o];
-        if (v < lo) v = A::sub(A::mul(2.0f, lo), v);
-        else if (v > hi) v = A::sub(A::mul(2.0f, hi), v);
-        r[o] = v;
+    if (u0 < lo0) u0 = A::sub(A::mul(2.0f, lo0), u0);
+    else if (u0 > hi0) u0 = A::sub(A::mul(2.0f, hi0), u0);
+    if (u1 < lo1) u1 = A::sub(A::mul(2.0f, lo1), u1);
+    else if (u1 > hi1) u1 = A::sub(A::mul(2.0f, hi1), u1);
+    if (a == 0) {
+        x = fa; y = u0; z = u1;
+    } else if (a == 1) {
+        x = u0; y = fa; z = u1;
+    } else {
+        x = u0; y = u1; z = fa;
     }
 }
 
 template <bool EXACT>
 __device__ __forceinline__ void apply_boundary(const jt_boundary& B, float& x, float& y, float& z) {
     if (B.inlet_mode != JT_INLET_OFF) {
-        float r[3] = {x, y, z};
-        bc_inlet<EXACT>(B, r);
-        x = r[0]; y = r[1]; z = r[2];
+        bc_inlet<EXACT>(B, x, y, z);
         return;
     }
     if (B.absorbing_joint) {

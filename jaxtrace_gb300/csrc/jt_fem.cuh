@@ -42,7 +42,7 @@ struct FemField {
         const int b0 = __ldg(F.cell_start + cell), b1 = __ldg(F.cell_start + cell + 1);
         // lax.scan over the cell's candidates keeps the first hit (:280-305)
         for (int s = b0; s < b1; ++s) {
-            float b[4];
+            float4 b;
             int4 cn;
             if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(F.cell_elems + s), b, cn)) continue;
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),

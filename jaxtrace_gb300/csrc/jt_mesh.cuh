@@ -29,10 +29,11 @@ __device__ __forceinline__ float det3(const V3& c0, const V3& c1, const V3& c2) 
 // Barycentric test of tetrahedron t (point_in_tetrahedron_fast,
 // …optimized.py:218-250, and point_in_tetrahedron, fem_interpolator.py:146-207,
 // which compute the same thing): true when the query's box test and the
-// tolerance test pass; b receives (b0..b3) and cn the vertex ids.
+// tolerance test pass; b receives (b0, b1, b2, b3) as (x, y, z, w) and cn
+// the vertex ids.
 template <bool EXACT>
 __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, const float* tet_geom, int t,
-                                         float b[4], int4& cn) {
+                                         float4& b, int4& cn) {
     typedef Ar<EXACT> A;
     const float4* bx = reinterpret_cast<const float4*>(tet_box) + 2 * (int64_t)t;
     const float4 mn = __ldg(bx), mx = __ldg(bx + 1);
@@ -44,13 +45,12 @@ __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, cons
     const V3 v0p{A::sub(q.x, v0.x), A::sub(q.y, v0.y), A::sub(q.z, v0.z)};
     float det = det3<EXACT>(v01, v02, v03);
     if (fabsf(det) < 1e-10f) det = 1.0f;
-    b[1] = A::div(det3<EXACT>(v0p, v02, v03), det);
-    b[2] = A::div(det3<EXACT>(v01, v0p, v03), det);
-    b[3] = A::div(det3<EXACT>(v01, v02, v0p), det);
-    b[0] = A::sub(A::sub(A::sub(1.0f, b[1]), b[2]), b[3]);
+    b.y = A::div(det3<EXACT>(v0p, v02, v03), det);
+    b.z = A::div(det3<EXACT>(v01, v0p, v03), det);
+    b.w = A::div(det3<EXACT>(v01, v02, v0p), det);
+    b.x = A::sub(A::sub(A::sub(1.0f, b.y), b.z), b.w);
     const float lo = -1e-6f, hi = 0.999999f;  // tol and 1 + tol as float32
-    if (!(b[0] >= lo && b[1] >= lo && b[2] >= lo && b[3] >= lo && b[0] <= hi && b[1] <= hi && b[2] <= hi &&
-          b[3] <= hi))
+    if (!(b.x >= lo && b.y >= lo && b.z >= lo && b.w >= lo && b.x <= hi && b.y <= hi && b.z <= hi && b.w <= hi))
         return false;
     cn = __ldg(reinterpret_cast<const int4*>(g + 3));
     return true;
@@ -58,11 +58,11 @@ __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, cons
 
 // jnp.dot(bary, node_values): terms accumulated in vertex order.
 template <bool EXACT>
-__device__ __forceinline__ V3 p1_combine(const float b[4], const V3& n0, const V3& n1, const V3& n2, const V3& n3) {
+__device__ __forceinline__ V3 p1_combine(const float4& b, const V3& n0, const V3& n1, const V3& n2, const V3& n3) {
     typedef Ar<EXACT> A;
-    return V3{A::add(A::add(A::add(A::mul(b[0], n0.x), A::mul(b[1], n1.x)), A::mul(b[2], n2.x)), A::mul(b[3], n3.x)),
-              A::add(A::add(A::add(A::mul(b[0], n0.y), A::mul(b[1], n1.y)), A::mul(b[2], n2.y)), A::mul(b[3], n3.y)),
-              A::add(A::add(A::add(A::mul(b[0], n0.z), A::mul(b[1], n1.z)), A::mul(b[2], n2.z)), A::mul(b[3], n3.z))};
+    return V3{A::add(A::add(A::add(A::mul(b.x, n0.x), A::mul(b.y, n1.x)), A::mul(b.z, n2.x)), A::mul(b.w, n3.x)),
+              A::add(A::add(A::add(A::mul(b.x, n0.y), A::mul(b.y, n1.y)), A::mul(b.z, n2.y)), A::mul(b.w, n3.y)),
+              A::add(A::add(A::add(A::mul(b.x, n0.z), A::mul(b.y, n1.z)), A::mul(b.z, n2.z)), A::mul(b.w, n3.z))};
 }
 
 template <bool EXACT, int STORE>
@@ -96,7 +96,7 @@ struct MeshField {
         // candidate scan (…optimized.py:309-360): first candidate whose box
         // holds the query and whose barycentrics pass the tolerance test
         for (int s = 0; s < cnt; ++s) {
-            float b[4];
+            float4 b;
             int4 cn;
             if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(L + s), b, cn)) continue;
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
