@@ -65,6 +65,8 @@ def args_parse():
     p.add_argument("--n-steps", type=int, default=1000)
     p.add_argument("--dt", type=float, default=0.002)
     p.add_argument("--sort-every", type=int, default=None, help="locality re-sort interval (default: automatic)")
+    p.add_argument("--sort-bits", type=int, default=None, help="cells per axis of the re-sort as 2^bits (default 7)")
+    p.add_argument("--block-size", type=int, default=0, help="tracking kernel threads per block (0: 256)")
     p.add_argument("--grid", type=int, default=128)
     p.add_argument("--no-error", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -73,6 +75,8 @@ def args_parse():
     p.add_argument("--no-fem", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--fem-steps", type=int, default=1000)
+    p.add_argument("--adj-lattice", default="256,256,64", help="seed lattice of the adjoint leg")
+    p.add_argument("--adj-steps", type=int, default=500)
     p.add_argument("--leg", default=None, choices=["fem", "batch", "adjoint"],
                    help="run one configuration leg alone and print its JSON (with --profile: the leg's timed "
                         "region bracketed by cudaProfilerStart/Stop)")
@@ -207,7 +211,7 @@ def run_reference(a, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def adjoint_leg(a):
+def adjoint_leg(a, profile=False):
     """Differentiation configuration: plain ABC field at 64^3 (16 snapshots,
     periodic), 256x256x64 lattice seeds, RK4 dt=0.01, 500 steps, checkpoint
     every 50; loss = sum |x_T - y|^2 with y ~ U[0,1)^3 (default_rng(3)).
@@ -221,14 +225,26 @@ def adjoint_leg(a):
     from jaxtrace_gb300.adjoint import AdjointRK4
     c = W.plain_rk4(n_particles=1, n=64, n_snap=16)
     g = c["grid"][0]
-    x0 = jt.uniform_grid_seeds((256, 256, 64), W.UNIT)
+    lattice = tuple(int(v) for v in a.adj_lattice.split(","))
+    x0 = jt.uniform_grid_seeds(lattice, W.UNIT)
     n = len(x0)
     y = np.random.default_rng(3).uniform(size=(n, 3)).astype(np.float32)
     solver = AdjointRK4(c["times"], g, g, g, "periodic", jt.periodic_boundary(W.UNIT), checkpoint_every=50)
     x0_t = torch.tensor(x0, device="cuda", requires_grad=True)
     U_t = torch.tensor(c["data"].reshape(16, 64, 64, 64, 3), device="cuda", requires_grad=True)
     y_t = torch.tensor(y, device="cuda")
-    n_steps, dt = 500, 0.01
+    n_steps, dt = a.adj_steps, 0.01
+    if profile:
+        # one untimed pass, then one pass inside cudaProfilerStart/Stop
+        for k in range(2):
+            if k == 1:
+                torch.cuda.synchronize()
+                torch.cuda.profiler.start()
+            xT = solver(x0_t, U_t, (0.0, n_steps * dt), n_steps + 1, dt=dt)
+            ((xT - y_t) ** 2).sum().backward()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        return {}
     fwd_ms, bwd_ms = [], []
     for it in range(a.warmup + a.steps):
         x0_t.grad = None
@@ -251,7 +267,7 @@ def adjoint_leg(a):
     obc = oracle.BoundarySpec(kinds=("periodic",) * 3)
     rng = np.random.default_rng(17)
     fd_stats = {}
-    for horizon in (50, 500):
+    for horizon in sorted({min(50, n_steps), n_steps}):
         if horizon != n_steps:
             # a shorter horizon needs its own adjoint
             xs = torch.tensor(x0[:4096], device="cuda", requires_grad=True)
@@ -305,8 +321,8 @@ def adjoint_leg(a):
             "samples": int(len(rel)), "subset_particles": m, "h": 1e-3}
     f, b = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
     return {"fd_check_dL_dU": fd_U,
-            "workload": "differentiation: 64^3 periodic ABC, 16 snapshots, 4,194,304 lattice seeds, RK4 dt=0.01, "
-                        "500 steps, checkpoint every 50, loss sum|x_T - y|^2",
+            "workload": f"differentiation: 64^3 periodic ABC, 16 snapshots, {n:,} lattice seeds, RK4 dt=0.01, "
+                        f"{n_steps} steps, checkpoint every 50, loss sum|x_T - y|^2",
             "forward_ms": f, "backward_ms": b, "backward_over_forward": b / f,
             "forward_particle_steps_per_s": n * n_steps / (f / 1e3),
             "adjoint_particle_steps_per_s": n * n_steps / (b / 1e3),
@@ -528,7 +544,7 @@ def main():
         from jaxtrace_gb300 import _lib as L
         L.load()
         if a.leg == "adjoint":
-            out = {} if a.profile else adjoint_leg(a)
+            out = adjoint_leg(a, profile=a.profile)
         else:
             out = {"fem": fem_leg, "batch": batch_leg}[a.leg](a, profile=a.profile)
         if rank == 0:
@@ -555,7 +571,8 @@ def main():
     clk = Clocks(local)
     for v in variants:
         field = jt.StructuredTimeSeriesField(case["data"], case["times"], g, g, g, "clamp", storage=v)
-        tr = jt.create_tracker("rk4", field, bc, record_final_only=True, sort_every=a.sort_every)
+        tr = jt.create_tracker("rk4", field, bc, record_final_only=True, sort_every=a.sort_every,
+                               sort_bits=a.sort_bits, block_size=a.block_size)
         trackers[v] = tr
         sched = torch.from_numpy(tr._schedule(times, case["dt"]).view(np.int32).reshape(-1, 8)).cuda()
         status = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -624,7 +641,7 @@ def main():
             "config": {"workload": workload_name(a), "storage": head, "particles": n,
                        "steps_per_pass": a.n_steps,
                        "l2": f"inputs larger than L2 (positions {n * 12 / 1e6:.0f} MB, snapshot pairs "
-                             f"{(len(case['times']) - 1) * g.size ** 3 * (32 if head == 'f32' else 16) / 1e9:.2f} GB)"},
+                             f"{(len(case['times']) - 1) * g.size ** 3 * (32 if head == 'f32' else 48) / 1e9:.2f} GB)"},
             "variants": {v: {k: r[k] for k in ("value", "ms_per_step", "track_kernel_ms_per_step", "status")} |
                          {"roofline_frac": r["roofline"]["frac"]} for v, r in results.items()},
             "roofline": results[head]["roofline"], "gpu_launches": launches}

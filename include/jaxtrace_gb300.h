@@ -116,13 +116,15 @@ typedef struct {
  * reference's ij layout.  Values are stored as snapshot PAIRS: record n of
  * pair p holds snapshot p and p+1 of node n side by side:
  *   F32 : 8 floats  {Ax,Ay,Bx,By, Az,Bz,0,0}        (32 B, one sector)
- *   BF16/F16 (grid field): 16 halves, the z-PAIR of node (i,j,k) and its
- *         z-successor (i,j,k1) -- k1 = (k+1) mod nz for periodic bounds,
- *         min(k+1, nz-1) otherwise: {node k: Ax,Ay,Bx,By,Az,Bz, node k1:
- *         Ax,Ay,Bx,By,Az,Bz, 0,0,0,0}                (32 B)
+ *   BF16/F16 (grid field): 24 halves, the yz-QUAD of node (i,j,k): nodes
+ *         (i,j,k), (i,j,k1), (i,j1,k), (i,j1,k1) with k1 = (k+1) mod nz for
+ *         periodic bounds and min(k+1, nz-1) otherwise (j1 alike), six
+ *         halves {Ax,Ay,Bx,By,Az,Bz} each in that order.  Halves 0-15 form a
+ *         32 B part A; halves 16-23 a 16 B part B stored after the part-A
+ *         records of all pairs (at pairs + 32 B * n_pairs * pair_stride).
  *   BF16/F16 (mesh, nearest fields): 8 halves {Ax,Ay,Bx,By,Az,Bz,0,0} (16 B)
- * so one aligned 256-bit load returns both bracketing snapshots of a node
- * (or of two z-neighbours), x,y components in register pairs. */
+ * so aligned 256-bit (and 128-bit) loads return both bracketing snapshots of
+ * a node (or of a yz-quad of nodes), x,y components in register pairs. */
 typedef struct {
     int32_t nx, ny, nz;
     int32_t bounds_mode;   /* JT_GRID_*                                       */
@@ -197,6 +199,16 @@ typedef struct {
     const float* tet_geom;  /* device (n_tets,16) as jt_mesh_field            */
     const int32_t* cell_start; /* device (cells+1) CSR offsets                 */
     const int32_t* cell_elems; /* device element ids, ascending within a cell */
+    /* Optional refinement that keeps the result: each hash cell split into
+     * sub_div^3 sub-cells, each listing (ascending) the cell's elements whose
+     * box, widened slightly, meets the sub-cell.  The element the cell scan
+     * would pick holds the query in its box, so it is on the query's
+     * sub-cell list, and every element before it there is before it in the
+     * cell list too.  sub_div 0: scan the cell lists. */
+    int32_t sub_div;
+    int32_t pad;
+    const int32_t* sub_start;  /* device (cells*sub_div^3 + 1) CSR offsets     */
+    const int32_t* sub_elems;  /* device element ids                          */
 } jt_fem_field;
 
 #define JT_FIELD_GRID 1

@@ -71,7 +71,8 @@ class NearestField(C.Structure):
 
 class FemField(C.Structure):
     _fields_ = [("nearest", NearestField), ("n_tets", i32), ("grid_size", i32 * 3), ("grid_min", f32 * 3),
-                ("cell_size", f32 * 3), ("tet_box", vp), ("tet_geom", vp), ("cell_start", vp), ("cell_elems", vp)]
+                ("cell_size", f32 * 3), ("tet_box", vp), ("tet_geom", vp), ("cell_start", vp), ("cell_elems", vp),
+                ("sub_div", i32), ("pad", i32), ("sub_start", vp), ("sub_elems", vp)]
 
 
 class Field(C.Structure):

@@ -57,15 +57,47 @@ __device__ __forceinline__ AxisD axis_d(float x, float org, float d, float inv_d
     return r;
 }
 
-// J^T g at p for entry e.  With acc set, the snapshot gradient of this
-// stage, w_c * g per corner node c, is added to acc (one float4 record per
-// node: x, y, z, unused); the blend coefficients of A and B are applied when
-// the accumulators are folded into the pair-record gradient.
-__device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, const jt_blend& e, const V3& g,
-                                       float4* __restrict__ acc) {
-    const AxisD ax = axis_d(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode);
-    const AxisD ay = axis_d(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode);
-    const AxisD az = axis_d(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode);
+// The three axes of a point: cells, weights and weight derivatives.
+struct Ax3 {
+    AxisD x, y, z;
+};
+
+__device__ __forceinline__ Ax3 axes_of(const jt_grid_field& F, const V3& p) {
+    return Ax3{axis_d(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode),
+               axis_d(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode),
+               axis_d(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode)};
+}
+
+__device__ __forceinline__ bool same_cell(const Ax3& a, const Ax3& b) {
+    return a.x.i0 == b.x.i0 && a.y.i0 == b.y.i0 && a.z.i0 == b.z.i0;
+}
+
+// Two schedule entries blend the same pair with the same coefficients.
+__device__ __forceinline__ bool same_entry(const jt_blend& a, const jt_blend& b) {
+    return a.pair == b.pair && a.form == b.form && __float_as_int(a.wa) == __float_as_int(b.wa) &&
+           __float_as_int(a.wb) == __float_as_int(b.wb);
+}
+
+// w_c * g into the accumulator records of the eight corners (no loads).
+__device__ __forceinline__ void scatter(const jt_grid_field& F, const Ax3& a, const V3& g, float4* __restrict__ acc) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
+        const int i = bx ? a.x.i1 : a.x.i0, j = by ? a.y.i1 : a.y.i0, k = bz ? a.z.i1 : a.z.i0;
+        const float w = (bx ? a.x.w : 1.0f - a.x.w) * (by ? a.y.w : 1.0f - a.y.w) * (bz ? a.z.w : 1.0f - a.z.w);
+        const int64_t node = (int64_t)(i * F.ny + j) * F.nz + k;
+        red_v4(reinterpret_cast<float*>(acc + node), w * g.x, w * g.y, w * g.z, 0.0f);
+    }
+}
+
+// J^T g at the point with axes a for entry e.  With acc set, the snapshot
+// gradient of this stage, w_c * g per corner node c, is added to acc (one
+// float4 record per node: x, y, z, unused); with `other` set (a second point
+// of the same stage time in the same cell), w'_c * g' is added in the same
+// atomic.  The blend coefficients of A and B are applied when the
+// accumulators are folded into the pair-record gradient.
+__device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const Ax3& a, const jt_blend& e, const V3& g,
+                                       float4* __restrict__ acc, const Ax3* other, const V3& g_other) {
     float ca, cb;
     blend_coefs(e, ca, cb);
     const int pr = min(max(e.pair, 0), F.n_pairs - 1);
@@ -74,8 +106,9 @@ __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, cons
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
-        const int i = bx ? ax.i1 : ax.i0, j = by ? ay.i1 : ay.i0, k = bz ? az.i1 : az.i0;
-        const float wx = bx ? ax.w : 1.0f - ax.w, wy = by ? ay.w : 1.0f - ay.w, wz = bz ? az.w : 1.0f - az.w;
+        const int i = bx ? a.x.i1 : a.x.i0, j = by ? a.y.i1 : a.y.i0, k = bz ? a.z.i1 : a.z.i0;
+        const float wx = bx ? a.x.w : 1.0f - a.x.w, wy = by ? a.y.w : 1.0f - a.y.w;
+        const float wz = bz ? a.z.w : 1.0f - a.z.w;
         const int64_t node = (int64_t)(i * F.ny + j) * F.nz + k;
         const PairVal pv = load_pair<JT_STORE_F32>(F.pairs, base + node);
         // blended corner value dotted with g
@@ -83,12 +116,20 @@ __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const V3& p, cons
         const float vz = ca * pv.az + cb * pv.bz;
         const float vg = vx * g.x + vy * g.y + vz * g.z;
         const float sx = bx ? 1.0f : -1.0f, sy = by ? 1.0f : -1.0f, sz = bz ? 1.0f : -1.0f;
-        jtg.x += sx * ax.dfdx * wy * wz * vg;
-        jtg.y += sy * ay.dfdx * wx * wz * vg;
-        jtg.z += sz * az.dfdx * wx * wy * vg;
+        jtg.x += sx * a.x.dfdx * wy * wz * vg;
+        jtg.y += sy * a.y.dfdx * wx * wz * vg;
+        jtg.z += sz * a.z.dfdx * wx * wy * vg;
         if (acc != nullptr) {
             const float w = wx * wy * wz;
-            red_v4(reinterpret_cast<float*>(acc + node), w * g.x, w * g.y, w * g.z, 0.0f);
+            float gx = w * g.x, gy = w * g.y, gz = w * g.z;
+            if (other != nullptr) {
+                const float ow = (bx ? other->x.w : 1.0f - other->x.w) * (by ? other->y.w : 1.0f - other->y.w) *
+                                 (bz ? other->z.w : 1.0f - other->z.w);
+                gx += ow * g_other.x;
+                gy += ow * g_other.y;
+                gz += ow * g_other.z;
+            }
+            red_v4(reinterpret_cast<float*>(acc + node), gx, gy, gz, 0.0f);
         }
     }
     return jtg;
@@ -112,10 +153,11 @@ __device__ __forceinline__ float bc_deriv(int kind, float x, float lo, float hi)
 }
 
 // Per recomputed step: the RK4 stage positions x0, x2 = x0 + h/2 k1,
-// x3 = x0 + h/2 k2, x4 = x0 + h k3 and the pre-boundary end point, with the
-// forward pass's exact arithmetic (integrate<true, JT_RK4>).
+// x3 = x0 + h/2 k2, x4 = x0 + h k3 and (PRE) the pre-boundary end point,
+// with the forward pass's exact arithmetic (integrate<true, JT_RK4>).
+template <bool PRE>
 struct StepRec {
-    float v[15];
+    float v[PRE ? 15 : 12];
 };
 
 #ifndef JT_ADJOINT_MIN_BLOCKS
@@ -125,6 +167,9 @@ struct StepRec {
 // One backward segment [s0, s1): lambda holds dL/dx_{s1} on entry, dL/dx_{s0}
 // on exit; acc (or NULL) receives the per-stage snapshot gradients, three
 // records per step (stage times t, t + h/2, t + h), (3*nseg, nodes) float4.
+// PRE: some axis has a boundary whose derivative is not 1 (clamp,
+// absorbing, reflective), so the pre-boundary end point is kept.
+template <bool PRE>
 __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
     k_adjoint_rk4(jt_grid_field F, jt_boundary B, jt_adjoint_params P, float4* __restrict__ acc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,7 +179,7 @@ __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
     typedef Ar<true> A;
     const int nseg = P.step_end - P.step_begin;
     const int64_t nodes = F.pair_stride;
-    StepRec rec[JT_ADJOINT_MAX_SEGMENT];
+    StepRec<PRE> rec[JT_ADJOINT_MAX_SEGMENT];
     V3 x{P.ckpt[3 * (int64_t)i], P.ckpt[3 * (int64_t)i + 1], P.ckpt[3 * (int64_t)i + 2]};
     const StepConst k{P.dt, P.dt_half, P.dt_sixth};
     int flags = 0;
@@ -160,37 +205,64 @@ __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
         }
         x = V3{A::add(x.x, A::mul(k.dt6, sm.x)), A::add(x.y, A::mul(k.dt6, sm.y)),
                A::add(x.z, A::mul(k.dt6, sm.z))};
-        r[12] = x.x; r[13] = x.y; r[14] = x.z;
+        if (PRE) { r[12] = x.x; r[13] = x.y; r[14] = x.z; }
         apply_boundary<true>(B, x.x, x.y, x.z);
     }
     V3 lam{P.lambda[3 * (int64_t)i], P.lambda[3 * (int64_t)i + 1], P.lambda[3 * (int64_t)i + 2]};
+    // The scatter of k1 = v(x0) at step s waits for step s-1: its stage time
+    // t_s usually carries the same blend entry as t_{s-1} + h (k4 of step
+    // s-1) and x0 lies next to x4 of step s-1, so one atomic per corner
+    // often carries both.  pend_* hold the waiting scatter.
+    bool pend = false;
+    Ax3 pend_ax;
+    V3 pend_g{0.f, 0.f, 0.f};
+    float4* pend_acc = nullptr;
+    const jt_blend* pend_e = nullptr;
+    const V3 none{0.f, 0.f, 0.f};
     for (int s = nseg - 1; s >= 0; --s) {
         const jt_blend* e = P.schedule + 4 * (int64_t)(P.step_begin + s);
         const jt_blend e0 = e[0], e1 = e[1], e2 = e[2];
         const float* r = rec[s].v;
         const V3 x0{r[0], r[1], r[2]}, x2{r[3], r[4], r[5]}, x3{r[6], r[7], r[8]}, x4{r[9], r[10], r[11]};
         // through the boundary at the pre-boundary end point
-        lam.x *= bc_deriv(B.axis_kind[0], r[12], B.lo[0], B.hi[0]);
-        lam.y *= bc_deriv(B.axis_kind[1], r[13], B.lo[1], B.hi[1]);
-        lam.z *= bc_deriv(B.axis_kind[2], r[14], B.lo[2], B.hi[2]);
+        if (PRE) {
+            lam.x *= bc_deriv(B.axis_kind[0], r[PRE ? 12 : 0], B.lo[0], B.hi[0]);
+            lam.y *= bc_deriv(B.axis_kind[1], r[PRE ? 13 : 1], B.lo[1], B.hi[1]);
+            lam.z *= bc_deriv(B.axis_kind[2], r[PRE ? 14 : 2], B.lo[2], B.hi[2]);
+        }
         float4* a0 = acc != nullptr ? acc + (int64_t)(3 * s) * nodes : nullptr;
         float4* a1 = acc != nullptr ? a0 + nodes : nullptr;
         float4* a2 = acc != nullptr ? a1 + nodes : nullptr;
         // reverse sweep
         const float c6 = k.dt6, c3 = 2.0f * k.dt6;
         V3 lx = lam;
-        const V3 d4 = grid_vjp(F, x4, e2, V3{c6 * lam.x, c6 * lam.y, c6 * lam.z}, a2);   // k4 = v(x4)
+        const Ax3 ax4 = axes_of(F, x4);
+        const bool join = pend && same_entry(*pend_e, e2) && same_cell(pend_ax, ax4);
+        if (pend && !join) scatter(F, pend_ax, pend_g, pend_acc);
+        const V3 d4 = grid_vjp(F, ax4, e2, V3{c6 * lam.x, c6 * lam.y, c6 * lam.z}, join ? pend_acc : a2,
+                               join ? &pend_ax : nullptr, pend_g);                         // k4 = v(x4)
         lx = V3{lx.x + d4.x, lx.y + d4.y, lx.z + d4.z};
         const V3 g3{c3 * lam.x + k.dt * d4.x, c3 * lam.y + k.dt * d4.y, c3 * lam.z + k.dt * d4.z};
-        const V3 d3 = grid_vjp(F, x3, e1, g3, a1);                                          // k3 = v(x3)
+        // k3 = v(x3) and k2 = v(x2) share the stage time t + h/2 and almost
+        // always the cell: one atomic per corner carries both contributions
+        const Ax3 ax3 = axes_of(F, x3), ax2 = axes_of(F, x2);
+        const bool merge = same_cell(ax3, ax2);
+        const V3 d3 = grid_vjp(F, ax3, e1, g3, merge ? nullptr : a1, nullptr, none);
         lx = V3{lx.x + d3.x, lx.y + d3.y, lx.z + d3.z};
         const V3 g2{c3 * lam.x + k.dth * d3.x, c3 * lam.y + k.dth * d3.y, c3 * lam.z + k.dth * d3.z};
-        const V3 d2 = grid_vjp(F, x2, e1, g2, a1);                                          // k2 = v(x2)
+        const V3 d2 = grid_vjp(F, ax2, e1, g2, a1, merge ? &ax3 : nullptr, g3);
         lx = V3{lx.x + d2.x, lx.y + d2.y, lx.z + d2.z};
         const V3 g1{c6 * lam.x + k.dth * d2.x, c6 * lam.y + k.dth * d2.y, c6 * lam.z + k.dth * d2.z};
-        const V3 d1 = grid_vjp(F, x0, e0, g1, a0);                                          // k1 = v(x0)
+        const Ax3 ax0 = axes_of(F, x0);
+        const V3 d1 = grid_vjp(F, ax0, e0, g1, nullptr, nullptr, none);                     // k1 = v(x0)
         lam = V3{lx.x + d1.x, lx.y + d1.y, lx.z + d1.z};
+        pend = acc != nullptr;
+        pend_ax = ax0;
+        pend_g = g1;
+        pend_acc = a0;
+        pend_e = e;
     }
+    if (pend) scatter(F, pend_ax, pend_g, pend_acc);
     P.lambda[3 * (int64_t)i] = lam.x;
     P.lambda[3 * (int64_t)i + 1] = lam.y;
     P.lambda[3 * (int64_t)i + 2] = lam.z;
@@ -268,7 +340,10 @@ extern "C" int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, cons
         const cudaError_t e = cudaMemsetAsync(acc, 0, need, s);
         if (e != cudaSuccess) return cuda_status(e, "adjoint workspace memset");
     }
-    k_adjoint_rk4<<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
+    bool pre = false;
+    for (int a = 0; a < 3; ++a) pre |= bc->axis_kind[a] != JT_BC_PERIODIC && bc->axis_kind[a] != JT_BC_NONE;
+    if (pre) k_adjoint_rk4<true><<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
+    else k_adjoint_rk4<false><<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
     int rc = cuda_status(cudaGetLastError(), "adjoint kernel launch");
     if (rc != JT_OK || acc == nullptr) return rc;
     k_adjoint_fold<<<grid_blocks(F.pair_stride), kBlock, 0, s>>>(F, p->schedule + 4 * (int64_t)p->step_begin, nseg,

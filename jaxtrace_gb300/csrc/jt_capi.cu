@@ -90,6 +90,9 @@ static int check_field(const jt_field* f) {
             if (h->tet_box == nullptr || h->tet_geom == nullptr || h->cell_start == nullptr ||
                 h->cell_elems == nullptr)
                 return set_error(JT_ERR_INVALID, "FEM field has a NULL array");
+            if (h->sub_div < 0 || h->sub_div > 16 || (h->sub_div > 0 && (h->sub_start == nullptr ||
+                                                                         h->sub_elems == nullptr)))
+                return set_error(JT_ERR_INVALID, "FEM sub-cell lists: sub_div must be 0..16 with both arrays set");
             return check_nearest(&h->nearest);
         }
         default:

@@ -151,14 +151,21 @@ __device__ __forceinline__ PairVal decode3(uint32_t w0, uint32_t w1, uint32_t w2
     return PairVal{a, b, z.x, z.y};
 }
 
-// 16-bit z-pair record of the grid field (32 B): node (i,j,k) in words 0-2
-// and its z-successor (i,j,k1) in words 3-5, k1 as the sampler computes it.
+// 16-bit yz-quad record of the grid field (48 B): nodes (i,j,k), (i,j,k1),
+// (i,j1,k), (i,j1,k1), j1 and k1 as the sampler computes them, three words
+// each in that order.  Words 0-7 are part A (32 B, records [0, part_b)) and
+// words 8-11 part B (16 B, after every part-A record), so one 256-bit and
+// one 128-bit load fetch the quad; 48 B for four corners instead of 64 B.
 template <int STORE>
-__device__ __forceinline__ void load_zpair(const void* base, int64_t rec, PairVal& p0, PairVal& p1) {
+__device__ __forceinline__ void load_quad(const void* base, int64_t part_b, int64_t rec, PairVal& p00,
+                                          PairVal& p01, PairVal& p10, PairVal& p11) {
     uint32_t w[8];
     ldg256(reinterpret_cast<const uint4*>(base) + 2 * rec, w);
-    p0 = decode3<STORE>(w[0], w[1], w[2]);
-    p1 = decode3<STORE>(w[3], w[4], w[5]);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(base) + 2 * part_b + rec);
+    p00 = decode3<STORE>(w[0], w[1], w[2]);
+    p01 = decode3<STORE>(w[3], w[4], w[5]);
+    p10 = decode3<STORE>(w[6], w[7], v.x);
+    p11 = decode3<STORE>(v.y, v.z, v.w);
 }
 
 // 16-bit single-node record (16 B), used by the mesh and nearest fields.

@@ -68,6 +68,34 @@ __device__ __forceinline__ float sph_w(float r, float h) {
     }
 }
 
+// The kernels again with the 1/h and sigma of a uniform smoothing length
+// hoisted out of the pair loop (no division per pair).
+template <int DIM, int KERN>
+__device__ __forceinline__ float sph_sigma(float hh) {
+    const float pi = 3.14159265358979f;
+    if (KERN == JT_SPH_CUBIC) return DIM == 2 ? 10.0f / (7.0f * pi * hh * hh) : 1.0f / (pi * hh * hh * hh);
+    if (KERN == JT_SPH_WENDLAND) return DIM == 2 ? 7.0f / (pi * hh * hh) : 21.0f / (2.0f * pi * hh * hh * hh);
+    const float ph2 = pi * hh * hh;
+    return DIM == 2 ? 1.0f / ph2 : 1.0f / (ph2 * sqrtf(ph2));
+}
+
+template <int KERN>
+__device__ __forceinline__ float sph_shape(float q) {
+    if (KERN == JT_SPH_CUBIC) {
+        if (q <= 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
+        if (q <= 2.0f) {
+            const float t = 2.0f - q;
+            return 0.25f * t * t * t;
+        }
+        return 0.0f;
+    } else if (KERN == JT_SPH_WENDLAND) {
+        const float t = fmaxf(1.0f - q, 0.0f);
+        const float t2 = t * t;
+        return t2 * t2 * (1.0f + 4.0f * q);
+    }
+    return expf(-q * q);
+}
+
 template <int DIM, int KERN>
 __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -84,23 +112,48 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
     const int y0 = max(cy - P.reach[1], 0), y1 = min(cy + P.reach[1], lim);
     const int x0 = max(cx - P.reach[0], 0), x1 = min(cx + P.reach[0], lim);
     double acc = 0.0;
-    for (int z = z0; z <= z1; ++z) {
-        for (int y = y0; y <= y1; ++y) {
-            uint32_t b, e;
-            row_range(P.cell_end, x0, x1, y, z, g.bits, b, e);
-            float part = 0.0f;
-            for (uint32_t j = b; j < e; ++j) {
-                const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
-                const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
-                const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 <= r2max) {
-                    const float h = P.h != nullptr ? __ldg(P.h + j) : P.h_const;
-                    const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
-                    part += m * sph_w<DIM, KERN>(sqrtf(d2), h);
+    if (P.h == nullptr) {
+        // uniform h: sigma and 1/h once; pairs beyond the kernel's support skip
+        const float hh = fmaxf(P.h_const, 1e-12f), inv = 1.0f / hh, sigma = sph_sigma<DIM, KERN>(hh);
+        const float sup = KERN == JT_SPH_CUBIC ? 2.0f * hh : (KERN == JT_SPH_WENDLAND ? hh : 3.4e38f);
+        const float r2lim = fminf(r2max, sup >= 1.8e19f ? r2max : sup * sup);
+        for (int z = z0; z <= z1; ++z) {
+            for (int y = y0; y <= y1; ++y) {
+                uint32_t b, e;
+                row_range(P.cell_end, x0, x1, y, z, g.bits, b, e);
+                float part = 0.0f;
+                for (uint32_t j = b; j < e; ++j) {
+                    const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
+                    const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
+                    const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 <= r2lim) {
+                        const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
+                        part += m * sph_shape<KERN>(sqrtf(d2) * inv);
+                    }
                 }
+                acc += (double)part * (double)sigma;
             }
-            acc += (double)part;
+        }
+    } else {
+        for (int z = z0; z <= z1; ++z) {
+            for (int y = y0; y <= y1; ++y) {
+                uint32_t b, e;
+                row_range(P.cell_end, x0, x1, y, z, g.bits, b, e);
+                float part = 0.0f;
+                for (uint32_t j = b; j < e; ++j) {
+                    const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
+                    const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
+                    const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 <= r2max) {
+                        const float h = __ldg(P.h + j);
+                        const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
+                        part += m * sph_w<DIM, KERN>(sqrtf(d2), h);
+                    }
+                }
+                acc += (double)part;
+            }
         }
     }
     P.out[i] = acc;

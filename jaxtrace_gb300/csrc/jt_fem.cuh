@@ -34,17 +34,41 @@ struct FemField {
         return (int)fminf(fmaxf(f, 0.0f), (float)(n - 1));
     }
 
+    // sub-cell of coordinate q inside hash cell c: floor((q - (lo + c*cs)) /
+    // (cs/S)) clipped to [0, S-1]; the host lists widen the sub-cells enough
+    // to absorb the rounding of this float32 arithmetic
+    __device__ __forceinline__ int sub_coord(float q, float lo, float cs, int c, int S) const {
+        const float cell_lo = lo + (float)c * cs;
+        const float f = floorf((q - cell_lo) * ((float)S / cs));
+        return (int)fminf(fmaxf(f, 0.0f), (float)(S - 1));
+    }
+
     __device__ __forceinline__ V3 operator()(const V3& q, const jt_blend& e, int& flags) const {
         const int cx = cell_coord(q.x, F.grid_min[0], F.cell_size[0], F.grid_size[0]);
         const int cy = cell_coord(q.y, F.grid_min[1], F.cell_size[1], F.grid_size[1]);
         const int cz = cell_coord(q.z, F.grid_min[2], F.cell_size[2], F.grid_size[2]);
         const int cell = (cx * F.grid_size[1] + cy) * F.grid_size[2] + cz;
-        const int b0 = __ldg(F.cell_start + cell), b1 = __ldg(F.cell_start + cell + 1);
+        const int32_t* list = F.cell_elems;
+        int b0, b1;
+        if (F.sub_div > 0) {
+            // the query's sub-cell, clamped into its hash cell
+            const int S = F.sub_div;
+            const int sx = sub_coord(q.x, F.grid_min[0], F.cell_size[0], cx, S);
+            const int sy = sub_coord(q.y, F.grid_min[1], F.cell_size[1], cy, S);
+            const int sz = sub_coord(q.z, F.grid_min[2], F.cell_size[2], cz, S);
+            const int64_t sc = (int64_t)cell * (S * S * S) + (sx * S + sy) * S + sz;
+            b0 = __ldg(F.sub_start + sc);
+            b1 = __ldg(F.sub_start + sc + 1);
+            list = F.sub_elems;
+        } else {
+            b0 = __ldg(F.cell_start + cell);
+            b1 = __ldg(F.cell_start + cell + 1);
+        }
         // lax.scan over the cell's candidates keeps the first hit (:280-305)
         for (int s = b0; s < b1; ++s) {
             float4 b;
             int4 cn;
-            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(F.cell_elems + s), b, cn)) continue;
+            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(list + s), b, cn)) continue;
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
                                      node_value(cn.w, e));
         }

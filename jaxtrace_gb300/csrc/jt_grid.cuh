@@ -89,7 +89,7 @@ struct GridField {
         const int r00 = (i0 * ny + j0) * nz, r10 = (i1 * ny + j0) * nz;
         const int r01 = (i0 * ny + j1) * nz, r11 = (i1 * ny + j1) * nz;
         // all gathers issued before any use: eight 32-byte float32 node
-        // records, or four 32-byte 16-bit z-pair records (k0 and k1 together)
+        // records, or two 48-byte 16-bit yz-quad records (i0 and i1)
         PairVal p000, p100, p010, p110, p001, p101, p011, p111;
         if (STORE == JT_STORE_F32) {
             p000 = load_pair<STORE>(F.pairs, base + (r00 + k0));
@@ -101,10 +101,9 @@ struct GridField {
             p011 = load_pair<STORE>(F.pairs, base + (r01 + k1));
             p111 = load_pair<STORE>(F.pairs, base + (r11 + k1));
         } else {
-            load_zpair<STORE>(F.pairs, base + (r00 + k0), p000, p001);
-            load_zpair<STORE>(F.pairs, base + (r10 + k0), p100, p101);
-            load_zpair<STORE>(F.pairs, base + (r01 + k0), p010, p011);
-            load_zpair<STORE>(F.pairs, base + (r11 + k0), p110, p111);
+            const int64_t part_b = (int64_t)F.n_pairs * F.pair_stride;
+            load_quad<STORE>(F.pairs, part_b, base + (r00 + k0), p000, p001, p010, p011);
+            load_quad<STORE>(F.pairs, part_b, base + (r10 + k0), p100, p101, p110, p111);
         }
         const bool wgt = e.form == JT_BLEND_WEIGHTED;
         const float2 WA = splat(e.wa), WB = splat(e.wb);

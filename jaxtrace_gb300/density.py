@@ -395,6 +395,9 @@ class SPHDensityEstimator:
         lo = [min(float(P3[:, a].min()), float(Q3[:, a].min())) for a in range(d)] + [0.0] * (3 - d)
         hi = [max(float(P3[:, a].max()), float(Q3[:, a].max())) for a in range(d)] + [0.0] * (3 - d)
         cl = CellList(P3, lo, hi, max(search / 2.0, 1e-6), d)
+        # queries in the same cell order, so a warp's queries walk the same
+        # candidate cells together (broadcast loads); results scattered back
+        qcl = CellList(Q3, lo, hi, max(search / 2.0, 1e-6), d)
         idx = cl.ids.long()
         h_sorted = None if self._uniform_h is not None else self.smoothing_lengths[idx].contiguous()
         m_sorted = None if self.masses_dev is None else self.masses_dev[idx].contiguous()
@@ -410,9 +413,11 @@ class SPHDensityEstimator:
         p.masses = m_sorted.data_ptr() if m_sorted is not None else None
         p.h = h_sorted.data_ptr() if h_sorted is not None else None
         p.cell_end = cl.cell_end.data_ptr()
-        p.queries = Q3.data_ptr()
-        p.out = out.data_ptr()
+        p.queries = qcl.sorted.data_ptr()
+        out_sorted = torch.empty(M, dtype=torch.float64, device="cuda")
+        p.out = out_sorted.data_ptr()
         L.check(L.load().jt_sph_density(C.byref(p), L.stream_ptr()))
+        out.index_copy_(0, qcl.ids.long(), out_sorted)
         return out
 
     def evaluate(self, eval_points) -> np.ndarray:

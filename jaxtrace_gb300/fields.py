@@ -77,48 +77,61 @@ def snapshot_scales(data: np.ndarray, storage: int) -> np.ndarray:
 A_SLOTS, B_SLOTS = [0, 1, 4], [2, 3, 5]   # record {Ax,Ay,Bx,By,Az,Bz,0,0}
 
 
-def build_pairs_device(data: np.ndarray, storage: int, device="cuda", z_successor: np.ndarray | None = None):
+def build_pairs_device(data: np.ndarray, storage: int, device="cuda", quad: tuple | None = None):
     """Upload (T,N,3) snapshots as (max(T-1,1), N, 8) pair records
     {Ax,Ay,Bx,By,Az,Bz,0,0} (A = snapshot p, B = snapshot p+1).
 
-    With ``z_successor`` (16-bit grid fields) each record is a 16-slot z-pair:
-    node n in slots 0-5 and node z_successor[n] in slots 6-11."""
+    With ``quad`` = (z_succ, y_succ) (16-bit grid fields) each node n gets a
+    48-byte yz-quad record of the nodes n, z_succ[n], y_succ[n] and
+    y_succ[z_succ[n]], six halves each in node order, split into a 32-byte
+    part A (halves 0-15, all part-A records first) and a 16-byte part B
+    (halves 16-23, after every part-A record) so both parts stay aligned for
+    one 256-bit and one 128-bit load.  Returns the flat buffer and scales."""
     torch = _torch_cuda()
     T, N, _ = data.shape
     P = max(T - 1, 1)
     scales = snapshot_scales(data, storage)
-    zp = z_successor is not None and storage != L.JT_STORE_F32
-    width = 16 if zp else 8
+    qd = quad is not None and storage != L.JT_STORE_F32
     if storage == L.JT_STORE_F32:
-        pairs = torch.zeros((P, N, width), dtype=torch.float32, device=device)
+        dt = torch.float32
     else:
         dt = torch.bfloat16 if storage == L.JT_STORE_BF16 else torch.float16
-        pairs = torch.zeros((P, N, width), dtype=dt, device=device)
-    a_idx = torch.tensor(A_SLOTS, device=device)
-    b_idx = torch.tensor(B_SLOTS, device=device)
-    a2_idx = a_idx + 6
-    b2_idx = b_idx + 6
-    succ = torch.from_numpy(np.asarray(z_successor, dtype=np.int64)).to(device) if zp else None
-    prev = None
+    if qd:
+        buf = torch.zeros(P * N * 24, dtype=dt, device=device)
+        part_a = buf[: P * N * 16].view(P, N, 16)
+        part_b = buf[P * N * 16:].view(P, N, 8)
+        zs = torch.from_numpy(np.asarray(quad[0], dtype=np.int64)).to(device)
+        ys = torch.from_numpy(np.asarray(quad[1], dtype=np.int64)).to(device)
+        yzs = ys[zs]
+    else:
+        buf = torch.zeros((P, N, 8), dtype=dt, device=device)
+    ix = lambda v: torch.tensor(v, device=device)  # noqa: E731
+    # part-A slots of the A and B snapshots of quad nodes 0 (n) and 1 (z_succ)
+    quad_slots = [([0, 1, 4], [2, 3, 5]), ([6, 7, 10], [8, 9, 11])]
     for t in range(T):
         snap = torch.from_numpy(np.ascontiguousarray(data[t])).to(device)
         if storage != L.JT_STORE_F32:
-            snap = (snap / float(scales[t])).to(pairs.dtype)
-        nxt = snap[succ] if zp else None
+            snap = (snap / float(scales[t])).to(dt)
+        targets = []
         if t < P:
-            pairs[t].index_copy_(1, a_idx, snap)
-            if zp:
-                pairs[t].index_copy_(1, a2_idx, nxt)
+            targets.append((t, 0))      # this snapshot is A of pair t
         if t >= 1:
-            pairs[t - 1].index_copy_(1, b_idx, snap)
-            if zp:
-                pairs[t - 1].index_copy_(1, b2_idx, nxt)
-        prev = (snap, nxt)
-    if T == 1:
-        pairs[0].index_copy_(1, b_idx, prev[0])
-        if zp:
-            pairs[0].index_copy_(1, b2_idx, prev[1])
-    return pairs, scales
+            targets.append((t - 1, 1))  # and B of pair t-1
+        if T == 1:
+            targets.append((0, 1))
+        for pr, side in targets:
+            if not qd:
+                buf[pr].index_copy_(1, ix(A_SLOTS if side == 0 else B_SLOTS), snap)
+                continue
+            vals = (snap, snap[zs], snap[ys], snap[yzs])
+            for node in range(2):
+                part_a[pr].index_copy_(1, ix(quad_slots[node][side]), vals[node])
+            # node y_succ: x, y in part A (A: 12,13 / B: 14,15), z in part B (A: 0 / B: 1)
+            part_a[pr].index_copy_(1, ix([12, 13] if side == 0 else [14, 15]), vals[2][:, :2].contiguous())
+            part_b[pr][:, 0 if side == 0 else 1] = vals[2][:, 2]
+            # node y_succ(z_succ): part B (A: 2,3,6 / B: 4,5,7)
+            part_b[pr].index_copy_(1, ix([2, 3, 6] if side == 0 else [4, 5, 7]), vals[3])
+    return buf, scales
 
 
 class _DeviceField:
@@ -310,21 +323,30 @@ class StructuredTimeSeriesField(_DeviceField):
         self.z_min, self.z_max = float(gz[0]), float(gz[-1])
         self._mode = codes[mode]
 
-    def _z_successor(self) -> np.ndarray:
-        """Node index of (i, j, k1) for every node (i, j, k), k1 as the sampler
-        computes it (structured.py:311-318)."""
+    def _successors(self):
+        """Node indices of (i, j, k1) and (i, j1, k) for every node (i, j, k),
+        j1 and k1 as the sampler computes them (structured.py:311-318)."""
         nx, ny, nz = self.Nx, self.Ny, self.Nz
-        k = np.arange(nz)
-        k1 = (k + 1) % max(nz, 1) if self._mode == L.JT_GRID_PERIODIC else np.minimum(k + 1, max(nz - 1, 0))
-        col = np.arange(nx * ny, dtype=np.int64)[:, None] * nz
-        return (col + k1[None, :]).reshape(-1)
+        per = self._mode == L.JT_GRID_PERIODIC
+
+        def nxt(n):
+            a = np.arange(n)
+            return (a + 1) % max(n, 1) if per else np.minimum(a + 1, max(n - 1, 0))
+
+        i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+        zs = (i * ny + j) * nz + nxt(nz)[k]
+        ys = (i * ny + nxt(ny)[j]) * nz + k
+        return zs.reshape(-1).astype(np.int64), ys.reshape(-1).astype(np.int64)
 
     def _device(self):
         if self._dev is not None:
             return
-        pairs, scales = build_pairs_device(self.data, self._storage, z_successor=self._z_successor())
+        pairs, scales = build_pairs_device(self.data, self._storage, quad=self._successors())
         self._scales = scales
-        self._dev = {"pairs": pairs}
+        P = max(self.data.shape[0] - 1, 1)
+        # node n's own six values sit in slots 0-5 of both record layouts
+        view = pairs if self._storage == L.JT_STORE_F32 else pairs[: P * self.N * 16].view(P, self.N, 16)
+        self._dev = {"pairs": view, "buffer": pairs}
         g = L.GridField()
         g.nx, g.ny, g.nz = self.Nx, self.Ny, self.Nz
         g.bounds_mode = self._mode
@@ -335,7 +357,7 @@ class StructuredTimeSeriesField(_DeviceField):
         g.valid_hi[:] = [F32(self.x_min + (self.Nx - 1) * self.dx), F32(self.y_min + (self.Ny - 1) * self.dy),
                          F32(self.z_min + (self.Nz - 1) * self.dz)]
         g.storage = self._storage
-        g.n_pairs = pairs.shape[0]
+        g.n_pairs = P
         g.pair_stride = self.N
         g.pairs = pairs.data_ptr()
         self._cgrid = g
@@ -484,7 +506,7 @@ class FemHashGrid:
     the reference's -1-padded table.
     """
 
-    def __init__(self, points, connectivity, grid_resolution: int = 32):
+    def __init__(self, points, connectivity, grid_resolution: int = 32, sub_div: int = 4):
         P = np.asarray(points, dtype=F32)
         T4 = np.asarray(connectivity, dtype=np.int32)
         if P.ndim != 2 or P.shape[1] != 3:
@@ -527,6 +549,7 @@ class FemHashGrid:
         self.cell_start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
         self.cell_elems = elem[order].astype(np.int32)
         self.max_elems_per_cell = int(counts.max()) if n_cells else 0
+        self._build_sub_cells(int(sub_div), elem, np.stack([i, j, k], axis=1), emin, emax, bmin, cell64)
         # device records: box (min xyz,0,max xyz,0) and geometry (v0, v1-v0, v2-v0, v3-v0, ids)
         M = len(T4)
         self.tet_box = np.zeros((M, 8), dtype=F32)
@@ -538,6 +561,44 @@ class FemHashGrid:
         self.tet_geom[:, 6:9] = V[:, 2] - v0
         self.tet_geom[:, 9:12] = V[:, 3] - v0
         self.tet_geom[:, 12:16] = T4.view(F32)
+
+    def _build_sub_cells(self, S, elem, cidx, emin, emax, bmin, cell64):
+        """Sub-cell lists (S^3 per hash cell): for each (element, cell) entry
+        the sub-cells of that cell its box meets, widened by a margin that
+        covers the float32 rounding of the device's sub-cell index; stable
+        ordering keeps the elements of every list ascending."""
+        self.sub_div = S
+        if S <= 0 or len(elem) == 0:
+            self.sub_div = 0
+            self.sub_start = np.zeros(1, np.int32)
+            self.sub_elems = np.zeros(1, np.int32)
+            return
+        sub = cell64 / S
+        scale = float(np.abs(self.points).max()) if len(self.points) else 1.0
+        eps = 1e-3 * sub + 4e-7 * max(scale, 1.0)
+        lo = bmin.astype(np.float64) + cidx * cell64               # the entry's cell corner
+        e_lo = emin[elem].astype(np.float64) - eps
+        e_hi = emax[elem].astype(np.float64) + eps
+        slo = np.clip(np.floor((e_lo - lo) / np.where(sub > 0, sub, 1.0)), 0, S - 1).astype(np.int64)
+        shi = np.clip(np.floor((e_hi - lo) / np.where(sub > 0, sub, 1.0)), 0, S - 1).astype(np.int64)
+        slo = np.where(sub > 0, slo, 0)
+        shi = np.where(sub > 0, shi, S - 1)
+        ext = shi - slo + 1
+        count = ext.prod(axis=1)
+        el = np.repeat(elem, count)
+        first = np.repeat(np.cumsum(count) - count, count)
+        r = np.arange(len(el), dtype=np.int64) - first
+        ez, ey = np.repeat(ext[:, 2], count), np.repeat(ext[:, 1], count)
+        sz = np.repeat(slo[:, 2], count) + r % ez
+        sy = np.repeat(slo[:, 1], count) + (r // ez) % ey
+        sx = np.repeat(slo[:, 0], count) + r // (ez * ey)
+        cell = np.repeat((cidx[:, 0] * self.grid_size[1] + cidx[:, 1]) * self.grid_size[2] + cidx[:, 2], count)
+        sid = cell * (S ** 3) + (sx * S + sy) * S + sz
+        order = np.argsort(sid, kind="stable")
+        n_sub = int(np.prod(self.grid_size)) * S ** 3
+        cnt = np.bincount(sid, minlength=n_sub)
+        self.sub_start = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
+        self.sub_elems = el[order].astype(np.int32)
 
     def cell_to_elements(self) -> np.ndarray:
         """The reference's (cells, max_per_cell) table, -1 padded."""
@@ -556,10 +617,10 @@ class FEMTimeSeriesField(TimeSeriesField):
 
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
-                 fem_grid_resolution: int = 32, *, storage: str = "f32"):
+                 fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: int = 4):
         super().__init__(data, times, positions, interpolation, extrapolation, _source_info, storage=storage,
                          time_semantics="jax")
-        self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution)
+        self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution, sub_div=sub_div)
 
     def _device(self):
         if self._dev is not None:
@@ -572,6 +633,8 @@ class FEMTimeSeriesField(TimeSeriesField):
         d["tet_geom"] = torch.from_numpy(h.tet_geom).cuda()
         d["cell_start"] = torch.from_numpy(h.cell_start).cuda()
         d["cell_elems"] = torch.from_numpy(h.cell_elems if len(h.cell_elems) else np.zeros(1, np.int32)).cuda()
+        d["sub_start"] = torch.from_numpy(h.sub_start).cuda()
+        d["sub_elems"] = torch.from_numpy(h.sub_elems if len(h.sub_elems) else np.zeros(1, np.int32)).cuda()
         f = L.FemField()
         f.nearest = self._cnear
         f.n_tets = len(h.connectivity)
@@ -580,6 +643,8 @@ class FEMTimeSeriesField(TimeSeriesField):
         f.cell_size[:] = [float(v) for v in h.grid_cell_size]
         f.tet_box, f.tet_geom = d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
         f.cell_start, f.cell_elems = d["cell_start"].data_ptr(), d["cell_elems"].data_ptr()
+        f.sub_div = h.sub_div
+        f.sub_start, f.sub_elems = d["sub_start"].data_ptr(), d["sub_elems"].data_ptr()
         self._cfem = f
         self._cfield = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(f))
 

@@ -48,3 +48,31 @@ def test_hash_grid_anisotropic_and_degenerate_inputs():
         jt.FemHashGrid(P, np.array([[0, 1, 2, 99]], np.int32))
     with pytest.raises(ValueError):
         jt.FemHashGrid(P[:, :2], T4)
+
+
+def test_sub_cell_lists_hold_every_candidate_the_cell_scan_can_pick():
+    """Every element of the query's hash-cell list whose box holds the query
+    is on the query's sub-cell list (sub-cell index computed with the
+    kernel's float32 arithmetic), and sub lists stay ascending, so the first
+    containing element found is the one the reference's cell scan finds."""
+    from jaxtrace_gb300 import workloads as W
+    P, T4 = W.kuhn_mesh(10, 0.2, 3)
+    h = jt.FemHashGrid(P, T4, 12, sub_div=4)
+    S = h.sub_div
+    rng = np.random.default_rng(5)
+    q = np.concatenate([rng.random((4000, 3)), rng.uniform(-0.2, 1.2, (500, 3)),
+                        P[rng.integers(0, len(P), 500)]]).astype(F32)
+    gmin, cs, gs = h.grid_min, h.grid_cell_size, np.array(h.grid_size)
+    eb = h.element_bounds
+    for p in q:
+        c = np.clip(np.floor((p - gmin) / cs), 0, gs - 1).astype(int)        # float32 ops, as the kernel
+        cell = (c[0] * gs[1] + c[1]) * gs[2] + c[2]
+        lo = (c.astype(F32) * cs + gmin).astype(F32)
+        f = np.floor((p - lo) * (F32(S) / cs))
+        sc = np.clip(f, 0, S - 1).astype(int)
+        sid = cell * S ** 3 + (sc[0] * S + sc[1]) * S + sc[2]
+        sub = h.sub_elems[h.sub_start[sid]:h.sub_start[sid + 1]]
+        assert np.all(np.diff(sub) > 0)
+        cand = h.cell_elems[h.cell_start[cell]:h.cell_start[cell + 1]]
+        holds = cand[np.all((eb[cand, 0] <= p) & (p <= eb[cand, 1]), axis=1)]
+        assert np.isin(holds, sub).all()
