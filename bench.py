@@ -33,9 +33,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "RK4 particle-steps/s on 1 GB300: BF16/adjoint vs plain FP32 at stated FP64 error"
 UNIT = "particle-steps/s"
-# algorithmic bytes per RK4 particle-step (cache-oblivious): 4 field evaluations
-# x 2 snapshots x 8 corners x 3 values + 24 B of position read/write
-BYTES_PER_PSTEP = {"f32": 4 * 2 * 8 * 12 + 24, "bf16": 4 * 2 * 8 * 6 + 24, "f16": 4 * 2 * 8 * 6 + 24}
+# algorithmic bytes per RK4 particle-step of k_track (cache-oblivious): 4 field
+# evaluations x 8 corners x 3 values of one pre-blended time level (float32 or
+# float16 stage fields) + 24 B of position read/write
+BYTES_PER_PSTEP = {"f32": 4 * 8 * 12 + 24, "bf16": 4 * 8 * 6 + 24, "f16": 4 * 8 * 6 + 24}
 
 
 def traffic_per_pstep(storage):
@@ -77,7 +78,8 @@ def args_parse():
     p.add_argument("--fem-steps", type=int, default=1000)
     p.add_argument("--adj-lattice", default="256,256,64", help="seed lattice of the adjoint leg")
     p.add_argument("--adj-steps", type=int, default=500)
-    p.add_argument("--leg", default=None, choices=["fem", "batch", "adjoint"],
+    p.add_argument("--density-particles", type=int, default=16_000_000)
+    p.add_argument("--leg", default=None, choices=["fem", "batch", "adjoint", "density"],
                    help="run one configuration leg alone and print its JSON (with --profile: the leg's timed "
                         "region bracketed by cudaProfilerStart/Stop)")
     p.add_argument("--profile", action="store_true",
@@ -456,7 +458,7 @@ def fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc):
                                   "oracle_fallbacks": info["fallback_count"]}}
 
 
-def batch_leg(a, profile=False):
+def batch_leg(a, profile=False, part="track"):
     """Batching + density configuration: 256 ensembles of round(10^U(3,6))
     particles (default_rng(7); 36,800,084 in all) released at U(0,0.5) on the
     FEM mesh, 400 RK4 steps of dt=0.005 each from its own release time, in
@@ -474,6 +476,10 @@ def batch_leg(a, profile=False):
     sizes, release, xs = W.ensembles()
     tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
     b = tr.ensemble_batch(xs, release, 401, dt=0.005)
+    if part == "density":
+        # positions only: one untimed pass, then the density passes alone
+        b.run()
+        return density_part(b.pos[: a.density_particles].contiguous(), profile)
     tune = jt.Autotuner(cache_path="").tune_batch(b)
     b.capture()
     b.run()
@@ -510,20 +516,37 @@ def batch_leg(a, profile=False):
                         "trials": len(tune.trials)},
            "parity_f32_oracle": {"bit_exact_fraction": exact / max(tot, 1), "particles": tot}}
     # density passes on the first 16,000,000 final positions
-    P = b.pos[:16_000_000].contiguous()
+    P = b.pos[: a.density_particles].contiguous()
     del b
     torch.cuda.empty_cache()
+    out["density"] = density_part(P, False)
+    return out
+
+
+def density_part(P, profile):
+    """Cubic-spline SPH (h = 0.02, 3-D) at every position and a Scott KDE on
+    the 100^3 grid; with ``profile`` both run once inside
+    cudaProfilerStart/Stop and nothing is returned."""
+    import torch
+
     from jaxtrace_gb300.density import KDEEstimator, SPHDensityEstimator
     sph = SPHDensityEstimator(P, dimensions="3d", smoothing_length=0.02, kernel_type="cubic_spline")
     sph.evaluate(P[:1024])
-    sph_ms = _timed(lambda: sph._density_sum(P), 1)
     kde = KDEEstimator(P, bandwidth_rule="scott")
     kde.evaluate_3d()
+    torch.cuda.synchronize()
+    if profile:
+        torch.cuda.profiler.start()
+        sph._density_sum(P)
+        kde.evaluate_3d()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        return {}
+    sph_ms = _timed(lambda: sph._density_sum(P), 1)
     kde_ms = _timed(kde.evaluate_3d, 1)
-    out["density"] = {"particles": int(P.shape[0]), "sph_ms": sph_ms, "sph_queries_per_s": P.shape[0] / (sph_ms / 1e3),
-                      "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3",
-                      "kde_particles_per_s": P.shape[0] / (kde_ms / 1e3)}
-    return out
+    n = int(P.shape[0])
+    return {"particles": n, "sph_ms": sph_ms, "sph_queries_per_s": n / (sph_ms / 1e3),
+            "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3", "kde_particles_per_s": n / (kde_ms / 1e3)}
 
 
 def workload_name(a):
@@ -546,7 +569,8 @@ def main():
         if a.leg == "adjoint":
             out = adjoint_leg(a, profile=a.profile)
         else:
-            out = {"fem": fem_leg, "batch": batch_leg}[a.leg](a, profile=a.profile)
+            out = {"fem": fem_leg, "batch": batch_leg,
+                   "density": lambda a, profile: batch_leg(a, profile, part="density")}[a.leg](a, profile=a.profile)
         if rank == 0:
             print(json.dumps({"leg": a.leg} | out), flush=True)
         return

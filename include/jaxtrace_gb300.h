@@ -54,6 +54,11 @@ extern "C" {
 #define JT_STORE_F32 0  /* float32 x,y,z                                   */
 #define JT_STORE_BF16 1 /* bfloat16 x,y,z with a per-snapshot float32 scale */
 #define JT_STORE_F16 2  /* float16  x,y,z with a per-snapshot float32 scale */
+/* Pre-blended stage fields of a regular grid (jt_stage_fields), tracking only:
+ * one time level per schedule entry, entry.pair = the field slot. */
+#define JT_STORE_STAGE_F32 3 /* float32 {x,y,z,0} per node (16 B)               */
+#define JT_STORE_STAGE_F16 4 /* float16 yz-quads per node (32 B); entry.wa holds
+                                the field's power-of-two scale                 */
 
 /* grid sampler bounds handling: fields/structured.py:89 */
 #define JT_GRID_CLAMP 0
@@ -318,6 +323,22 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
                        int32_t integrator, int32_t arith, float dt,
                        const float* dt_per_particle, const float* x_in,
                        float* x_out, int32_t n, int32_t* status, void* stream);
+
+/* ---- pre-blended stage fields --------------------------------------------- */
+/* No reference counterpart as an entry point: TimeSeriesField.sample_at_time
+ * (time_series.py:306-389) blends every node at the query time before
+ * StructuredGridSampler interpolates; this does that once per schedule entry
+ * of a time chunk so the tracking kernel gathers one time level.
+ * field: a regular-grid field (F32 or 16-bit pair storage).
+ * entries: device (n) schedule entries (their pair and blend); out_scales:
+ * device (n) power-of-two scales for JT_STORE_STAGE_F16 (NULL for F32).
+ * out: device, n fields of nodes records of out_storage, field j at
+ * out + j * nodes * record_bytes.  The tracking launch then takes a
+ * jt_grid_field with storage = out_storage, pairs = out, n_pairs = n,
+ * pair_stride = nodes and entries whose pair is the slot j (and, for F16,
+ * wa = out_scales[j]). */
+int jt_stage_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
+                    int32_t out_storage, void* out, void* stream);
 
 /* ---- adjoint ------------------------------------------------------------- */
 /* No reference counterpart: JAXTrace has no gradients (no jax.grad on this

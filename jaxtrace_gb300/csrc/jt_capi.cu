@@ -67,6 +67,7 @@ static int check_field(const jt_field* f) {
             if (g->n_pairs < 1 || g->pairs == nullptr) return set_error(JT_ERR_INVALID, "grid field has no snapshot pairs");
             if (g->pair_stride < (int64_t)g->nx * g->ny * g->nz)
                 return set_error(JT_ERR_INVALID, "pair_stride smaller than the node count");
+            if (g->storage == JT_STORE_STAGE_F32 || g->storage == JT_STORE_STAGE_F16) return JT_OK;
             return check_storage(g->storage);
         }
         case JT_FIELD_MESH: {

@@ -68,6 +68,10 @@ __device__ __forceinline__ float sph_w(float r, float h) {
     }
 }
 
+// |d| from d^2 through the hardware reciprocal square root (two instructions
+// instead of the correctly rounded square root; about 2 ulp).
+__device__ __forceinline__ float fast_dist(float d2) { return d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f; }
+
 // The kernels again with the 1/h and sigma of a uniform smoothing length
 // hoisted out of the pair loop (no division per pair).
 template <int DIM, int KERN>
@@ -117,10 +121,24 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
         const float hh = fmaxf(P.h_const, 1e-12f), inv = 1.0f / hh, sigma = sph_sigma<DIM, KERN>(hh);
         const float sup = KERN == JT_SPH_CUBIC ? 2.0f * hh : (KERN == JT_SPH_WENDLAND ? hh : 3.4e38f);
         const float r2lim = fminf(r2max, sup >= 1.8e19f ? r2max : sup * sup);
+        // rows of the cell box whose slab lies beyond the support sphere are
+        // skipped and the rest trimmed in x (with a margin: only whole
+        // cells that cannot hold a term are dropped)
+        const float csy = 1.0f / g.inv_cell[1], csz = DIM == 3 ? 1.0f / g.inv_cell[2] : 0.0f;
         for (int z = z0; z <= z1; ++z) {
+            const float dzr = DIM == 3 ? fmaxf(fmaxf(g.origin[2] + z * csz - qz, qz - (g.origin[2] + (z + 1) * csz)),
+                                               0.0f)
+                                       : 0.0f;
             for (int y = y0; y <= y1; ++y) {
+                const float dyr = fmaxf(fmaxf(g.origin[1] + y * csy - qy, qy - (g.origin[1] + (y + 1) * csy)), 0.0f);
+                const float rem = r2lim - dyr * dyr - dzr * dzr;
+                if (rem < -1e-6f * r2lim) continue;
+                const float rx = sqrtf(fmaxf(rem, 0.0f)) * 1.0001f + 1e-7f;
+                const int xa = max(x0, cell_of(qx - rx, g.origin[0], g.inv_cell[0], lim));
+                const int xb = min(x1, cell_of(qx + rx, g.origin[0], g.inv_cell[0], lim));
+                if (xa > xb) continue;
                 uint32_t b, e;
-                row_range(P.cell_end, x0, x1, y, z, g.bits, b, e);
+                row_range(P.cell_end, xa, xb, y, z, g.bits, b, e);
                 float part = 0.0f;
                 for (uint32_t j = b; j < e; ++j) {
                     const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
@@ -129,7 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
                     const float d2 = dx * dx + dy * dy + dz * dz;
                     if (d2 <= r2lim) {
                         const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
-                        part += m * sph_shape<KERN>(sqrtf(d2) * inv);
+                        part += m * sph_shape<KERN>(fast_dist(d2) * inv);
                     }
                 }
                 acc += (double)part * (double)sigma;
@@ -246,6 +264,98 @@ __global__ void __launch_bounds__(kKdeThreads) k_kde_grid(jt_kde_params P) {
     }
 }
 
+// 3-D KDE with register blocking: a block owns an 8^3 tile of grid points
+// and each of its 128 threads four consecutive z points, so one particle
+// costs a thread two scalar shared loads (x and y factors), one 128-bit
+// shared load (four z factors) and one multiply plus four FMAs, instead of
+// three shared loads per point.  z factors are stored particle-major (32 B
+// per particle).  The tile stays 8^3 so the dilated box of particles each
+// tile visits stays small.
+constexpr int kKbT = 8;
+constexpr int kKbThreads = 128;
+constexpr int kKbChunk = 480;  // 16 rows x 481 x 4 B + 480 x 32 B = 46.2 KB
+static_assert(kKbThreads * 4 == kKbT * kKbT * kKbT, "four z points per thread");
+
+__global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params P) {
+    __shared__ float fab[2 * kKbT][kKbChunk + 1];
+    __shared__ __align__(16) float fc[kKbChunk][kKbT];
+    __shared__ float gcoord[3][kKbT];
+    const int t = threadIdx.x;
+    const int tiles_a = (P.res[0] + kKbT - 1) / kKbT, tiles_b = (P.res[1] + kKbT - 1) / kKbT;
+    const int ta = blockIdx.x % tiles_a, tb = (blockIdx.x / tiles_a) % tiles_b;
+    const int tc = blockIdx.x / (tiles_a * tiles_b);
+    const int b0 = ta * kKbT, b1 = tb * kKbT, b2 = tc * kKbT;
+    const int n0 = min(kKbT, P.res[0] - b0), n1 = min(kKbT, P.res[1] - b1), n2 = min(kKbT, P.res[2] - b2);
+    if (t < 3 * kKbT) {
+        const int a = t / kKbT, k = t % kKbT;
+        const int na = a == 0 ? n0 : (a == 1 ? n1 : n2), ba = a == 0 ? b0 : (a == 1 ? b1 : b2);
+        gcoord[a][k] = k < na ? __ldg(P.axis[a] + ba + k) : 0.0f;
+    }
+    __syncthreads();
+    // thread -> (pa, pb, four z points from pc0); z fastest
+    const int pc0 = 4 * (t % (kKbT / 4));
+    const int pb = (t / (kKbT / 4)) % kKbT;
+    const int pa = t / ((kKbT / 4) * kKbT);
+    const jt_sort_grid& g = P.grid;
+    const int lim = (1 << g.bits) - 1;
+    const int lo0 = cell_of(gcoord[0][0] - P.radius, g.origin[0], g.inv_cell[0], lim);
+    const int hi0 = cell_of(gcoord[0][n0 - 1] + P.radius, g.origin[0], g.inv_cell[0], lim);
+    const int lo1 = cell_of(gcoord[1][0] - P.radius, g.origin[1], g.inv_cell[1], lim);
+    const int hi1 = cell_of(gcoord[1][n1 - 1] + P.radius, g.origin[1], g.inv_cell[1], lim);
+    const int lo2 = cell_of(gcoord[2][0] - P.radius, g.origin[2], g.inv_cell[2], lim);
+    const int hi2 = cell_of(gcoord[2][n2 - 1] + P.radius, g.origin[2], g.inv_cell[2], lim);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int cz = lo2; cz <= hi2; ++cz)
+        for (int cy = lo1; cy <= hi1; ++cy) {
+            uint32_t b, e;
+            row_range(P.cell_end, lo0, hi0, cy, cz, g.bits, b, e);
+            for (uint32_t c0 = b; c0 < e; c0 += kKbChunk) {
+                const int n = (int)min((uint32_t)kKbChunk, e - c0);
+                for (int j = t; j < n; j += kKbThreads) {
+                    const int64_t pj = c0 + j;
+                    const float px = __ldg(P.particles + 3 * pj), py = __ldg(P.particles + 3 * pj + 1);
+                    const float pz = __ldg(P.particles + 3 * pj + 2);
+                    float zf[kKbT];
+#pragma unroll
+                    for (int q = 0; q < kKbT; ++q) {
+                        const float dx = gcoord[0][q] - px, dy = gcoord[1][q] - py, dz = gcoord[2][q] - pz;
+                        fab[q][j] = __expf(-dx * dx * P.half_inv_h2);
+                        fab[kKbT + q][j] = __expf(-dy * dy * P.half_inv_h2);
+                        zf[q] = __expf(-dz * dz * P.half_inv_h2);
+                    }
+#pragma unroll
+                    for (int q = 0; q < kKbT; q += 4)
+                        *reinterpret_cast<float4*>(&fc[j][q]) = make_float4(zf[q], zf[q + 1], zf[q + 2], zf[q + 3]);
+                }
+                __syncthreads();
+                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+                const float* fa = fab[pa];
+                const float* fb = fab[kKbT + pb];
+#pragma unroll 4
+                for (int j = 0; j < n; ++j) {
+                    const float ab = fa[j] * fb[j];
+                    const float4 c = *reinterpret_cast<const float4*>(&fc[j][pc0]);
+                    p0 = fmaf(ab, c.x, p0);
+                    p1 = fmaf(ab, c.y, p1);
+                    p2 = fmaf(ab, c.z, p2);
+                    p3 = fmaf(ab, c.w, p3);
+                }
+                a0 += (double)p0;
+                a1 += (double)p1;
+                a2 += (double)p2;
+                a3 += (double)p3;
+                __syncthreads();
+            }
+        }
+    if (pa < n0 && pb < n1) {
+        const int64_t row = ((int64_t)(b0 + pa) * P.res[1] + (b1 + pb)) * P.res[2] + b2 + pc0;
+        if (pc0 < n2) P.out[row] = a0;
+        if (pc0 + 1 < n2) P.out[row + 1] = a1;
+        if (pc0 + 2 < n2) P.out[row + 2] = a2;
+        if (pc0 + 3 < n2) P.out[row + 3] = a3;
+    }
+}
+
 // KDE at arbitrary points: one point per thread over the cells within radius.
 template <int DIM>
 __global__ void __launch_bounds__(kBlock) k_kde_points(jt_kde_params P, const float* __restrict__ pts, int m,
@@ -329,13 +439,18 @@ extern "C" int jt_kde_grid(const jt_kde_params* p, void* stream) {
         if (p->res[a] < 1 || p->axis[a] == nullptr) return set_error(JT_ERR_INVALID, "grid axis %d is empty", a);
     if (D == 2 && p->res[2] != 1) return set_error(JT_ERR_INVALID, "2-D grids have res[2] == 1");
     if (p->out == nullptr) return set_error(JT_ERR_INVALID, "out is NULL");
-    const int T = D == 3 ? kTile3 : kTile2;
-    int64_t blocks = (int64_t)((p->res[0] + T - 1) / T) * ((p->res[1] + T - 1) / T);
-    if (D == 3) blocks *= (p->res[2] + T - 1) / T;
-    if (blocks > 0x7fffffff) return set_error(JT_ERR_INVALID, "grid too large");
     cudaStream_t st = (cudaStream_t)stream;
-    if (D == 3) k_kde_grid<3><<<(unsigned)blocks, kKdeThreads, 0, st>>>(*p);
-    else k_kde_grid<2><<<(unsigned)blocks, kKdeThreads, 0, st>>>(*p);
+    if (D == 3) {
+        const int64_t blocks = (int64_t)((p->res[0] + kKbT - 1) / kKbT) * ((p->res[1] + kKbT - 1) / kKbT) *
+                               ((p->res[2] + kKbT - 1) / kKbT);
+        if (blocks > 0x7fffffff) return set_error(JT_ERR_INVALID, "grid too large");
+        k_kde_grid3_blocked<<<(unsigned)blocks, kKbThreads, 0, st>>>(*p);
+    } else {
+        const int T = kTile2;
+        const int64_t blocks = (int64_t)((p->res[0] + T - 1) / T) * ((p->res[1] + T - 1) / T);
+        if (blocks > 0x7fffffff) return set_error(JT_ERR_INVALID, "grid too large");
+        k_kde_grid<2><<<(unsigned)blocks, kKdeThreads, 0, st>>>(*p);
+    }
     return cuda_status(cudaGetLastError(), "KDE grid kernel launch");
 }
 

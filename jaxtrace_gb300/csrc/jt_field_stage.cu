@@ -1,0 +1,129 @@
+// Pre-blended stage fields of a regular grid and the tracking kernel that
+// gathers them (StageGridField in jt_grid.cuh).  TimeSeriesField blends
+// every node at the query time and StructuredGridSampler then interpolates
+// (time_series.py:326-367, structured.py:284-349); k_stage_* do the blend
+// once per schedule entry of a time chunk, with the arithmetic the gathered
+// corners would get (blend_cv), so the float32 path stays bit-identical.
+#include <cuda_fp16.h>
+
+#include "jt_grid.cuh"
+#include "jt_internal.h"
+#include "jt_kernels.cuh"
+
+namespace jt {
+
+// float32 pairs -> float4 {x, y, z, 0} per node, one thread per node walking
+// the chunk's entries (a pair record is reloaded only when the pair changes).
+template <bool EXACT>
+__global__ void __launch_bounds__(kBlock) k_stage_f32(jt_grid_field F, const jt_blend* __restrict__ ent, int n,
+                                                       float4* __restrict__ out) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = F.pair_stride;
+    if (node >= N) return;
+    int cur = -1;
+    PairVal pv{};
+    for (int j = 0; j < n; ++j) {
+        const jt_blend e = ent[j];
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        if (pr != cur) {
+            pv = load_pair<JT_STORE_F32>(F.pairs, (int64_t)pr * N + node);
+            cur = pr;
+        }
+        const CV v = blend_cv<EXACT, JT_STORE_F32>(pv, e, splat(e.wa), splat(e.wb), e.form == JT_BLEND_WEIGHTED);
+        out[(int64_t)j * N + node] = make_float4(v.xy.x, v.xy.y, v.z, 0.0f);
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// 16-bit yz-quad pairs -> float16 yz-quads of the blended values divided by
+// the entry's power-of-two scale.
+template <int STORE>
+__global__ void __launch_bounds__(kBlock) k_stage_f16(jt_grid_field F, const jt_blend* __restrict__ ent,
+                                                       const float* __restrict__ scales, int n,
+                                                       uint4* __restrict__ out) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = F.pair_stride;
+    if (node >= N) return;
+    const int64_t part_b = (int64_t)F.n_pairs * N;
+    int cur = -1;
+    PairVal p00{}, p01{}, p10{}, p11{};
+    for (int j = 0; j < n; ++j) {
+        const jt_blend e = ent[j];
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        if (pr != cur) {
+            load_quad<STORE>(F.pairs, part_b, (int64_t)pr * N + node, p00, p01, p10, p11);
+            cur = pr;
+        }
+        const bool w = e.form == JT_BLEND_WEIGHTED;
+        const float2 WA = splat(e.wa), WB = splat(e.wb);
+        const CV c00 = blend_cv<false, STORE>(p00, e, WA, WB, w), c01 = blend_cv<false, STORE>(p01, e, WA, WB, w);
+        const CV c10 = blend_cv<false, STORE>(p10, e, WA, WB, w), c11 = blend_cv<false, STORE>(p11, e, WA, WB, w);
+        const float inv = 1.0f / __ldg(scales + j);  // a power of two: exact
+        uint4 a, b;
+        a.x = pack_h2(c00.xy.x * inv, c00.xy.y * inv);
+        a.y = pack_h2(c01.xy.x * inv, c01.xy.y * inv);
+        a.z = pack_h2(c10.xy.x * inv, c10.xy.y * inv);
+        a.w = pack_h2(c11.xy.x * inv, c11.xy.y * inv);
+        b.x = pack_h2(c00.z * inv, c01.z * inv);
+        b.y = pack_h2(c10.z * inv, c11.z * inv);
+        b.z = 0u;
+        b.w = 0u;
+        uint4* o = out + 2 * ((int64_t)j * N + node);
+        o[0] = a;
+        o[1] = b;
+    }
+}
+
+typedef Launcher<StageGridField, jt_grid_field, int> StageL;
+
+int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
+    const bool exact = p.arith == JT_ARITH_EXACT;
+    cudaError_t err;
+    if (f.storage == JT_STORE_STAGE_F32) {
+        err = exact ? StageL::track_s<true, JT_STORE_STAGE_F32>(f, 0, b, p, s)
+                    : StageL::track_s<false, JT_STORE_STAGE_F32>(f, 0, b, p, s);
+    } else {
+        if (exact) return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
+        err = StageL::track_s<false, JT_STORE_STAGE_F16>(f, 0, b, p, s);
+    }
+    return cuda_status(err, "tracking kernel launch");
+}
+
+}  // namespace jt
+
+using namespace jt;
+
+extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
+                               int32_t out_storage, void* out, void* stream) {
+    if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
+        return set_error(JT_ERR_INVALID, "stage fields need a regular-grid field");
+    const jt_grid_field& F = *field->grid;
+    if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
+    if (n == 0) return JT_OK;
+    if (entries == nullptr || out == nullptr) return set_error(JT_ERR_INVALID, "entries and out are required");
+    if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshot pairs");
+    const int64_t N = (int64_t)F.nx * F.ny * F.nz;
+    if (F.pair_stride != N) return set_error(JT_ERR_INVALID, "pair_stride must equal the node count");
+    const unsigned g = grid_blocks(N);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (out_storage == JT_STORE_STAGE_F32) {
+        if (F.storage != JT_STORE_F32)
+            return set_error(JT_ERR_UNSUPPORTED, "float32 stage fields come from float32 snapshots");
+        k_stage_f32<true><<<g, kBlock, 0, s>>>(F, entries, n, reinterpret_cast<float4*>(out));
+    } else if (out_storage == JT_STORE_STAGE_F16) {
+        if (out_scales == nullptr) return set_error(JT_ERR_INVALID, "float16 stage fields need out_scales");
+        if (F.storage == JT_STORE_BF16)
+            k_stage_f16<JT_STORE_BF16><<<g, kBlock, 0, s>>>(F, entries, out_scales, n, reinterpret_cast<uint4*>(out));
+        else if (F.storage == JT_STORE_F16)
+            k_stage_f16<JT_STORE_F16><<<g, kBlock, 0, s>>>(F, entries, out_scales, n, reinterpret_cast<uint4*>(out));
+        else
+            return set_error(JT_ERR_UNSUPPORTED, "float16 stage fields come from 16-bit snapshots");
+    } else {
+        return set_error(JT_ERR_INVALID, "out_storage must be JT_STORE_STAGE_F32 or JT_STORE_STAGE_F16");
+    }
+    return cuda_status(cudaGetLastError(), "stage field launch");
+}

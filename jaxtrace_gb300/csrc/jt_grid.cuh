@@ -65,6 +65,31 @@ __device__ __forceinline__ CV blend_cv(const PairVal& p, const jt_blend& e, floa
     return CV{make_float2(v.x, v.y), v.z};
 }
 
+// structured.py:334-342: lerp in x, then y, then z; every product rounded
+// before its sum in the exact mode.  x,y travel as packed pairs; z pairs up
+// across corners: (c00z, c01z) and (c10z, c11z), then (c0z, c1z).
+template <bool EXACT>
+__device__ __forceinline__ V3 trilinear(const CV& v000, const CV& v100, const CV& v010, const CV& v110,
+                                        const CV& v001, const CV& v101, const CV& v011, const CV& v111, float wx,
+                                        float wy, float wz) {
+    typedef Ar<EXACT> A;
+    const float ox = A::sub(1.0f, wx), oy = A::sub(1.0f, wy), oz = A::sub(1.0f, wz);
+    const float2 OX = splat(ox), WX = splat(wx), OY = splat(oy), WY = splat(wy), OZ = splat(oz), WZ = splat(wz);
+    const float2 c00 = dot2p<EXACT>(v000.xy, OX, v100.xy, WX);
+    const float2 c10 = dot2p<EXACT>(v010.xy, OX, v110.xy, WX);
+    const float2 c01 = dot2p<EXACT>(v001.xy, OX, v101.xy, WX);
+    const float2 c11 = dot2p<EXACT>(v011.xy, OX, v111.xy, WX);
+    const float2 c0 = dot2p<EXACT>(c00, OY, c10, WY);
+    const float2 c1 = dot2p<EXACT>(c01, OY, c11, WY);
+    const float2 rxy = dot2p<EXACT>(c0, OZ, c1, WZ);
+    const float2 cz0 = dot2p<EXACT>(make_float2(v000.z, v001.z), OX, make_float2(v100.z, v101.z), WX);
+    const float2 cz1 = dot2p<EXACT>(make_float2(v010.z, v011.z), OX, make_float2(v110.z, v111.z), WX);
+    const float2 cz = dot2p<EXACT>(cz0, OY, cz1, WY);
+    return V3{rxy.x, rxy.y, A::dot2(cz.x, oz, cz.y, wz)};
+}
+
+__device__ __forceinline__ float2 h2f2(uint32_t w) { return __half22float2(*reinterpret_cast<const __half2*>(&w)); }
+
 template <bool EXACT, int STORE>
 struct GridField {
     jt_grid_field F;
@@ -112,22 +137,72 @@ struct GridField {
         const CV v001 = blend_cv<EXACT, STORE>(p001, e, WA, WB, wgt), v101 = blend_cv<EXACT, STORE>(p101, e, WA, WB, wgt);
         const CV v011 = blend_cv<EXACT, STORE>(p011, e, WA, WB, wgt), v111 = blend_cv<EXACT, STORE>(p111, e, WA, WB, wgt);
 
-        // structured.py:334-342: lerp in x, then y, then z; every product
-        // rounded before its sum in the exact mode
-        const float ox = A::sub(1.0f, wx), oy = A::sub(1.0f, wy), oz = A::sub(1.0f, wz);
-        const float2 OX = splat(ox), WX = splat(wx), OY = splat(oy), WY = splat(wy), OZ = splat(oz), WZ = splat(wz);
-        const float2 c00 = dot2p<EXACT>(v000.xy, OX, v100.xy, WX);
-        const float2 c10 = dot2p<EXACT>(v010.xy, OX, v110.xy, WX);
-        const float2 c01 = dot2p<EXACT>(v001.xy, OX, v101.xy, WX);
-        const float2 c11 = dot2p<EXACT>(v011.xy, OX, v111.xy, WX);
-        const float2 c0 = dot2p<EXACT>(c00, OY, c10, WY);
-        const float2 c1 = dot2p<EXACT>(c01, OY, c11, WY);
-        const float2 rxy = dot2p<EXACT>(c0, OZ, c1, WZ);
-        // z: (c00z, c01z) and (c10z, c11z) as pairs, then (c0z, c1z)
-        const float2 cz0 = dot2p<EXACT>(make_float2(v000.z, v001.z), OX, make_float2(v100.z, v101.z), WX);
-        const float2 cz1 = dot2p<EXACT>(make_float2(v010.z, v011.z), OX, make_float2(v110.z, v111.z), WX);
-        const float2 cz = dot2p<EXACT>(cz0, OY, cz1, WY);
-        V3 r{rxy.x, rxy.y, A::dot2(cz.x, oz, cz.y, wz)};
+        V3 r = trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
+        if (F.bounds_mode == JT_GRID_ZERO || F.bounds_mode == JT_GRID_NAN) {
+            if (!(vx && vy && vz)) {
+                const float o = F.bounds_mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);
+                r = V3{o, o, o};
+            }
+        }
+        return r;
+    }
+};
+
+// Pre-blended stage field of a time chunk: one time level per schedule entry
+// (slot = e.pair), blended per node ahead of the tracking launch exactly as
+// TimeSeriesField.sample_at_time blends every node (time_series.py:326-367)
+// before StructuredGridSampler interpolates -- the reference's own order, so
+// the exact mode is bit-identical to blending the gathered corners.
+//   JT_STORE_STAGE_F32: float4 {x, y, z, 0} per node (16 B);
+//   JT_STORE_STAGE_F16: float16 yz-quads per node (32 B): words 0-3 the
+//     (x, y) of nodes (j,k), (j,k1), (j1,k), (j1,k1); words 4-5 their z in
+//     pairs; values divided by the power-of-two scale carried in e.wa.
+template <bool EXACT, int OUT>
+struct StageGridField {
+    jt_grid_field F;
+
+    static StageGridField create(const jt_grid_field& d, int) { return StageGridField{d}; }
+
+    __device__ __forceinline__ V3 operator()(const V3& p, const jt_blend& e, int& flags) const {
+        int i0, i1, j0, j1, k0, k1;
+        float wx, wy, wz;
+        bool vx, vy, vz;
+        grid_axis<EXACT>(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode, F.valid_hi[0], i0,
+                         i1, wx, vx, flags);
+        grid_axis<EXACT>(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode, F.valid_hi[1], j0,
+                         j1, wy, vy, flags);
+        grid_axis<EXACT>(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode, F.valid_hi[2], k0,
+                         k1, wz, vz, flags);
+        const int slot = min(max(e.pair, 0), F.n_pairs - 1);
+        const int64_t base = (int64_t)slot * F.pair_stride;
+        const int ny = F.ny, nz = F.nz;
+        const int r00 = (i0 * ny + j0) * nz, r10 = (i1 * ny + j0) * nz;
+        CV v000, v100, v010, v110, v001, v101, v011, v111;
+        V3 r;
+        if (OUT == JT_STORE_STAGE_F32) {
+            const int r01 = (i0 * ny + j1) * nz, r11 = (i1 * ny + j1) * nz;
+            const float4* b4 = reinterpret_cast<const float4*>(F.pairs) + base;
+            const float4 a000 = __ldg(b4 + r00 + k0), a100 = __ldg(b4 + r10 + k0);
+            const float4 a010 = __ldg(b4 + r01 + k0), a110 = __ldg(b4 + r11 + k0);
+            const float4 a001 = __ldg(b4 + r00 + k1), a101 = __ldg(b4 + r10 + k1);
+            const float4 a011 = __ldg(b4 + r01 + k1), a111 = __ldg(b4 + r11 + k1);
+            v000 = CV{make_float2(a000.x, a000.y), a000.z}; v100 = CV{make_float2(a100.x, a100.y), a100.z};
+            v010 = CV{make_float2(a010.x, a010.y), a010.z}; v110 = CV{make_float2(a110.x, a110.y), a110.z};
+            v001 = CV{make_float2(a001.x, a001.y), a001.z}; v101 = CV{make_float2(a101.x, a101.y), a101.z};
+            v011 = CV{make_float2(a011.x, a011.y), a011.z}; v111 = CV{make_float2(a111.x, a111.y), a111.z};
+            r = trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
+        } else {
+            uint32_t q0[8], q1[8];
+            ldg256(reinterpret_cast<const uint4*>(F.pairs) + 2 * (base + r00 + k0), q0);
+            ldg256(reinterpret_cast<const uint4*>(F.pairs) + 2 * (base + r10 + k0), q1);
+            const float2 z0a = h2f2(q0[4]), z0b = h2f2(q0[5]), z1a = h2f2(q1[4]), z1b = h2f2(q1[5]);
+            v000 = CV{h2f2(q0[0]), z0a.x}; v001 = CV{h2f2(q0[1]), z0a.y};
+            v010 = CV{h2f2(q0[2]), z0b.x}; v011 = CV{h2f2(q0[3]), z0b.y};
+            v100 = CV{h2f2(q1[0]), z1a.x}; v101 = CV{h2f2(q1[1]), z1a.y};
+            v110 = CV{h2f2(q1[2]), z1b.x}; v111 = CV{h2f2(q1[3]), z1b.y};
+            r = trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
+            r = V3{r.x * e.wa, r.y * e.wa, r.z * e.wa};
+        }
         if (F.bounds_mode == JT_GRID_ZERO || F.bounds_mode == JT_GRID_NAN) {
             if (!(vx && vy && vz)) {
                 const float o = F.bounds_mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);

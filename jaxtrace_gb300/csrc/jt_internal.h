@@ -33,6 +33,8 @@ int nearest_step(const jt_nearest_field& f, int arith, const StageBlends& sb, in
 int nearest_sample(const jt_nearest_field& f, int arith, const jt_blend& e, const float* pos, float* out,
                    int m, int32_t* status, cudaStream_t s);
 
+int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+
 int fem_track(const jt_fem_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
 int fem_step(const jt_fem_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
              const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);

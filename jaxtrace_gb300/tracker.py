@@ -57,6 +57,10 @@ class TrackerOptions:
                        short sample of the run (``autotune.Autotuner``)
     cuda_graph         capture the whole tracking pass of ``track_ensembles``
                        in a CUDA graph and replay it
+    stage_fields       regular grids: blend every node once per stage time
+                       of a chunk of ``stage_chunk`` steps before the tracking
+                       launch, so it gathers one time level (the reference's
+                       own order of operations; float32 stays bit-identical)
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -87,6 +91,8 @@ class TrackerOptions:
     block_size: int = 0
     autotune: bool = False
     cuda_graph: bool = False
+    stage_fields: bool = True
+    stage_chunk: int = 32
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
         """tracker.py:142-153."""
@@ -416,6 +422,11 @@ class _Engine:
         if ens is not None:       # (device offsets (E+1,) int32, E, schedule entries per ensemble)
             self.ens = ens
             self.p.ens_offsets, self.p.n_ens, self.p.schedule_stride = ens[0].data_ptr(), ens[1], ens[2]
+        self.stage = None
+        if ens is None and tracker.options.stage_fields and n_steps > 0 and self.n > 0:
+            from .fields import StructuredTimeSeriesField
+            if isinstance(tracker._field, StructuredTimeSeriesField):
+                self.stage = _StageFields(tracker._field, sched_dev, n_steps, int(tracker.options.stage_chunk))
 
     def _sort(self, first=False):
         src_pos = self.out if first else self.pos
@@ -444,6 +455,15 @@ class _Engine:
                 if s > 0 and s % self.sort_every == 0:
                     self._sort()
                 stop = min(e, (s // self.sort_every + 1) * self.sort_every)
+            staged = self.stage is not None and not (rec is not None and rec[1] is not None)
+            if staged:
+                stop = min(stop, s + self.stage.chunk)
+                self.kernels += self.stage.prepare(s, stop)
+                field_c = self.stage.field_c
+                p.schedule = self.stage.sched.data_ptr()
+            else:
+                field_c = self.field_c
+                p.schedule = self.sched.data_ptr()
             p.pos = self.pos.data_ptr()
             p.comp = self.comp.data_ptr() if self.comp is not None else None
             p.ids = self.ids.data_ptr() if self.ids is not None else None
@@ -459,7 +479,7 @@ class _Engine:
                 import torch
                 ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                 ev[0].record()
-            L.check(self.lib.jt_track(C.byref(self.field_c), C.byref(self.bc_c), C.byref(p), self.stream))
+            L.check(self.lib.jt_track(C.byref(field_c), C.byref(self.bc_c), C.byref(p), self.stream))
             if self.timers is not None:
                 ev[1].record()
                 self.timers.append(ev)
@@ -579,6 +599,90 @@ class EnsembleBatch:
         out = self.pos.cpu().numpy()
         self.check_status()
         return [out[a:b] for a, b in zip(self.offsets[:-1], self.offsets[1:])]
+
+
+class _StageFields:
+    """Pre-blended stage fields of a regular-grid run (jt_stage_fields).
+
+    Step s, stage k (0: t, 1: t + h/2, 2: t + h) reads field slot
+    3 * (s mod chunk) + k, so a launch of at most ``chunk`` steps finds every
+    step's fields in place after ``prepare``.  Float32 snapshots give float32
+    node records blended with the exact arithmetic; 16-bit snapshots give
+    float16 yz-quads divided by a power-of-two bound of the blend.
+    """
+
+    def __init__(self, field, sched_dev, n_steps: int, chunk: int):
+        import torch
+        from .schedule import BLEND_DTYPE
+        self.lib = L.load()
+        self.chunk = max(1, min(int(chunk), n_steps))
+        host = np.ascontiguousarray(sched_dev.cpu().numpy()).view(BLEND_DTYPE).reshape(-1)
+        n_ent = 4 * n_steps
+        host = host[:n_ent].copy()
+        src = host.reshape(n_steps, 4)[:, :3].reshape(-1).copy()          # 3 entries per step
+        self.f32 = field._storage == L.JT_STORE_F32
+        self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
+        scales = np.ones(len(src), dtype=F32)
+        if not self.f32:
+            scales = _stage_scales(src)
+        # the tracking schedule: pair -> slot, weights -> the slot's scale
+        stage = host.copy().reshape(n_steps, 4)
+        steps = np.arange(n_steps)
+        for k in range(3):
+            stage[:, k]["pair"] = 3 * (steps % self.chunk) + k
+            stage[:, k]["form"] = L.JT_BLEND_WEIGHTED
+            stage[:, k]["wa"] = scales.reshape(n_steps, 3)[:, k]
+            stage[:, k]["wb"] = 0.0
+        dev = sched_dev.device
+        self.sched = torch.from_numpy(stage.reshape(-1).view(np.int32).reshape(-1, 8).copy()).to(dev)
+        self.src = torch.from_numpy(src.view(np.int32).reshape(-1, 8).copy()).to(dev)
+        self.scales = torch.from_numpy(scales).to(dev)
+        field._device()
+        g0 = field._cgrid
+        nodes = int(g0.pair_stride)
+        rec = 4 if self.f32 else 8                                           # float32 words per node
+        self.buf = torch.empty(3 * self.chunk * nodes * rec, dtype=torch.float32, device=dev)
+        self.nodes, self.rec = nodes, rec
+        g = L.GridField()
+        C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
+        g.storage = self.out_storage
+        g.n_pairs = 3 * self.chunk
+        g.pair_stride = nodes
+        g.pairs = self.buf.data_ptr()
+        self.grid = g
+        self.field_c = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
+        self.src_field = field.jt_field()
+
+    def prepare(self, s: int, stop: int) -> int:
+        """Blend the fields of steps [s, stop) into their slots; returns the
+        number of kernels launched."""
+        launched = 0
+        stream = L.stream_ptr()
+        while s < stop:
+            first = s % self.chunk
+            run = min(stop - s, self.chunk - first)
+            ent = self.src.data_ptr() + 3 * s * 32
+            sc = self.scales.data_ptr() + 3 * s * 4
+            out = self.buf.data_ptr() + 3 * first * self.nodes * self.rec * 4
+            L.check(self.lib.jt_stage_fields(C.byref(self.src_field), C.c_void_p(ent),
+                                             C.c_void_p(None if self.f32 else sc), 3 * run, self.out_storage,
+                                             C.c_void_p(out), stream))
+            launched += 1
+            s += run
+        return launched
+
+
+def _stage_scales(src) -> np.ndarray:
+    """Power-of-two bounds of |blend| on raw 16-bit values (|raw| <= 1):
+    |wa| + |wb| for the folded forms, (sa + sb)(1 + |w|) for the lerps."""
+    wa = np.abs(src["wa"].astype(np.float64))
+    wb = np.abs(src["wb"].astype(np.float64))
+    sa = np.abs(src["sa"].astype(np.float64))
+    sb = np.abs(src["sb"].astype(np.float64))
+    lerp = (src["form"] == L.JT_BLEND_LERP_FWD) | (src["form"] == L.JT_BLEND_LERP_BWD)
+    bound = np.where(lerp, (sa + sb) * (1.0 + wb), wa + wb)
+    bound = np.where(bound > 0, bound, 1.0)
+    return np.exp2(np.ceil(np.log2(bound))).astype(F32)
 
 
 def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:
