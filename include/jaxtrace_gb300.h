@@ -450,8 +450,10 @@ typedef struct {
     float h_const;             /* smoothing length when h == NULL            */
     jt_sort_grid grid;         /* cell grid of the particle cell list        */
     int32_t reach[3];          /* cells searched on each side, per axis      */
-    int32_t pad;
-    const float* particles;    /* device (N,3) in cell order                 */
+    int32_t packed;            /* 0: particles (N,3) and masses apart; 1:
+                                  particles (N,4) {x,y,z,mass} in one 16-byte
+                                  record (masses then unused)                */
+    const float* particles;    /* device (N,3) or (N,4) in cell order        */
     const float* masses;       /* device (N) in cell order, or NULL (unit masses) */
     const float* h;            /* device (N) in cell order, or NULL (h_const) */
     const uint32_t* cell_end;  /* device, from jt_cell_list                  */

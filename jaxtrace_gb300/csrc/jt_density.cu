@@ -86,16 +86,14 @@ __device__ __forceinline__ float sph_sigma(float hh) {
 template <int KERN>
 __device__ __forceinline__ float sph_shape(float q) {
     if (KERN == JT_SPH_CUBIC) {
-        if (q <= 1.0f) return 1.0f - 1.5f * q * q + 0.75f * q * q * q;
-        if (q <= 2.0f) {
-            const float t = 2.0f - q;
-            return 0.25f * t * t * t;
-        }
-        return 0.0f;
+        const float t = fmaxf(2.0f - q, 0.0f);
+        const float outer = 0.25f * t * t * t;                        // 1 < q <= 2
+        const float inner = fmaf(q * q, fmaf(0.75f, q, -1.5f), 1.0f);  // q <= 1
+        return q <= 1.0f ? inner : outer;
     } else if (KERN == JT_SPH_WENDLAND) {
         const float t = fmaxf(1.0f - q, 0.0f);
         const float t2 = t * t;
-        return t2 * t2 * (1.0f + 4.0f * q);
+        return t2 * t2 * fmaf(4.0f, q, 1.0f);
     }
     return expf(-q * q);
 }
@@ -140,14 +138,27 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
                 uint32_t b, e;
                 row_range(P.cell_end, xa, xb, y, z, g.bits, b, e);
                 float part = 0.0f;
-                for (uint32_t j = b; j < e; ++j) {
-                    const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
-                    const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
-                    const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
-                    const float d2 = dx * dx + dy * dy + dz * dz;
-                    if (d2 <= r2lim) {
-                        const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
-                        part += m * sph_shape<KERN>(fast_dist(d2) * inv);
+                if (P.packed) {
+                    // {x, y, z, m} records; FMA-contracted distance (no parity
+                    // constraint on the density passes)
+                    const float4* p4 = reinterpret_cast<const float4*>(P.particles);
+#pragma unroll 4
+                    for (uint32_t j = b; j < e; ++j) {
+                        const float4 r = __ldg(p4 + j);
+                        const float dx = r.x - qx, dy = r.y - qy, dz = DIM == 3 ? r.z - qz : 0.0f;
+                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        if (d2 <= r2lim) part = fmaf(r.w, sph_shape<KERN>(fast_dist(d2) * inv), part);
+                    }
+                } else {
+                    for (uint32_t j = b; j < e; ++j) {
+                        const float dx = __ldg(P.particles + 3 * (int64_t)j) - qx;
+                        const float dy = __ldg(P.particles + 3 * (int64_t)j + 1) - qy;
+                        const float dz = DIM == 3 ? __ldg(P.particles + 3 * (int64_t)j + 2) - qz : 0.0f;
+                        const float d2 = dx * dx + dy * dy + dz * dz;
+                        if (d2 <= r2lim) {
+                            const float m = P.masses != nullptr ? __ldg(P.masses + j) : 1.0f;
+                            part += m * sph_shape<KERN>(fast_dist(d2) * inv);
+                        }
                     }
                 }
                 acc += (double)part * (double)sigma;

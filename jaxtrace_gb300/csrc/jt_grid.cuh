@@ -156,9 +156,18 @@ struct GridField {
 //   JT_STORE_STAGE_F32: float4 {x, y, z, 0} per node (16 B);
 //   JT_STORE_STAGE_F16: float16 yz-quads per node (32 B): words 0-3 the
 //     (x, y) of nodes (j,k), (j,k1), (j1,k), (j1,k1); words 4-5 their z in
-//     pairs; values divided by the power-of-two scale carried in e.wa.
+//     pairs; values divided by the power-of-two scale carried in e.wa.  Two
+//     256-bit loads per evaluation measured faster than eight 64-bit loads of
+//     float16 node records, although those fit L2 and the quads do not.
+#ifndef JT_STAGE16_MIN_BLOCKS
+#define JT_STAGE16_MIN_BLOCKS 6
+#endif
+
 template <bool EXACT, int OUT>
 struct StageGridField {
+    // float16 quads fit 6 blocks of 256 (38 registers, no spills), which
+    // hides more of the stage fields' HBM latency; float32 records take 64 at 4
+    static constexpr int kMinBlocks = OUT == JT_STORE_STAGE_F16 ? JT_STAGE16_MIN_BLOCKS : 4;
     jt_grid_field F;
 
     static StageGridField create(const jt_grid_field& d, int) { return StageGridField{d}; }

@@ -17,8 +17,20 @@ constexpr int kBlock = 256;
 #endif
 
 // Persistent tracking: tracker.py:236-242 (scan body) over [step_begin, step_end).
+// Blocks per SM the tracking kernel is compiled for: a field type may name its
+// own (kMinBlocks, e.g. a lighter gather needs fewer registers), otherwise
+// JT_TRACK_MIN_BLOCKS.
+template <class F, class = void>
+struct MinBlocksOf {
+    static constexpr int value = JT_TRACK_MIN_BLOCKS;
+};
+template <class F>
+struct MinBlocksOf<F, decltype(void(F::kMinBlocks))> {
+    static constexpr int value = F::kMinBlocks;
+};
+
 template <bool EXACT, int INTEG, class Field>
-__global__ void __launch_bounds__(kBlock, JT_TRACK_MIN_BLOCKS) k_track(Field f, jt_boundary B, jt_track_params P) {
+__global__ void __launch_bounds__(kBlock, MinBlocksOf<Field>::value) k_track(Field f, jt_boundary B, jt_track_params P) {
     track_body<EXACT, INTEG>(f, B, P);
 }
 

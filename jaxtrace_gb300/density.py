@@ -409,8 +409,17 @@ class SPHDensityEstimator:
         p.h_const = self._uniform_h if self._uniform_h is not None else 0.0
         p.grid = cl.grid
         p.reach[:] = cl.reach(search)
-        p.particles = cl.sorted.data_ptr()
-        p.masses = m_sorted.data_ptr() if m_sorted is not None else None
+        p.masses = None
+        if h_sorted is None:
+            # uniform h: {x, y, z, mass} records, one 16-byte load per candidate
+            P4 = torch.cat([cl.sorted, m_sorted[:, None] if m_sorted is not None else
+                            torch.ones((cl.n, 1), dtype=torch.float32, device="cuda")], dim=1).contiguous()
+            p.packed = 1
+            p.particles = P4.data_ptr()
+        else:
+            p.packed = 0
+            p.particles = cl.sorted.data_ptr()
+            p.masses = m_sorted.data_ptr() if m_sorted is not None else None
         p.h = h_sorted.data_ptr() if h_sorted is not None else None
         p.cell_end = cl.cell_end.data_ptr()
         p.queries = qcl.sorted.data_ptr()
