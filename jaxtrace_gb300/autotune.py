@@ -21,8 +21,6 @@ import os
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Tuple
 
-import numpy as np
-
 BLOCK_SIZES = (128, 256, 64)
 SORT_EVERY = (0, 20, 50, 100)
 SORT_BITS = (7, 6, 5)

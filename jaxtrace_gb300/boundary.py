@@ -8,8 +8,7 @@ kernel's per-step epilogue.
 from __future__ import annotations
 
 import ctypes as C
-import math
-from typing import Dict, Optional, Union
+from typing import Dict, Optional
 
 import numpy as np
 

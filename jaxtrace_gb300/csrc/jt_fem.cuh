@@ -15,6 +15,7 @@ namespace jt {
 
 template <bool EXACT, int STORE>
 struct FemField {
+    static constexpr int kMinBlocks = JT_MESH_MIN_BLOCKS;
     jt_fem_field F;
     float h_min;  // smallest nearest-node cell edge (ring-stop bound)
 

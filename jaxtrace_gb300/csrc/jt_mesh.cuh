@@ -65,8 +65,15 @@ __device__ __forceinline__ V3 p1_combine(const float4& b, const V3& n0, const V3
               A::add(A::add(A::add(A::mul(b.x, n0.z), A::mul(b.y, n1.z)), A::mul(b.z, n2.z)), A::mul(b.w, n3.z))};
 }
 
+#ifndef JT_MESH_MIN_BLOCKS
+#define JT_MESH_MIN_BLOCKS 4
+#endif
+
 template <bool EXACT, int STORE>
 struct MeshField {
+    // the dependent gather chain is latency-bound: 4 blocks of 256 (64
+    // registers, no spills) keep more warps in flight than the default 3
+    static constexpr int kMinBlocks = JT_MESH_MIN_BLOCKS;
     jt_mesh_field F;
 
     static MeshField create(const jt_mesh_field& d, int) { return MeshField{d}; }

@@ -36,18 +36,6 @@ def _entry(pair, form, wa, wb, sa=1.0, sb=1.0):
     return (int(pair), int(form), F32(wa), F32(wb), F32(sa), F32(sb), 0, 0)
 
 
-def _pair_for(il: int, ir: int, n_snap: int):
-    """Snapshot pair holding snapshots il and ir, and whether il is its A slot."""
-    if n_snap == 1:
-        return 0, True
-    if ir == il + 1:
-        return il, True
-    # il == ir (clamped at an end): the pair that contains il
-    if il >= n_snap - 1:
-        return n_snap - 2, False
-    return il, True
-
-
 def blend_numpy(times: np.ndarray, t, interpolation: str = "linear", extrapolation: str = "constant"):
     """Blend entry for ``TimeSeriesField.sample_at_time(t)`` on the NumPy path.
 

@@ -9,8 +9,6 @@ written straight into a device trajectory slab that streams to the host.
 from __future__ import annotations
 
 import ctypes as C
-import math
-import warnings
 from dataclasses import dataclass, field as dc_field
 from typing import Any, Callable, Dict, List, Optional, Tuple
 
