@@ -361,6 +361,10 @@ typedef struct {
                                       jt_adjoint_workspace_bytes(nodes, steps) bytes when
                                       grad is set; zeroed by the call           */
     int64_t work_bytes;
+    const float* stage;            /* device float32 stage fields of the segment
+                                      (jt_stage_fields with JT_STORE_STAGE_F32 over its
+                                      3 * steps schedule entries, slot 3*s + k), or NULL to
+                                      blend the pair records                     */
 } jt_adjoint_params;
 
 /* Workspace of one backward segment of n_steps steps over n_nodes grid

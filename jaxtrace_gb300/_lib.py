@@ -104,7 +104,7 @@ class SortGrid(C.Structure):
 class AdjointParams(C.Structure):
     _fields_ = [("n_particles", i32), ("step_begin", i32), ("step_end", i32), ("dt", f32), ("dt_half", f32),
                 ("dt_sixth", f32), ("pad", i32), ("schedule", vp), ("ckpt", vp), ("lambda_", vp), ("grad", vp),
-                ("work", vp), ("work_bytes", i64)]
+                ("work", vp), ("work_bytes", i64), ("stage", vp)]
 
 
 JT_ORDER_MORTON, JT_ORDER_LINEAR = 0, 1

@@ -43,7 +43,8 @@ class AdjointRK4:
 
     def __init__(self, times, grid_x, grid_y, grid_z, bounds_handling: str = "periodic",
                  boundary: Optional[BoundaryDescriptor] = None, checkpoint_every: int = 50,
-                 time_semantics: str = "numpy", sort_bits: int = 6, sort_min_particles: int = 1 << 16):
+                 time_semantics: str = "numpy", sort_bits: int = 6, sort_min_particles: int = 1 << 16,
+                 stage_fields: bool = True):
         from .fields import StructuredTimeSeriesField
         self.times = np.asarray(times, dtype=F32)
         self.gx, self.gy, self.gz = (np.asarray(g, dtype=F32) for g in (grid_x, grid_y, grid_z))
@@ -65,6 +66,9 @@ class AdjointRK4:
             raise ValueError("sort_bits must be in 0..7")
         self.sort_bits = int(sort_bits)
         self.sort_min_particles = int(sort_min_particles)
+        # the backward gathers pre-blended float32 stage fields of each segment
+        # (bit-identical recompute, half the bytes of the pair records)
+        self.stage_fields = bool(stage_fields)
 
     def _field(self, pairs):
         t = self._tmpl
@@ -190,9 +194,20 @@ def _make_function():
                 work = torch.empty(wb // 4, dtype=torch.float32, device=lam.device)
                 a.work, a.work_bytes = work.data_ptr(), wb
             stream = L.stream_ptr()
+            stage = src = None
+            if solver.stage_fields:
+                # 3 schedule entries (stage times) per step, and room for one segment's fields
+                src = ctx.sched.view(-1, 4, 8)[:, :3].contiguous().view(-1, 8)
+                stage = torch.empty((3 * k * solver.nodes, 4), dtype=torch.float32, device=lam.device)
             for sgi in reversed(range(n_seg)):
                 a.step_begin, a.step_end = sgi * k, min((sgi + 1) * k, ctx.n_steps)
                 a.ckpt = ckpt[sgi].data_ptr()
+                if stage is not None:
+                    ns = a.step_end - a.step_begin
+                    L.check(lib.jt_stage_fields(C.byref(field), C.c_void_p(src.data_ptr() + 3 * a.step_begin * 32),
+                                                None, 3 * ns, L.JT_STORE_STAGE_F32, C.c_void_p(stage.data_ptr()),
+                                                stream))
+                    a.stage = stage.data_ptr()
                 if ids_all is not None:
                     idx = ids_all[sgi].long()
                     lam_s = lam.index_select(0, idx).contiguous()    # slot order of the segment

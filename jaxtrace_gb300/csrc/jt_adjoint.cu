@@ -96,10 +96,16 @@ __device__ __forceinline__ void scatter(const jt_grid_field& F, const Ax3& a, co
 // of the same stage time in the same cell), w'_c * g' is added in the same
 // atomic.  The blend coefficients of A and B are applied when the
 // accumulators are folded into the pair-record gradient.
+//
+// STAGE: the blended corner values come from a pre-blended float32 stage
+// field (stage + slot * nodes, one float4 per node) instead of the pair
+// records: half the bytes, no blend arithmetic.
+template <bool STAGE>
 __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const Ax3& a, const jt_blend& e, const V3& g,
-                                       float4* __restrict__ acc, const Ax3* other, const V3& g_other) {
-    float ca, cb;
-    blend_coefs(e, ca, cb);
+                                       float4* __restrict__ acc, const Ax3* other, const V3& g_other,
+                                       const float4* __restrict__ stage) {
+    float ca = 0.f, cb = 0.f;
+    if (!STAGE) blend_coefs(e, ca, cb);
     const int pr = min(max(e.pair, 0), F.n_pairs - 1);
     const int64_t base = (int64_t)pr * F.pair_stride;
     V3 jtg{0.f, 0.f, 0.f};
@@ -110,10 +116,17 @@ __device__ __forceinline__ V3 grid_vjp(const jt_grid_field& F, const Ax3& a, con
         const float wx = bx ? a.x.w : 1.0f - a.x.w, wy = by ? a.y.w : 1.0f - a.y.w;
         const float wz = bz ? a.z.w : 1.0f - a.z.w;
         const int64_t node = (int64_t)(i * F.ny + j) * F.nz + k;
-        const PairVal pv = load_pair<JT_STORE_F32>(F.pairs, base + node);
         // blended corner value dotted with g
-        const float vx = ca * pv.axy.x + cb * pv.bxy.x, vy = ca * pv.axy.y + cb * pv.bxy.y;
-        const float vz = ca * pv.az + cb * pv.bz;
+        float vx, vy, vz;
+        if (STAGE) {
+            const float4 v = __ldg(stage + node);
+            vx = v.x; vy = v.y; vz = v.z;
+        } else {
+            const PairVal pv = load_pair<JT_STORE_F32>(F.pairs, base + node);
+            vx = ca * pv.axy.x + cb * pv.bxy.x;
+            vy = ca * pv.axy.y + cb * pv.bxy.y;
+            vz = ca * pv.az + cb * pv.bz;
+        }
         const float vg = vx * g.x + vy * g.y + vz * g.z;
         const float sx = bx ? 1.0f : -1.0f, sy = by ? 1.0f : -1.0f, sz = bz ? 1.0f : -1.0f;
         jtg.x += sx * a.x.dfdx * wy * wz * vg;
@@ -169,13 +182,22 @@ struct StepRec {
 // records per step (stage times t, t + h/2, t + h), (3*nseg, nodes) float4.
 // PRE: some axis has a boundary whose derivative is not 1 (clamp,
 // absorbing, reflective), so the pre-boundary end point is kept.
-template <bool PRE>
+// STAGE: P.stage holds the segment's float32 stage fields (3 per step, slot
+// 3*s + k for stage k of local step s), used for the recompute (bit-identical
+// to blending the pair records) and the vector-Jacobian products.
+template <bool PRE, bool STAGE>
 __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
     k_adjoint_rk4(jt_grid_field F, jt_boundary B, jt_adjoint_params P, float4* __restrict__ acc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n_particles) return;
     typedef GridField<true, JT_STORE_F32> Fw;
     const Fw f{F};
+    jt_grid_field FS = F;  // the stage fields as a grid descriptor
+    FS.storage = JT_STORE_STAGE_F32;
+    FS.pairs = P.stage;
+    FS.n_pairs = 3 * (P.step_end - P.step_begin);
+    const StageGridField<true, JT_STORE_STAGE_F32> fs{FS};
+    const float4* stage4 = reinterpret_cast<const float4*>(P.stage);
     typedef Ar<true> A;
     const int nseg = P.step_end - P.step_begin;
     const int64_t nodes = F.pair_stride;
@@ -190,8 +212,15 @@ __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
 #pragma unroll 1
         for (int st = 0; st < 4; ++st) {
             r[3 * st] = xs.x; r[3 * st + 1] = xs.y; r[3 * st + 2] = xs.z;
-            const jt_blend es = e[st == 0 ? 0 : (st == 3 ? 2 : 1)];
-            const V3 kk = f(xs, es, flags);
+            const int sk = st == 0 ? 0 : (st == 3 ? 2 : 1);
+            V3 kk;
+            if (STAGE) {
+                jt_blend es{};
+                es.pair = 3 * s + sk;
+                kk = fs(xs, es, flags);
+            } else {
+                kk = f(xs, e[sk], flags);
+            }
             if (st == 0) {
                 sm = kk;
             } else if (st == 3) {
@@ -239,22 +268,25 @@ __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
         const Ax3 ax4 = axes_of(F, x4);
         const bool join = pend && same_entry(*pend_e, e2) && same_cell(pend_ax, ax4);
         if (pend && !join) scatter(F, pend_ax, pend_g, pend_acc);
-        const V3 d4 = grid_vjp(F, ax4, e2, V3{c6 * lam.x, c6 * lam.y, c6 * lam.z}, join ? pend_acc : a2,
-                               join ? &pend_ax : nullptr, pend_g);                         // k4 = v(x4)
+        const float4* s0 = STAGE ? stage4 + (int64_t)(3 * s) * nodes : nullptr;
+        const float4* s1 = STAGE ? s0 + nodes : nullptr;
+        const float4* s2 = STAGE ? s1 + nodes : nullptr;
+        const V3 d4 = grid_vjp<STAGE>(F, ax4, e2, V3{c6 * lam.x, c6 * lam.y, c6 * lam.z}, join ? pend_acc : a2,
+                                      join ? &pend_ax : nullptr, pend_g, s2);                         // k4 = v(x4)
         lx = V3{lx.x + d4.x, lx.y + d4.y, lx.z + d4.z};
         const V3 g3{c3 * lam.x + k.dt * d4.x, c3 * lam.y + k.dt * d4.y, c3 * lam.z + k.dt * d4.z};
         // k3 = v(x3) and k2 = v(x2) share the stage time t + h/2 and almost
         // always the cell: one atomic per corner carries both contributions
         const Ax3 ax3 = axes_of(F, x3), ax2 = axes_of(F, x2);
         const bool merge = same_cell(ax3, ax2);
-        const V3 d3 = grid_vjp(F, ax3, e1, g3, merge ? nullptr : a1, nullptr, none);
+        const V3 d3 = grid_vjp<STAGE>(F, ax3, e1, g3, merge ? nullptr : a1, nullptr, none, s1);
         lx = V3{lx.x + d3.x, lx.y + d3.y, lx.z + d3.z};
         const V3 g2{c3 * lam.x + k.dth * d3.x, c3 * lam.y + k.dth * d3.y, c3 * lam.z + k.dth * d3.z};
-        const V3 d2 = grid_vjp(F, ax2, e1, g2, a1, merge ? &ax3 : nullptr, g3);
+        const V3 d2 = grid_vjp<STAGE>(F, ax2, e1, g2, a1, merge ? &ax3 : nullptr, g3, s1);
         lx = V3{lx.x + d2.x, lx.y + d2.y, lx.z + d2.z};
         const V3 g1{c6 * lam.x + k.dth * d2.x, c6 * lam.y + k.dth * d2.y, c6 * lam.z + k.dth * d2.z};
         const Ax3 ax0 = axes_of(F, x0);
-        const V3 d1 = grid_vjp(F, ax0, e0, g1, nullptr, nullptr, none);                     // k1 = v(x0)
+        const V3 d1 = grid_vjp<STAGE>(F, ax0, e0, g1, nullptr, nullptr, none, s0);          // k1 = v(x0)
         lam = V3{lx.x + d1.x, lx.y + d1.y, lx.z + d1.z};
         pend = acc != nullptr;
         pend_ax = ax0;
@@ -342,8 +374,14 @@ extern "C" int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, cons
     }
     bool pre = false;
     for (int a = 0; a < 3; ++a) pre |= bc->axis_kind[a] != JT_BC_PERIODIC && bc->axis_kind[a] != JT_BC_NONE;
-    if (pre) k_adjoint_rk4<true><<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
-    else k_adjoint_rk4<false><<<grid_blocks(p->n_particles), kBlock, 0, s>>>(F, *bc, *p, acc);
+    const unsigned gb = grid_blocks(p->n_particles);
+    if (p->stage != nullptr) {
+        if (pre) k_adjoint_rk4<true, true><<<gb, kBlock, 0, s>>>(F, *bc, *p, acc);
+        else k_adjoint_rk4<false, true><<<gb, kBlock, 0, s>>>(F, *bc, *p, acc);
+    } else {
+        if (pre) k_adjoint_rk4<true, false><<<gb, kBlock, 0, s>>>(F, *bc, *p, acc);
+        else k_adjoint_rk4<false, false><<<gb, kBlock, 0, s>>>(F, *bc, *p, acc);
+    }
     int rc = cuda_status(cudaGetLastError(), "adjoint kernel launch");
     if (rc != JT_OK || acc == nullptr) return rc;
     k_adjoint_fold<<<grid_blocks(F.pair_stride), kBlock, 0, s>>>(F, p->schedule + 4 * (int64_t)p->step_begin, nseg,

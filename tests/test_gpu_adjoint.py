@@ -137,14 +137,16 @@ def test_adjoint_reflective_and_segments():
 
 
 def test_adjoint_position_gradient_alone_and_sorted_agree():
-    """dL/dx0 without a snapshot gradient equals the one computed with it, and
-    the cell-sorted and unsorted runs give the same forward positions."""
+    """dL/dx0 without a snapshot gradient equals the one computed with it, the
+    cell-sorted and unsorted runs give the same forward positions, and the
+    backward on float32 stage fields gives the same bits as on pair records
+    (the stage fields are blended with the same arithmetic)."""
     import torch
     g, st, data, x0, y = _setup(npart=3000, seed=8)
     outs = []
-    for sort_min, need_u in ((1 << 30, True), (0, True), (0, False)):
+    for sort_min, need_u, stage in ((1 << 30, True, False), (0, True, True), (0, False, True)):
         solver = AdjointRK4(st, g, g, g, "periodic", jt.periodic_boundary(W.UNIT), checkpoint_every=9,
-                            sort_bits=4, sort_min_particles=sort_min)
+                            sort_bits=4, sort_min_particles=sort_min, stage_fields=stage)
         x0_t = torch.tensor(x0, device="cuda", requires_grad=True)
         U_t = torch.tensor(data.reshape(len(st), 16, 16, 16, 3), device="cuda", requires_grad=need_u)
         xT = solver(x0_t, U_t, (0.0, 0.25), 26, dt=0.01)

@@ -145,3 +145,43 @@ def test_estimate_batch_size_matches_reference_rule():
     from jaxtrace_gb300.tracker import _estimate_memory_usage
     assert _estimate_memory_usage(bs, 1001) <= 1.0
     assert _estimate_memory_usage(bs * 2, 1001) > 1.0 or bs * 2 > 100_000
+
+
+def test_new_entry_points_validate_before_touching_the_device():
+    """Argument checks of the entry points added beside the reference API
+    return their error codes without a GPU."""
+    lib = L.load()
+    # stage fields need a regular-grid field and a known output storage
+    with pytest.raises(ValueError, match="regular-grid"):
+        L.check(lib.jt_stage_fields(None, None, None, 3, L.JT_STORE_STAGE_F32, None, None))
+    g = L.GridField()
+    g.nx = g.ny = g.nz = 4
+    g.pair_stride = 64
+    g.n_pairs = 1
+    g.pairs = 16                     # never dereferenced: rejected first
+    f = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
+    with pytest.raises(ValueError, match="out_storage"):
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, 7, C.c_void_p(16), None))
+    with pytest.raises(ValueError, match="out_scales"):
+        g.storage = L.JT_STORE_BF16
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F16, C.c_void_p(16), None))
+    with pytest.raises(NotImplementedError, match="float32 stage fields"):
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(16), None))
+    assert lib.jt_stage_fields(C.byref(f), None, None, 0, L.JT_STORE_STAGE_F32, None, None) == 0
+    # adjoint workspace: three float4 accumulators per step and node
+    assert lib.jt_adjoint_workspace_bytes(1000, 50) == 3 * 50 * 1000 * 16
+    assert lib.jt_adjoint_workspace_bytes(1000, 65) == 0
+    # tracking launch parameters
+    p = L.TrackParams()
+    p.integrator, p.n_particles, p.step_end = L.JT_RK4, 10, 5
+    p.schedule, p.pos = 16, 16
+    p.block_size = 96
+    bc = L.Boundary()
+    g.storage = L.JT_STORE_F32
+    with pytest.raises(ValueError, match="block_size"):
+        L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    # FEM hash-grid descriptors
+    h = L.FemField()
+    ff = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(h))
+    with pytest.raises(ValueError, match="FEM field"):
+        L.check(lib.jt_track(C.byref(ff), C.byref(bc), C.byref(p), None))
