@@ -281,11 +281,16 @@ def adjoint_leg(a, profile=False):
             gref, pool = gx, n
         times = np.linspace(0.0, horizon * dt, horizon + 1, dtype=np.float32)
         picks = list(zip(rng.integers(0, pool, 96), rng.integers(0, 3, 96)))
-        for h in (1e-3, 1e-5):
+        for h in (1e-3, 1e-5, 1e-7):
             ad, fd = [], []
             for i, ax in picks:
-                pair = np.repeat(x0[i:i + 1], 2, axis=0)
-                xp, xm = np.float32(float(x0[i, ax]) + h), np.float32(float(x0[i, ax]) - h)
+                if h < 1e-6:
+                    # below float32 resolution: float64 start points straddle fewer cell faces
+                    pair = np.repeat(x0[i:i + 1].astype(np.float64), 2, axis=0)
+                    xp, xm = float(x0[i, ax]) + h, float(x0[i, ax]) - h
+                else:
+                    pair = np.repeat(x0[i:i + 1], 2, axis=0)
+                    xp, xm = np.float32(float(x0[i, ax]) + h), np.float32(float(x0[i, ax]) - h)
                 pair[0, ax], pair[1, ax] = xp, xm
                 out, _, _ = oracle.track(spec, obc, pair, times, dt, precision=oracle.ORC_F64)
                 fd.append((np.sum((out[0] - y[i]) ** 2) - np.sum((out[1] - y[i]) ** 2)) / (float(xp) - float(xm)))
@@ -297,30 +302,33 @@ def adjoint_leg(a, profile=False):
     # dL/dU of a 2048-particle subset's loss against float64 central differences
     # (h = 1e-3 on one snapshot value; each difference reruns the subset in the oracle)
     m = 2048
-    xs = torch.tensor(x0[:m], device="cuda")
-    Us = U_t.detach().clone().requires_grad_(True)
-    xh = solver(xs, Us, (0.0, n_steps * dt), n_steps + 1, dt=dt)
-    ((xh - y_t[:m]) ** 2).sum().backward()
-    gU = Us.grad.cpu().numpy().reshape(16, -1, 3).astype(np.float64)
-    nz = np.argwhere(gU != 0.0)
-    times = np.linspace(0.0, n_steps * dt, n_steps + 1, dtype=np.float32)
+    fd_U = {}
+    for horizon in sorted({min(50, n_steps), n_steps}):
+        xs = torch.tensor(x0[:m], device="cuda")
+        Us = U_t.detach().clone().requires_grad_(True)
+        xh = solver(xs, Us, (0.0, horizon * dt), horizon + 1, dt=dt)
+        ((xh - y_t[:m]) ** 2).sum().backward()
+        gU = Us.grad.cpu().numpy().reshape(16, -1, 3).astype(np.float64)
+        nz = np.argwhere(gU != 0.0)
+        times = np.linspace(0.0, horizon * dt, horizon + 1, dtype=np.float32)
 
-    def sub_loss(d):
-        s = oracle.GridSpec(d, c["times"], g, g, g, "periodic")
-        o, _, _ = oracle.track(s, obc, x0[:m], times, dt, precision=oracle.ORC_F64)
-        return float(np.sum((o - y[:m]) ** 2))
+        def sub_loss(d):
+            s = oracle.GridSpec(d, c["times"], g, g, g, "periodic")
+            o, _, _ = oracle.track(s, obc, x0[:m], times, dt, precision=oracle.ORC_F64)
+            return float(np.sum((o - y[:m]) ** 2))
 
-    ad, fd = [], []
-    for t, nd, cc in nz[rng.choice(len(nz), size=min(24, len(nz)), replace=False)]:
-        dp, dm = c["data"].copy(), c["data"].copy()
-        dp[t, nd, cc] += np.float32(1e-3)
-        dm[t, nd, cc] -= np.float32(1e-3)
-        fd.append((sub_loss(dp) - sub_loss(dm)) / (float(dp[t, nd, cc]) - float(dm[t, nd, cc])))
-        ad.append(gU[t, nd, cc])
-    ad, fd = np.array(ad), np.array(fd)
-    rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
-    fd_U = {"frac_within_1e-3": float(np.mean(rel < 1e-3)), "median_rel": float(np.median(rel)),
-            "samples": int(len(rel)), "subset_particles": m, "h": 1e-3}
+        ad, fd = [], []
+        for t, nd, cc in nz[rng.choice(len(nz), size=min(24, len(nz)), replace=False)]:
+            dp, dm = c["data"].copy(), c["data"].copy()
+            dp[t, nd, cc] += np.float32(1e-3)
+            dm[t, nd, cc] -= np.float32(1e-3)
+            fd.append((sub_loss(dp) - sub_loss(dm)) / (float(dp[t, nd, cc]) - float(dm[t, nd, cc])))
+            ad.append(gU[t, nd, cc])
+        ad, fd = np.array(ad), np.array(fd)
+        rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
+        fd_U[f"{horizon}_steps_h0.001"] = {"frac_within_1e-3": float(np.mean(rel < 1e-3)),
+                                           "median_rel": float(np.median(rel)), "samples": int(len(rel)),
+                                           "subset_particles": m}
     f, b = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
     return {"fd_check_dL_dU": fd_U,
             "workload": f"differentiation: 64^3 periodic ABC, 16 snapshots, {n:,} lattice seeds, RK4 dt=0.01, "
@@ -329,9 +337,10 @@ def adjoint_leg(a, profile=False):
             "forward_particle_steps_per_s": n * n_steps / (f / 1e3),
             "adjoint_particle_steps_per_s": n * n_steps / (b / 1e3),
             "fd_check_dL_dx0": fd_stats,
-            "fd_note": "float64 central differences of single particles at h=1e-3 and h=1e-5 on x0; trilinear "
-                       "cell faces make the exact derivative jump, so the wider step and the longer horizon "
-                       "have more samples whose difference straddles a face"}
+            "fd_note": "float64 central differences of single particles at h=1e-3, 1e-5 (float32 start points) "
+                       "and 1e-7 (float64 start points) on x0; trilinear cell faces make the exact derivative "
+                       "jump, so the wider steps and the longer horizon have more samples whose difference "
+                       "straddles a face"}
 
 
 def _mesh_oracle_spec(c, f):

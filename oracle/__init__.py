@@ -82,7 +82,8 @@ def load():
     if _lib is None:
         build()
         lib = C.CDLL(str(LIB))
-        lib.orc_track.argtypes = [C.POINTER(OrcField), C.POINTER(OrcBoundary), C.POINTER(OrcRun), i32, vp, vp, vp, vp]
+        lib.orc_track.argtypes = [C.POINTER(OrcField), C.POINTER(OrcBoundary), C.POINTER(OrcRun), i32, vp, vp, vp, vp,
+                                  vp]
         lib.orc_track.restype = i32
         lib.orc_sample.argtypes = [C.POINTER(OrcField), f64, i32, i32, i32, vp, vp, vp]
         lib.orc_sample.restype = i32
@@ -233,8 +234,12 @@ class FemSpec:
 
 def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F32, n_threads=0,
           record=False):
-    """Run the oracle; returns (final positions, trajectory or None, run info)."""
+    """Run the oracle; returns (final positions, trajectory or None, run info).
+    In float64 mode a float64 ``x0`` is used as given (no float32 rounding)."""
     lib = load()
+    x64 = None
+    if precision == ORC_F64 and np.asarray(x0).dtype == np.float64:
+        x64 = np.ascontiguousarray(np.asarray(x0, np.float64).reshape(-1, 3))
     x0 = np.ascontiguousarray(np.asarray(x0, np.float32).reshape(-1, 3))
     st = np.ascontiguousarray(np.asarray(step_times, np.float32))
     n = x0.shape[0]
@@ -244,7 +249,7 @@ def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F
     out64 = np.zeros((n, 3), np.float64) if precision == ORC_F64 else None
     traj = np.zeros((len(st), n, 3), np.float32) if (record and precision == ORC_F32) else None
     rc = lib.orc_track(C.byref(field.c), C.byref(boundary.c), C.byref(r), n, x0.ctypes.data, _p(out32), _p(out64),
-                       _p(traj))
+                       _p(traj), _p(x64))
     if rc != 0:
         raise RuntimeError("oracle rejected its arguments")
     out = out32 if precision == ORC_F32 else out64

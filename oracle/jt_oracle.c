@@ -803,9 +803,12 @@ static void step_d(const orc_field* F, const orc_run* R, int s, double* x, int64
 /* Track n particles through all steps (tracker.py:441-446).  x0: (n,3)
  * float32.  out_f32 (n,3) in ORC_F32 mode or out_f64 (n,3) in ORC_F64 mode.
  * traj (T,n,3) float32 may be NULL; when given every step is recorded. */
+/* x0_f64 (optional, float64 mode): float64 initial positions, so finite
+ * differences can use steps below float32 resolution. */
 int orc_track(const orc_field* F, const orc_boundary* B, orc_run* R, int n, const float* x0,
-              float* out_f32, double* out_f64, float* traj) {
-    if (F == NULL || B == NULL || R == NULL || n < 0 || x0 == NULL) return -1;
+              float* out_f32, double* out_f64, float* traj, const double* x0_f64) {
+    if (F == NULL || B == NULL || R == NULL || n < 0 || (x0 == NULL && x0_f64 == NULL)) return -1;
+    if (x0 == NULL && R->precision == ORC_F32) return -1;
     const float* lat[2] = {B->lattice[0], B->lattice[1]};
     if (B->inlet_axis >= 0 && (lat[0] == NULL || lat[1] == NULL)) return -1;
     int64_t fb = 0, wr = 0;
@@ -825,7 +828,8 @@ int orc_track(const orc_field* F, const orc_boundary* B, orc_run* R, int n, cons
             }
             memcpy(out_f32 + 3 * (size_t)i, x, sizeof x);
         } else {
-            double x[3] = {x0[3 * (size_t)i], x0[3 * (size_t)i + 1], x0[3 * (size_t)i + 2]};
+            double x[3];
+            for (int a = 0; a < 3; ++a) x[a] = x0_f64 ? x0_f64[3 * (size_t)i + a] : (double)x0[3 * (size_t)i + a];
             for (int s = 0; s + 1 < T; ++s) {
                 step_d(F, R, s, x, &fb);
                 boundary_d(B, lat[0], lat[1], x);
