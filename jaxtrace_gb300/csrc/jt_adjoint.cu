@@ -348,6 +348,7 @@ extern "C" int jt_adjoint_rk4(const jt_field* field, const jt_boundary* bc, cons
     if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
         return set_error(JT_ERR_UNSUPPORTED, "the adjoint runs on regular-grid fields");
     const jt_grid_field& F = *field->grid;
+    if (int rc = check_grid_shape(F)) return rc;
     if (F.storage != JT_STORE_F32) return set_error(JT_ERR_UNSUPPORTED, "the adjoint needs float32 snapshot storage");
     if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshot pairs");
     if (bc == nullptr || p == nullptr) return set_error(JT_ERR_INVALID, "boundary and params are required");

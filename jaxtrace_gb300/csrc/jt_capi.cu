@@ -54,14 +54,25 @@ static int check_nearest(const jt_nearest_field* q) {
     return check_storage(q->storage);
 }
 
+int check_grid_shape(const jt_grid_field& g) {
+    if (g.nx < 1 || g.ny < 1 || g.nz < 1)
+        return set_error(JT_ERR_INVALID, "grid shape (%d,%d,%d) must be positive", g.nx, g.ny, g.nz);
+    const int32_t kAxisMax = 1 << 24;
+    if (g.nx > kAxisMax || g.ny > kAxisMax || g.nz > kAxisMax)
+        return set_error(JT_ERR_INVALID, "grid axes hold at most 2^24 nodes, got (%d,%d,%d)", g.nx, g.ny, g.nz);
+    if ((int64_t)g.nx * g.ny * g.nz > (int64_t)INT32_MAX)
+        return set_error(JT_ERR_INVALID, "grid holds %lld nodes, more than 2^31 - 1",
+                         (long long)((int64_t)g.nx * g.ny * g.nz));
+    return JT_OK;
+}
+
 static int check_field(const jt_field* f) {
     if (f == nullptr) return set_error(JT_ERR_INVALID, "field is NULL");
     switch (f->kind) {
         case JT_FIELD_GRID: {
             const jt_grid_field* g = f->grid;
             if (g == nullptr) return set_error(JT_ERR_INVALID, "grid field descriptor is NULL");
-            if (g->nx < 1 || g->ny < 1 || g->nz < 1)
-                return set_error(JT_ERR_INVALID, "grid shape (%d,%d,%d) must be positive", g->nx, g->ny, g->nz);
+            if (int rc = check_grid_shape(*g)) return rc;
             if (g->bounds_mode < JT_GRID_CLAMP || g->bounds_mode > JT_GRID_PERIODIC)
                 return set_error(JT_ERR_INVALID, "unknown bounds_mode %d", g->bounds_mode);
             if (g->n_pairs < 1 || g->pairs == nullptr) return set_error(JT_ERR_INVALID, "grid field has no snapshot pairs");

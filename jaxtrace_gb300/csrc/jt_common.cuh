@@ -15,8 +15,9 @@ namespace jt {
 
 // Tuning switches.  JT_LERP_NOINLINE=1 moves the rarely taken extrapolation
 // blend out of line (measured 2x slower: the call forces a stack frame on the
-// hot path); JT_STAGE_UNROLL unrolls the RK stage loop (measured slower at the
-// default occupancy: more registers, more instruction-cache misses).
+// hot path); JT_STAGE_UNROLL unrolls the RK stage loop of every field (measured
+// slower for the pair-gather, mesh and FEM bodies: more registers, more
+// instruction-cache misses); a field type opts in with kUnrollStages.
 #ifndef JT_LERP_NOINLINE
 #define JT_LERP_NOINLINE 0
 #endif
@@ -372,6 +373,48 @@ struct StepConst {
     float dt, dth, dt6;
 };
 
+// Whether a field's evaluations are unrolled over the integrator stages: a
+// field type may set kUnrollStages (a short evaluation body, where the loop's
+// own instructions cost more than the larger code), otherwise the stage loop
+// follows JT_STAGE_UNROLL.
+template <class F, class = void>
+struct UnrollStagesOf {
+    static constexpr bool value = false;
+};
+template <class F>
+struct UnrollStagesOf<F, decltype(void(F::kUnrollStages))> {
+    static constexpr bool value = F::kUnrollStages;
+};
+
+// RK4 stage st: evaluate at xs, fold k into the weighted sum sm and move xs to
+// the next stage position (rk4.py:82-106).
+template <bool EXACT, class Field>
+__device__ __forceinline__ void rk4_stage(const Field& f, const jt_blend* s, const StepConst& k, int st,
+                                          const V3& x, V3& xs, V3& sm, int& flags) {
+    typedef Ar<EXACT> A;
+    const jt_blend e = s[st == 0 ? 0 : (st == 3 ? 2 : 1)];
+    const V3 kk = f(xs, e, flags);
+    if (st == 0) {
+        sm = kk;
+    } else if (st == 3) {
+        sm = V3{A::add(sm.x, kk.x), A::add(sm.y, kk.y), A::add(sm.z, kk.z)};
+    } else {
+        sm = V3{A::axpy(sm.x, 2.0f, kk.x), A::axpy(sm.y, 2.0f, kk.y), A::axpy(sm.z, 2.0f, kk.z)};
+    }
+    const float h = st < 2 ? k.dth : k.dt;
+    xs = V3{A::axpy(x.x, h, kk.x), A::axpy(x.y, h, kk.y), A::axpy(x.z, h, kk.z)};
+}
+
+// RK2 stage st: evaluate at xs and move xs to the midpoint (rk2.py:283-309).
+template <bool EXACT, class Field>
+__device__ __forceinline__ void rk2_stage(const Field& f, const jt_blend* s, const StepConst& k, int st,
+                                          const V3& x, V3& xs, V3& v, int& flags) {
+    typedef Ar<EXACT> A;
+    const jt_blend e = s[st];
+    v = f(xs, e, flags);
+    xs = V3{A::axpy(x.x, k.dth, v.x), A::axpy(x.y, k.dth, v.y), A::axpy(x.z, k.dth, v.z)};
+}
+
 template <bool EXACT, int INTEG, bool COMP, class Field>
 __device__ __forceinline__ void integrate(const Field& f, const jt_blend* s, const StepConst& k,
                                           V3& x, V3& c, int& flags) {
@@ -382,29 +425,22 @@ __device__ __forceinline__ void integrate(const Field& f, const jt_blend* s, con
         // x + dth*k2, x + dt*k3 and the sum ((k1 + 2k2) + 2k3) + k4 in the
         // reference's left-to-right order.
         V3 sm{0.f, 0.f, 0.f}, xs = x;
+        if (UnrollStagesOf<Field>::value) {
+#pragma unroll
+            for (int st = 0; st < 4; ++st) rk4_stage<EXACT>(f, s, k, st, x, xs, sm, flags);
+        } else {
 JT_UNROLL(JT_STAGE_UNROLL)
-        for (int st = 0; st < 4; ++st) {
-            const jt_blend e = s[st == 0 ? 0 : (st == 3 ? 2 : 1)];
-            const V3 kk = f(xs, e, flags);
-            if (st == 0) {
-                sm = kk;
-            } else if (st == 3) {
-                sm = V3{A::add(sm.x, kk.x), A::add(sm.y, kk.y), A::add(sm.z, kk.z)};
-            } else {
-                sm = V3{A::add(sm.x, A::mul(2.0f, kk.x)), A::add(sm.y, A::mul(2.0f, kk.y)),
-                        A::add(sm.z, A::mul(2.0f, kk.z))};
-            }
-            const float h = st < 2 ? k.dth : k.dt;
-            xs = V3{A::axpy(x.x, h, kk.x), A::axpy(x.y, h, kk.y), A::axpy(x.z, h, kk.z)};
+            for (int st = 0; st < 4; ++st) rk4_stage<EXACT>(f, s, k, st, x, xs, sm, flags);
         }
         inc = V3{A::mul(k.dt6, sm.x), A::mul(k.dt6, sm.y), A::mul(k.dt6, sm.z)};
     } else if (INTEG == JT_RK2) {
         V3 xs = x, v{0.f, 0.f, 0.f};
+        if (UnrollStagesOf<Field>::value) {
+#pragma unroll
+            for (int st = 0; st < 2; ++st) rk2_stage<EXACT>(f, s, k, st, x, xs, v, flags);
+        } else {
 JT_UNROLL(JT_STAGE_UNROLL)
-        for (int st = 0; st < 2; ++st) {
-            const jt_blend e = s[st];
-            v = f(xs, e, flags);
-            xs = V3{A::axpy(x.x, k.dth, v.x), A::axpy(x.y, k.dth, v.y), A::axpy(x.z, k.dth, v.z)};
+            for (int st = 0; st < 2; ++st) rk2_stage<EXACT>(f, s, k, st, x, xs, v, flags);
         }
         inc = V3{A::mul(k.dt, v.x), A::mul(k.dt, v.y), A::mul(k.dt, v.z)};
     } else {

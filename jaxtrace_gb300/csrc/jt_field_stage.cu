@@ -78,17 +78,34 @@ __global__ void __launch_bounds__(kBlock) k_stage_f16(jt_grid_field F, const jt_
     }
 }
 
-typedef Launcher<StageGridField, jt_grid_field, int> StageL;
+// The bounds mode as a template argument: clamp and periodic get their own
+// kernels, zero and nan share the run-time one.
+template <bool E, int O>
+using StageClamp = StageGridField<E, O, JT_GRID_CLAMP>;
+template <bool E, int O>
+using StagePeriodic = StageGridField<E, O, JT_GRID_PERIODIC>;
+template <bool E, int O>
+using StageAnyMode = StageGridField<E, O, -1>;
+
+template <template <bool, int> class FT>
+static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p,
+                                cudaStream_t s, bool exact) {
+    typedef Launcher<FT, jt_grid_field, int> L;
+    if (f.storage == JT_STORE_STAGE_F32)
+        return exact ? L::template track_s<true, JT_STORE_STAGE_F32>(f, 0, b, p, s)
+                     : L::template track_s<false, JT_STORE_STAGE_F32>(f, 0, b, p, s);
+    return L::template track_s<false, JT_STORE_STAGE_F16>(f, 0, b, p, s);
+}
 
 int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
     const bool exact = p.arith == JT_ARITH_EXACT;
+    if (f.storage != JT_STORE_STAGE_F32 && exact)
+        return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
     cudaError_t err;
-    if (f.storage == JT_STORE_STAGE_F32) {
-        err = exact ? StageL::track_s<true, JT_STORE_STAGE_F32>(f, 0, b, p, s)
-                    : StageL::track_s<false, JT_STORE_STAGE_F32>(f, 0, b, p, s);
-    } else {
-        if (exact) return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
-        err = StageL::track_s<false, JT_STORE_STAGE_F16>(f, 0, b, p, s);
+    switch (f.bounds_mode) {
+        case JT_GRID_CLAMP: err = stage_launch<StageClamp>(f, b, p, s, exact); break;
+        case JT_GRID_PERIODIC: err = stage_launch<StagePeriodic>(f, b, p, s, exact); break;
+        default: err = stage_launch<StageAnyMode>(f, b, p, s, exact); break;
     }
     return cuda_status(err, "tracking kernel launch");
 }
@@ -102,6 +119,7 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
         return set_error(JT_ERR_INVALID, "stage fields need a regular-grid field");
     const jt_grid_field& F = *field->grid;
+    if (int rc = check_grid_shape(F)) return rc;
     if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
     if (n == 0) return JT_OK;
     if (entries == nullptr || out == nullptr) return set_error(JT_ERR_INVALID, "entries and out are required");

@@ -14,12 +14,14 @@
 namespace jt {
 
 // Continuous index, cell and weight of one axis (structured.py:289-322).
-template <bool EXACT>
+// FMA_IDX (fast arithmetic only): the index as one FMA, x * inv_d + nofs with
+// nofs = -x_min * inv_d.
+template <bool EXACT, bool FMA_IDX = false>
 __device__ __forceinline__ void grid_axis(float x, float org, float d, float inv_d, int n, int mode, float vhi,
-                                          int& i0, int& i1, float& w, bool& valid, int& flags) {
+                                          int& i0, int& i1, float& w, bool& valid, int& flags, float nofs = 0.0f) {
     typedef Ar<EXACT> A;
     // (x - x_min) / dx; the fast modes multiply by the reciprocal
-    float f = EXACT ? __fdiv_rn(__fsub_rn(x, org), d) : (x - org) * inv_d;
+    float f = EXACT ? __fdiv_rn(__fsub_rn(x, org), d) : (FMA_IDX ? fmaf(x, inv_d, nofs) : (x - org) * inv_d);
     if (mode == JT_GRID_PERIODIC) {
         const int nn = n > 1 ? n : 1;
         f = np_mod(f, (float)nn);          // np.mod(fx, max(Nx,1))
@@ -39,9 +41,9 @@ __device__ __forceinline__ void grid_axis(float x, float org, float d, float inv
         const float hi = (float)(n > 1 ? n - 1 : 0);
         f = np_clip(f, 0.0f, hi);          // np.clip(fx, 0, max(Nx-1,0))
         const float fl = floorf(f);
-        int i = (int)fl;
-        if (i < 0) i = 0;
-        if (i > n - 1) i = n - 1;
+        // fl is an integer in [0, n-1] (n <= 2^24, so n-1 is exact), or NaN,
+        // which converts to 0: the cell is always in range
+        const int i = __float2int_rz(fl);
         w = A::sub(f, fl);
         i0 = i;
         i1 = (i + 1 > n - 1) ? (n - 1) : i + 1;  // np.clip(i0+1, 0, max(Nx-1,0))
@@ -86,6 +88,29 @@ __device__ __forceinline__ V3 trilinear(const CV& v000, const CV& v100, const CV
     const float2 cz1 = dot2p<EXACT>(make_float2(v010.z, v011.z), OX, make_float2(v110.z, v111.z), WX);
     const float2 cz = dot2p<EXACT>(cz0, OY, cz1, WY);
     return V3{rxy.x, rxy.y, A::dot2(cz.x, oz, cz.y, wz)};
+}
+
+// b - a on a pair, as one packed FMA with -1 (exact: a single rounding).
+__device__ __forceinline__ float2 sub2(float2 b, float2 a) { return __ffma2_rn(a, make_float2(-1.0f, -1.0f), b); }
+
+// Fast-arithmetic trilinear in lerp form, a + w (b - a) per level: the same
+// x, then y, then z order without the (1 - w) weights.
+__device__ __forceinline__ V3 trilinear_lerp(const CV& v000, const CV& v100, const CV& v010, const CV& v110,
+                                             const CV& v001, const CV& v101, const CV& v011, const CV& v111, float wx,
+                                             float wy, float wz) {
+    const float2 WX = splat(wx), WY = splat(wy), WZ = splat(wz);
+    const float2 c00 = __ffma2_rn(WX, sub2(v100.xy, v000.xy), v000.xy);
+    const float2 c10 = __ffma2_rn(WX, sub2(v110.xy, v010.xy), v010.xy);
+    const float2 c01 = __ffma2_rn(WX, sub2(v101.xy, v001.xy), v001.xy);
+    const float2 c11 = __ffma2_rn(WX, sub2(v111.xy, v011.xy), v011.xy);
+    const float2 c0 = __ffma2_rn(WY, sub2(c10, c00), c00);
+    const float2 c1 = __ffma2_rn(WY, sub2(c11, c01), c01);
+    const float2 rxy = __ffma2_rn(WZ, sub2(c1, c0), c0);
+    const float2 z0 = make_float2(v000.z, v001.z), z1 = make_float2(v010.z, v011.z);
+    const float2 cz0 = __ffma2_rn(WX, sub2(make_float2(v100.z, v101.z), z0), z0);
+    const float2 cz1 = __ffma2_rn(WX, sub2(make_float2(v110.z, v111.z), z1), z1);
+    const float2 cz = __ffma2_rn(WY, sub2(cz1, cz0), cz0);
+    return V3{rxy.x, rxy.y, fmaf(wz, cz.y - cz.x, cz.x)};
 }
 
 __device__ __forceinline__ float2 h2f2(uint32_t w) { return __half22float2(*reinterpret_cast<const __half2*>(&w)); }
@@ -163,25 +188,40 @@ struct GridField {
 #define JT_STAGE16_MIN_BLOCKS 6
 #endif
 
-template <bool EXACT, int OUT>
+//
+// MODE >= 0 fixes the bounds mode at compile time (clamp and periodic, the
+// common ones), which removes the mode tests and the unused validity tests
+// from every evaluation; MODE < 0 reads F.bounds_mode at run time.  The fast
+// arithmetic maps coordinates to indices with one FMA and interpolates in
+// lerp form.
+template <bool EXACT, int OUT, int MODE = -1>
 struct StageGridField {
-    // float16 quads fit 6 blocks of 256 (38 registers, no spills), which
-    // hides more of the stage fields' HBM latency; float32 records take 64 at 4
+    // float16 quads fit 6 blocks of 256 (no spills), which hides more of the
+    // stage fields' latency; float32 records take 64 registers at 4
     static constexpr int kMinBlocks = OUT == JT_STORE_STAGE_F16 ? JT_STAGE16_MIN_BLOCKS : 4;
+    // the evaluation is short enough that the kernel is bound by instruction
+    // issue: unrolled stages drop the loop's own instructions
+    static constexpr bool kUnrollStages = true;
     jt_grid_field F;
+    float nofs[3];  // -origin * inv_spacing per axis (fast arithmetic)
 
-    static StageGridField create(const jt_grid_field& d, int) { return StageGridField{d}; }
+    static StageGridField create(const jt_grid_field& d, int) {
+        StageGridField s{d, {0.0f, 0.0f, 0.0f}};
+        for (int a = 0; a < 3; ++a) s.nofs[a] = -d.origin[a] * d.inv_spacing[a];
+        return s;
+    }
 
     __device__ __forceinline__ V3 operator()(const V3& p, const jt_blend& e, int& flags) const {
+        const int mode = MODE >= 0 ? MODE : F.bounds_mode;
         int i0, i1, j0, j1, k0, k1;
         float wx, wy, wz;
         bool vx, vy, vz;
-        grid_axis<EXACT>(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, F.bounds_mode, F.valid_hi[0], i0,
-                         i1, wx, vx, flags);
-        grid_axis<EXACT>(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, F.bounds_mode, F.valid_hi[1], j0,
-                         j1, wy, vy, flags);
-        grid_axis<EXACT>(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, F.bounds_mode, F.valid_hi[2], k0,
-                         k1, wz, vz, flags);
+        grid_axis<EXACT, !EXACT>(p.x, F.origin[0], F.spacing[0], F.inv_spacing[0], F.nx, mode, F.valid_hi[0], i0,
+                                 i1, wx, vx, flags, nofs[0]);
+        grid_axis<EXACT, !EXACT>(p.y, F.origin[1], F.spacing[1], F.inv_spacing[1], F.ny, mode, F.valid_hi[1], j0,
+                                 j1, wy, vy, flags, nofs[1]);
+        grid_axis<EXACT, !EXACT>(p.z, F.origin[2], F.spacing[2], F.inv_spacing[2], F.nz, mode, F.valid_hi[2], k0,
+                                 k1, wz, vz, flags, nofs[2]);
         const int slot = min(max(e.pair, 0), F.n_pairs - 1);
         const int64_t base = (int64_t)slot * F.pair_stride;
         const int ny = F.ny, nz = F.nz;
@@ -199,7 +239,8 @@ struct StageGridField {
             v010 = CV{make_float2(a010.x, a010.y), a010.z}; v110 = CV{make_float2(a110.x, a110.y), a110.z};
             v001 = CV{make_float2(a001.x, a001.y), a001.z}; v101 = CV{make_float2(a101.x, a101.y), a101.z};
             v011 = CV{make_float2(a011.x, a011.y), a011.z}; v111 = CV{make_float2(a111.x, a111.y), a111.z};
-            r = trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
+            r = EXACT ? trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz)
+                      : trilinear_lerp(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
         } else {
             uint32_t q0[8], q1[8];
             ldg256(reinterpret_cast<const uint4*>(F.pairs) + 2 * (base + r00 + k0), q0);
@@ -209,12 +250,12 @@ struct StageGridField {
             v010 = CV{h2f2(q0[2]), z0b.x}; v011 = CV{h2f2(q0[3]), z0b.y};
             v100 = CV{h2f2(q1[0]), z1a.x}; v101 = CV{h2f2(q1[1]), z1a.y};
             v110 = CV{h2f2(q1[2]), z1b.x}; v111 = CV{h2f2(q1[3]), z1b.y};
-            r = trilinear<EXACT>(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
+            r = trilinear_lerp(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
             r = V3{r.x * e.wa, r.y * e.wa, r.z * e.wa};
         }
-        if (F.bounds_mode == JT_GRID_ZERO || F.bounds_mode == JT_GRID_NAN) {
+        if (mode == JT_GRID_ZERO || mode == JT_GRID_NAN) {
             if (!(vx && vy && vz)) {
-                const float o = F.bounds_mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);
+                const float o = mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);
                 r = V3{o, o, o};
             }
         }

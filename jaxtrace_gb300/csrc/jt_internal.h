@@ -11,6 +11,10 @@ namespace jt {
 int set_error(int code, const char* fmt, ...);
 // JT_OK for cudaSuccess, else JT_ERR_CUDA with the CUDA error string.
 int cuda_status(cudaError_t e, const char* what);
+// Grid shape limits the kernels rely on: every axis 1..2^24 nodes (its last
+// index is exact in float32, so a clipped coordinate floors to a valid cell)
+// and fewer than 2^31 nodes (32-bit node offsets within a snapshot).
+int check_grid_shape(const jt_grid_field& g);
 
 struct StageBlends;
 struct StepConst;

@@ -444,7 +444,13 @@ class _Engine:
         if ens is None and tracker.options.stage_fields and n_steps > 0 and self.n > 0:
             from .fields import StructuredTimeSeriesField
             if isinstance(tracker._field, StructuredTimeSeriesField):
-                self.stage = _StageFields(tracker._field, sched_dev, n_steps, int(tracker.options.stage_chunk))
+                f = tracker._field
+                rec_bytes = 16 if f._storage == L.JT_STORE_F32 else 32
+                free = torch.cuda.mem_get_info(pos.device)[0]
+                chunk = _stage_chunk(int(tracker.options.stage_chunk), n_steps, len(f.grid_x) * len(f.grid_y) * len(f.grid_z),
+                                     rec_bytes, free)
+                if chunk > 0:
+                    self.stage = _StageFields(f, sched_dev, n_steps, chunk)
 
     def _sort(self, first=False):
         src_pos = self.out if first else self.pos
@@ -622,11 +628,15 @@ class EnsembleBatch:
 class _StageFields:
     """Pre-blended stage fields of a regular-grid run (jt_stage_fields).
 
-    Step s, stage k (0: t, 1: t + h/2, 2: t + h) reads field slot
-    3 * (s mod chunk) + k, so a launch of at most ``chunk`` steps finds every
-    step's fields in place after ``prepare``.  Float32 snapshots give float32
-    node records blended with the exact arithmetic; 16-bit snapshots give
-    float16 yz-quads divided by a power-of-two bound of the blend.
+    The stage entries of the run (step s, stage k: 0 at t, 1 at t + h/2,
+    2 at t + h) are numbered in order, and an entry equal to the one before it
+    (the t + h entry of a step and the t entry of the next, when the float32
+    times agree) takes the same number u.  Entry u lives in ring slot
+    u mod (3 * chunk); the entries of a launch of at most ``chunk`` steps span
+    at most 3 * chunk numbers, so ``prepare`` finds room for all of them.
+    Float32 snapshots give float32 node records blended with the exact
+    arithmetic; 16-bit snapshots give float16 yz-quads divided by a
+    power-of-two bound of the blend.
     """
 
     def __init__(self, field, sched_dev, n_steps: int, chunk: int):
@@ -637,7 +647,13 @@ class _StageFields:
         host = np.ascontiguousarray(sched_dev.cpu().numpy()).view(BLEND_DTYPE).reshape(-1)
         n_ent = 4 * n_steps
         host = host[:n_ent].copy()
-        src = host.reshape(n_steps, 4)[:, :3].reshape(-1).copy()          # 3 entries per step
+        every = host.reshape(n_steps, 4)[:, :3].reshape(-1).copy()        # 3 entries per step
+        self.uid = _stage_numbers(every)
+        first = np.ones(len(every), dtype=bool)
+        first[1:] = self.uid[1:] != self.uid[:-1]
+        src = every[first]                                                  # one entry per number
+        self.slots = 3 * self.chunk
+        self.ready = -1                                                     # last number blended
         self.f32 = field._storage == L.JT_STORE_F32
         self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
         scales = np.ones(len(src), dtype=F32)
@@ -645,11 +661,11 @@ class _StageFields:
             scales = _stage_scales(src)
         # the tracking schedule: pair -> slot, weights -> the slot's scale
         stage = host.copy().reshape(n_steps, 4)
-        steps = np.arange(n_steps)
+        uid = self.uid.reshape(n_steps, 3)
         for k in range(3):
-            stage[:, k]["pair"] = 3 * (steps % self.chunk) + k
+            stage[:, k]["pair"] = uid[:, k] % self.slots
             stage[:, k]["form"] = L.JT_BLEND_WEIGHTED
-            stage[:, k]["wa"] = scales.reshape(n_steps, 3)[:, k]
+            stage[:, k]["wa"] = scales[uid[:, k]]
             stage[:, k]["wb"] = 0.0
         dev = sched_dev.device
         self.sched = torch.from_numpy(stage.reshape(-1).view(np.int32).reshape(-1, 8).copy()).to(dev)
@@ -659,12 +675,12 @@ class _StageFields:
         g0 = field._cgrid
         nodes = int(g0.pair_stride)
         rec = 4 if self.f32 else 8                                           # float32 words per node
-        self.buf = torch.empty(3 * self.chunk * nodes * rec, dtype=torch.float32, device=dev)
+        self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
         self.nodes, self.rec = nodes, rec
         g = L.GridField()
         C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
         g.storage = self.out_storage
-        g.n_pairs = 3 * self.chunk
+        g.n_pairs = self.slots
         g.pair_stride = nodes
         g.pairs = self.buf.data_ptr()
         self.grid = g
@@ -674,20 +690,59 @@ class _StageFields:
     def prepare(self, s: int, stop: int) -> int:
         """Blend the fields of steps [s, stop) into their slots; returns the
         number of kernels launched."""
-        launched = 0
         stream = L.stream_ptr()
-        while s < stop:
-            first = s % self.chunk
-            run = min(stop - s, self.chunk - first)
-            ent = self.src.data_ptr() + 3 * s * 32
-            sc = self.scales.data_ptr() + 3 * s * 4
-            out = self.buf.data_ptr() + 3 * first * self.nodes * self.rec * 4
+        runs, self.ready = _stage_plan(self.uid, s, stop, self.ready, self.slots)
+        for lo, run in runs:
+            ent = self.src.data_ptr() + lo * 32
+            sc = self.scales.data_ptr() + lo * 4
+            out = self.buf.data_ptr() + (lo % self.slots) * self.nodes * self.rec * 4
             L.check(self.lib.jt_stage_fields(C.byref(self.src_field), C.c_void_p(ent),
-                                             C.c_void_p(None if self.f32 else sc), 3 * run, self.out_storage,
+                                             C.c_void_p(None if self.f32 else sc), run, self.out_storage,
                                              C.c_void_p(out), stream))
-            launched += 1
-            s += run
-        return launched
+        return len(runs)
+
+
+def _stage_numbers(entries) -> np.ndarray:
+    """Run-ordered numbers of blend entries: an entry whose bytes equal the
+    previous entry's takes its number, any other the next one."""
+    raw = np.ascontiguousarray(entries).view(np.uint8).reshape(len(entries), -1)
+    new = np.ones(len(entries), dtype=np.int64)
+    if len(entries) > 1:
+        new[1:] = np.any(raw[1:] != raw[:-1], axis=1)
+    new[0] = 0
+    return np.cumsum(new)
+
+
+def _stage_chunk(chunk: int, n_steps: int, nodes: int, rec_bytes: int, free_bytes: int) -> int:
+    """Steps per stage-field chunk: the requested chunk, shortened so that the
+    ring (3 fields per step, ``rec_bytes`` per node) takes at most a quarter
+    of the free device memory; 0 (gather snapshot pairs instead) when fewer
+    than 4 steps would fit."""
+    chunk = max(1, min(int(chunk), int(n_steps)))
+    fit = (free_bytes // 4) // max(1, 3 * nodes * rec_bytes)
+    chunk = min(chunk, int(fit))
+    return chunk if chunk >= min(4, n_steps) and chunk > 0 else 0
+
+
+def _stage_plan(uid: np.ndarray, s: int, stop: int, ready: int, slots: int):
+    """Blend launches that put every field of steps [s, stop) in its slot.
+
+    Returns ([(first number, count), ...], new ``ready``).  Numbers up to
+    ``ready`` were blended by earlier launches in order; the last ``slots`` of
+    them are still in the ring, so a range that starts at or before ``ready``
+    only needs the numbers after it.  A range that wraps the ring is split.
+    """
+    lo, hi = int(uid[3 * s]), int(uid[3 * stop - 1]) + 1
+    if hi - lo > slots:
+        raise ValueError("a tracking launch spans more stage fields than the ring holds")
+    if lo <= ready < hi:
+        lo = ready + 1
+    runs = []
+    while lo < hi:
+        run = min(hi - lo, slots - lo % slots)
+        runs.append((lo, run))
+        lo += run
+    return runs, hi - 1
 
 
 def _stage_scales(src) -> np.ndarray:

@@ -168,6 +168,16 @@ def test_new_entry_points_validate_before_touching_the_device():
     with pytest.raises(NotImplementedError, match="float32 stage fields"):
         L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(16), None))
     assert lib.jt_stage_fields(C.byref(f), None, None, 0, L.JT_STORE_STAGE_F32, None, None) == 0
+    # grid shapes the kernels index safely: axes of at most 2^24 nodes, < 2^31 nodes in all
+    g.storage = L.JT_STORE_F32
+    for shape in ((1 << 24) + 1, 1, 1), (2048, 2048, 1024), (0, 4, 4):
+        g.nx, g.ny, g.nz = shape
+        g.pair_stride = max(1, shape[0] * shape[1] * shape[2])
+        with pytest.raises(ValueError, match="grid"):
+            L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(16),
+                                        None))
+    g.nx = g.ny = g.nz = 4
+    g.pair_stride = 64
     # adjoint workspace: three float4 accumulators per step and node
     assert lib.jt_adjoint_workspace_bytes(1000, 50) == 3 * 50 * 1000 * 16
     assert lib.jt_adjoint_workspace_bytes(1000, 65) == 0

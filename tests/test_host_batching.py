@@ -93,3 +93,74 @@ def test_autotuner_cache_file_roundtrip(tmp_path):
     t._save()
     assert json.loads(p.read_text())["k"]["sort_bits"] == 6
     assert A.Autotuner(cache_path=str(p)).cache["k"]["block_size"] == 128
+
+
+def test_stage_field_numbers_share_equal_consecutive_entries():
+    from jaxtrace_gb300 import _lib as L
+    from jaxtrace_gb300.schedule import build_schedule
+    from jaxtrace_gb300.tracker import _stage_numbers
+    times = np.linspace(0, 2, 1001, dtype=F32)
+    sched = build_schedule(times[:-1], F32(0.002), L.JT_RK4, np.linspace(0, 2, 64).astype(F32))
+    every = sched.reshape(-1, 4)[:, :3].reshape(-1)
+    uid = _stage_numbers(every)
+    assert uid[0] == 0 and np.all(np.diff(uid) >= 0) and np.all(np.diff(uid) <= 1)
+    # equal numbers <=> equal bytes, and only between neighbours
+    same = np.diff(uid) == 0
+    raw = every.view(np.uint8).reshape(len(every), -1)
+    assert np.array_equal(same, np.all(raw[1:] == raw[:-1], axis=1))
+    # t + h of a step and t of the next coincide on most steps of this float32 time grid
+    assert 0.6 < same.mean() * 3 < 0.9
+    # t and t + h/2 never coincide here (they bracket different times)
+    assert not np.any(same[0::3])
+
+
+@pytest.mark.parametrize("chunk", [1, 2, 5, 32])
+def test_stage_field_ring_holds_every_field_of_each_launch(chunk):
+    """Simulate the slot ring: before each tracking launch, every stage field
+    of its steps sits in its slot, for launches cut by chunks and sort
+    intervals, with coincident and constant-extrapolation entries."""
+    from jaxtrace_gb300.tracker import _stage_numbers, _stage_plan
+    from jaxtrace_gb300.schedule import BLEND_DTYPE
+    rng = np.random.default_rng(5)
+    n_steps = 97
+    ent = np.zeros(3 * n_steps, dtype=BLEND_DTYPE)
+    ent["wa"] = rng.uniform(size=len(ent)).astype(F32)
+    for i in range(1, len(ent)):                      # coincidences of both kinds, and long constant runs
+        if (i % 3 == 0 and rng.uniform() < 0.7) or i > 250:
+            ent[i] = ent[i - 1]
+    uid = _stage_numbers(ent)
+    slots = 3 * chunk
+    ring = np.full(slots, -1)
+    ready = -1
+    for sort_every in (0, 7, 10):
+        s = 0
+        ring[:] = -1
+        ready = -1
+        while s < n_steps:
+            stop = n_steps
+            if sort_every:
+                stop = min(stop, (s // sort_every + 1) * sort_every)
+            stop = min(stop, s + chunk)
+            runs, ready = _stage_plan(uid, s, stop, ready, slots)
+            for lo, run in runs:
+                assert (lo % slots) + run <= slots
+                ring[np.arange(lo, lo + run) % slots] = np.arange(lo, lo + run)
+            need = uid[3 * s:3 * stop]
+            assert np.array_equal(ring[need % slots], need)
+            s = stop
+    with pytest.raises(ValueError):
+        _stage_plan(np.arange(30), 0, 10, -1, 9)   # 30 numbers cannot fit 9 slots
+
+
+def test_stage_chunk_fits_a_quarter_of_free_memory():
+    from jaxtrace_gb300.tracker import _stage_chunk
+    nodes = 128 ** 3
+    # 128^3 float16 quads: 3 x 67 MB per step; 100 GB free holds the full 32-step ring
+    assert _stage_chunk(32, 1000, nodes, 32, 100 << 30) == 32
+    # 8 GB free: 2 GB for the ring -> 10 steps
+    assert _stage_chunk(32, 1000, nodes, 32, 8 << 30) == 10
+    # too little room for 4 steps: gather snapshot pairs instead
+    assert _stage_chunk(32, 1000, nodes, 32, 2 << 30) == 0
+    # short runs keep a chunk of their own length
+    assert _stage_chunk(32, 3, nodes, 16, 100 << 30) == 3
+    assert _stage_chunk(32, 1, 8, 16, 1 << 20) == 1
