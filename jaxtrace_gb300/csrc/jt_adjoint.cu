@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kBlock, JT_ADJOINT_MIN_BLOCKS)
     FS.storage = JT_STORE_STAGE_F32;
     FS.pairs = P.stage;
     FS.n_pairs = 3 * (P.step_end - P.step_begin);
-    const StageGridField<true, JT_STORE_STAGE_F32> fs{FS};
+    const StageGridField<true, JT_STORE_STAGE_F32> fs = StageGridField<true, JT_STORE_STAGE_F32>::create(FS, 0);
     const float4* stage4 = reinterpret_cast<const float4*>(P.stage);
     typedef Ar<true> A;
     const int nseg = P.step_end - P.step_begin;

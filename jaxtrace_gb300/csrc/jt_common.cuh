@@ -301,20 +301,44 @@ __device__ __forceinline__ float nearest_lattice(const float* g, int n, float c)
     return __ldg(g + best);
 }
 
+// The continuous inlet's bounds in its own frame: the flow axis a and the two
+// others o0 < o1 (o0 = a == 0 ? 1 : 0, o1 = a == 2 ? 1 : 2), with the mirror
+// offsets 2*lo and 2*hi (exact in float32).  Built once per launch on the host
+// so that the kernel reads them as launch constants instead of selecting them
+// by a run-time axis at every step.
+struct InletFrame {
+    float amin, amax, lo0, hi0, lo1, hi1, lo0x2, hi0x2, lo1x2, hi1x2;
+};
+
+__host__ __device__ inline InletFrame inlet_frame(const jt_boundary& B) {
+    const int a = B.inlet_axis;
+    const int o0 = a == 0 ? 1 : 0, o1 = a == 2 ? 1 : 2;
+    const int aa = a == 0 ? 0 : (a == 1 ? 1 : 2);
+    InletFrame I;
+    I.amin = B.lo[aa];
+    I.amax = B.hi[aa];
+    I.lo0 = B.lo[o0];
+    I.hi0 = B.hi[o0];
+    I.lo1 = B.lo[o1];
+    I.hi1 = B.hi[o1];
+    I.lo0x2 = 2.0f * I.lo0;
+    I.hi0x2 = 2.0f * I.hi0;
+    I.lo1x2 = 2.0f * I.lo1;
+    I.hi1x2 = 2.0f * I.hi1;
+    return I;
+}
+
 // Continuous inlet with grid-preserving replacement (boundary.py:1517-1599).
 template <bool EXACT>
-__device__ __forceinline__ void bc_inlet(const jt_boundary& B, float& x, float& y, float& z) {
+__device__ __forceinline__ void bc_inlet(const jt_boundary& B, const InletFrame& I, float& x, float& y, float& z) {
     typedef Ar<EXACT> A;
-    // The flow axis a and the two others o0 < o1, picked with selects so that
-    // nothing is indexed by a run-time axis (no local-memory copy of B).
+    // the particle's coordinates in the inlet frame, picked with selects so
+    // that nothing is indexed by a run-time axis (no local-memory copy of B)
     const int a = B.inlet_axis;
     float fa = a == 0 ? x : (a == 1 ? y : z);
-    float u0 = a == 0 ? y : x;  // axis o0 = (a == 0 ? 1 : 0)
-    float u1 = a == 2 ? y : z;  // axis o1 = (a == 2 ? 1 : 2)
-    const float amin = a == 0 ? B.lo[0] : (a == 1 ? B.lo[1] : B.lo[2]);
-    const float amax = a == 0 ? B.hi[0] : (a == 1 ? B.hi[1] : B.hi[2]);
-    const float lo0 = a == 0 ? B.lo[1] : B.lo[0], hi0 = a == 0 ? B.hi[1] : B.hi[0];
-    const float lo1 = a == 2 ? B.lo[1] : B.lo[2], hi1 = a == 2 ? B.hi[1] : B.hi[2];
+    float u0 = a == 0 ? y : x;
+    float u1 = a == 2 ? y : z;
+    const float amin = I.amin, amax = I.amax, lo0 = I.lo0, hi0 = I.hi0, lo1 = I.lo1, hi1 = I.hi1;
     const bool exited = B.inlet_positive ? (fa > amax) : (fa < amin);
     if (exited && B.inlet_mode == JT_INLET_GRID) {
         const float g0 = nearest_lattice(B.inlet_coords[0], B.inlet_res[0], u0);
@@ -329,11 +353,11 @@ __device__ __forceinline__ void bc_inlet(const jt_boundary& B, float& x, float& 
     } else {
         if (fa > amax) fa = B.inlet_nudge;
     }
-    // boundary.py:1590-1597  one mirror on the other axes
-    if (u0 < lo0) u0 = A::sub(A::mul(2.0f, lo0), u0);
-    else if (u0 > hi0) u0 = A::sub(A::mul(2.0f, hi0), u0);
-    if (u1 < lo1) u1 = A::sub(A::mul(2.0f, lo1), u1);
-    else if (u1 > hi1) u1 = A::sub(A::mul(2.0f, hi1), u1);
+    // boundary.py:1590-1597  one mirror on the other axes (2*lo - u, 2*hi - u)
+    if (u0 < lo0) u0 = A::sub(I.lo0x2, u0);
+    else if (u0 > hi0) u0 = A::sub(I.hi0x2, u0);
+    if (u1 < lo1) u1 = A::sub(I.lo1x2, u1);
+    else if (u1 > hi1) u1 = A::sub(I.hi1x2, u1);
     if (a == 0) {
         x = fa; y = u0; z = u1;
     } else if (a == 1) {
@@ -344,9 +368,10 @@ __device__ __forceinline__ void bc_inlet(const jt_boundary& B, float& x, float& 
 }
 
 template <bool EXACT>
-__device__ __forceinline__ void apply_boundary(const jt_boundary& B, float& x, float& y, float& z) {
+__device__ __forceinline__ void apply_boundary(const jt_boundary& B, const InletFrame& I, float& x, float& y,
+                                               float& z) {
     if (B.inlet_mode != JT_INLET_OFF) {
-        bc_inlet<EXACT>(B, x, y, z);
+        bc_inlet<EXACT>(B, I, x, y, z);
         return;
     }
     if (B.absorbing_joint) {
@@ -359,6 +384,11 @@ __device__ __forceinline__ void apply_boundary(const jt_boundary& B, float& x, f
     x = bc_axis<EXACT>(B.axis_kind[0], x, B.lo[0], B.hi[0], B.outside_value);
     y = bc_axis<EXACT>(B.axis_kind[1], y, B.lo[1], B.hi[1], B.outside_value);
     z = bc_axis<EXACT>(B.axis_kind[2], z, B.lo[2], B.hi[2], B.outside_value);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ void apply_boundary(const jt_boundary& B, float& x, float& y, float& z) {
+    apply_boundary<EXACT>(B, inlet_frame(B), x, y, z);
 }
 
 // ---------------------------------------------------------------------------
@@ -483,7 +513,7 @@ __device__ __forceinline__ int find_ensemble(const int32_t* off, int n_ens, int 
 // Persistent tracking kernel body: one particle per thread, the time loop in
 // registers, boundary fused after every step, optional strided recording.
 template <bool EXACT, int INTEG, class Field>
-__device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
+__device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B, const InletFrame& I,
                                            const jt_track_params& P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n_particles) return;
@@ -507,7 +537,7 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
         const jt_blend* e = sched + 4 * (int64_t)s;
         if (comp) integrate<EXACT, INTEG, true>(f, e, k, x, c, flags);
         else integrate<EXACT, INTEG, false>(f, e, k, x, c, flags);
-        apply_boundary<EXACT>(B, x.x, x.y, x.z);
+        apply_boundary<EXACT>(B, I, x.x, x.y, x.z);
         if (P.traj != nullptr) {
             const int cnt = s + 1;
             if (cnt % P.record_every == 0) {

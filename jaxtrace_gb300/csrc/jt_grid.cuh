@@ -39,7 +39,10 @@ __device__ __forceinline__ void grid_axis(float x, float org, float d, float inv
     } else {
         valid = (x >= org) && (x <= vhi);  // structured.py:299-302
         const float hi = (float)(n > 1 ? n - 1 : 0);
-        f = np_clip(f, 0.0f, hi);          // np.clip(fx, 0, max(Nx-1,0))
+        // np.clip(fx, 0, max(Nx-1,0)); the fast modes clip with min/max, which
+        // send NaN to cell 0 instead of carrying it in the weight (the
+        // particle's position stays NaN either way)
+        f = EXACT ? np_clip(f, 0.0f, hi) : fminf(fmaxf(f, 0.0f), hi);
         const float fl = floorf(f);
         // fl is an integer in [0, n-1] (n <= 2^24, so n-1 is exact), or NaN,
         // which converts to 0: the cell is always in range
@@ -113,6 +116,11 @@ __device__ __forceinline__ V3 trilinear_lerp(const CV& v000, const CV& v100, con
     return V3{rxy.x, rxy.y, fmaf(wz, cz.y - cz.x, cz.x)};
 }
 
+// One 32-byte float16 yz-quad record.
+struct alignas(32) Quad32 {
+    uint4 lo, hi;
+};
+
 __device__ __forceinline__ float2 h2f2(uint32_t w) { return __half22float2(*reinterpret_cast<const __half2*>(&w)); }
 
 template <bool EXACT, int STORE>
@@ -185,7 +193,7 @@ struct GridField {
 //     256-bit loads per evaluation measured faster than eight 64-bit loads of
 //     float16 node records, although those fit L2 and the quads do not.
 #ifndef JT_STAGE16_MIN_BLOCKS
-#define JT_STAGE16_MIN_BLOCKS 6
+#define JT_STAGE16_MIN_BLOCKS 5
 #endif
 
 //
@@ -196,17 +204,19 @@ struct GridField {
 // lerp form.
 template <bool EXACT, int OUT, int MODE = -1>
 struct StageGridField {
-    // float16 quads fit 6 blocks of 256 (no spills), which hides more of the
-    // stage fields' latency; float32 records take 64 registers at 4
+    // float16 quads at 5 blocks of 256 (48 registers, no spills; 1 % faster
+    // than 6 blocks at 40 registers with spills); float32 records take 64
+    // registers at 4
     static constexpr int kMinBlocks = OUT == JT_STORE_STAGE_F16 ? JT_STAGE16_MIN_BLOCKS : 4;
     // the evaluation is short enough that the kernel is bound by instruction
     // issue: unrolled stages drop the loop's own instructions
     static constexpr bool kUnrollStages = true;
     jt_grid_field F;
     float nofs[3];  // -origin * inv_spacing per axis (fast arithmetic)
+    int sx;         // node stride of the x axis, ny * nz
 
-    static StageGridField create(const jt_grid_field& d, int) {
-        StageGridField s{d, {0.0f, 0.0f, 0.0f}};
+    __host__ __device__ static StageGridField create(const jt_grid_field& d, int) {
+        StageGridField s{d, {0.0f, 0.0f, 0.0f}, d.ny * d.nz};
         for (int a = 0; a < 3; ++a) s.nofs[a] = -d.origin[a] * d.inv_spacing[a];
         return s;
     }
@@ -224,17 +234,20 @@ struct StageGridField {
                                  k1, wz, vz, flags, nofs[2]);
         const int slot = min(max(e.pair, 0), F.n_pairs - 1);
         const int64_t base = (int64_t)slot * F.pair_stride;
-        const int ny = F.ny, nz = F.nz;
-        const int r00 = (i0 * ny + j0) * nz, r10 = (i1 * ny + j0) * nz;
+        // 32-bit node offsets within the slot (fewer than 2^31 nodes), scaled
+        // to bytes by the wide multiply-add of the address
+        const int nz = F.nz;
+        const int n000 = i0 * sx + (j0 * nz + k0);
+        const int n100 = n000 + (i1 - i0) * sx;
         CV v000, v100, v010, v110, v001, v101, v011, v111;
         V3 r;
         if (OUT == JT_STORE_STAGE_F32) {
-            const int r01 = (i0 * ny + j1) * nz, r11 = (i1 * ny + j1) * nz;
+            const int dy = (j1 - j0) * nz, dz = k1 - k0;
             const float4* b4 = reinterpret_cast<const float4*>(F.pairs) + base;
-            const float4 a000 = __ldg(b4 + r00 + k0), a100 = __ldg(b4 + r10 + k0);
-            const float4 a010 = __ldg(b4 + r01 + k0), a110 = __ldg(b4 + r11 + k0);
-            const float4 a001 = __ldg(b4 + r00 + k1), a101 = __ldg(b4 + r10 + k1);
-            const float4 a011 = __ldg(b4 + r01 + k1), a111 = __ldg(b4 + r11 + k1);
+            const float4 a000 = __ldg(b4 + n000), a100 = __ldg(b4 + n100);
+            const float4 a010 = __ldg(b4 + (n000 + dy)), a110 = __ldg(b4 + (n100 + dy));
+            const float4 a001 = __ldg(b4 + (n000 + dz)), a101 = __ldg(b4 + (n100 + dz));
+            const float4 a011 = __ldg(b4 + (n000 + dy + dz)), a111 = __ldg(b4 + (n100 + dy + dz));
             v000 = CV{make_float2(a000.x, a000.y), a000.z}; v100 = CV{make_float2(a100.x, a100.y), a100.z};
             v010 = CV{make_float2(a010.x, a010.y), a010.z}; v110 = CV{make_float2(a110.x, a110.y), a110.z};
             v001 = CV{make_float2(a001.x, a001.y), a001.z}; v101 = CV{make_float2(a101.x, a101.y), a101.z};
@@ -243,8 +256,9 @@ struct StageGridField {
                       : trilinear_lerp(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
         } else {
             uint32_t q0[8], q1[8];
-            ldg256(reinterpret_cast<const uint4*>(F.pairs) + 2 * (base + r00 + k0), q0);
-            ldg256(reinterpret_cast<const uint4*>(F.pairs) + 2 * (base + r10 + k0), q1);
+            const Quad32* bq = reinterpret_cast<const Quad32*>(F.pairs) + base;
+            ldg256(bq + n000, q0);
+            ldg256(bq + n100, q1);
             const float2 z0a = h2f2(q0[4]), z0b = h2f2(q0[5]), z1a = h2f2(q1[4]), z1b = h2f2(q1[5]);
             v000 = CV{h2f2(q0[0]), z0a.x}; v001 = CV{h2f2(q0[1]), z0a.y};
             v010 = CV{h2f2(q0[2]), z0b.x}; v011 = CV{h2f2(q0[3]), z0b.y};

@@ -30,8 +30,9 @@ struct MinBlocksOf<F, decltype(void(F::kMinBlocks))> {
 };
 
 template <bool EXACT, int INTEG, class Field>
-__global__ void __launch_bounds__(kBlock, MinBlocksOf<Field>::value) k_track(Field f, jt_boundary B, jt_track_params P) {
-    track_body<EXACT, INTEG>(f, B, P);
+__global__ void __launch_bounds__(kBlock, MinBlocksOf<Field>::value)
+    k_track(Field f, jt_boundary B, InletFrame I, jt_track_params P) {
+    track_body<EXACT, INTEG>(f, B, I, P);
 }
 
 // Field evaluation at M points with one blend: sample_at_positions(pos, t).
@@ -96,10 +97,11 @@ struct Launcher {
         // block_size was validated to 0, 64, 128 or 256 (<= kBlock, the launch bound)
         const int bs = P.block_size > 0 ? P.block_size : kBlock;
         const unsigned g = (unsigned)((P.n_particles + bs - 1) / bs);
+        const InletFrame I = inlet_frame(B);
         switch (P.integrator) {
-            case JT_EULER: k_track<EXACT, JT_EULER><<<g, bs, 0, st>>>(f, B, P); break;
-            case JT_RK2: k_track<EXACT, JT_RK2><<<g, bs, 0, st>>>(f, B, P); break;
-            default: k_track<EXACT, JT_RK4><<<g, bs, 0, st>>>(f, B, P); break;
+            case JT_EULER: k_track<EXACT, JT_EULER><<<g, bs, 0, st>>>(f, B, I, P); break;
+            case JT_RK2: k_track<EXACT, JT_RK2><<<g, bs, 0, st>>>(f, B, I, P); break;
+            default: k_track<EXACT, JT_RK4><<<g, bs, 0, st>>>(f, B, I, P); break;
         }
         return cudaGetLastError();
     }
