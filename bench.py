@@ -68,6 +68,9 @@ def args_parse():
     p.add_argument("--sort-every", type=int, default=None, help="locality re-sort interval (default: automatic)")
     p.add_argument("--sort-bits", type=int, default=None, help="cells per axis of the re-sort as 2^bits (default 7)")
     p.add_argument("--block-size", type=int, default=0, help="tracking kernel threads per block (0: 256)")
+    p.add_argument("--stage-chunk", type=int, default=32, help="steps per stage-field chunk")
+    p.add_argument("--no-stage-overlap", action="store_true",
+                   help="blend each chunk's stage fields before its launch instead of during the previous one")
     p.add_argument("--grid", type=int, default=128)
     p.add_argument("--no-error", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -605,7 +608,8 @@ def main():
     for v in variants:
         field = jt.StructuredTimeSeriesField(case["data"], case["times"], g, g, g, "clamp", storage=v)
         tr = jt.create_tracker("rk4", field, bc, record_final_only=True, sort_every=a.sort_every,
-                               sort_bits=a.sort_bits, block_size=a.block_size)
+                               sort_bits=a.sort_bits, block_size=a.block_size, stage_chunk=a.stage_chunk,
+                               stage_overlap=not a.no_stage_overlap)
         trackers[v] = tr
         sched = torch.from_numpy(tr._schedule(times, case["dt"]).view(np.int32).reshape(-1, 8)).cuda()
         status = torch.zeros(1, dtype=torch.int32, device="cuda")

@@ -34,15 +34,24 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(jt_grid_field F, const jt_
     }
 }
 
+__device__ __forceinline__ CV scale_cv(CV c, float s) {
+    return CV{make_float2(c.xy.x * s, c.xy.y * s), c.z * s};
+}
+
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
     const __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
 // 16-bit yz-quad pairs -> float16 yz-quads of the blended values divided by
-// the entry's power-of-two scale.
+// the entry's power-of-two scale.  Blocks of 64 threads at <= 64 registers
+// (4,096 per block): one fits beside five blocks of the float16 tracking
+// kernel (5 x 256 threads x 48 registers), so the next chunk's fields are
+// blended on a side stream while the current chunk is tracked.
+constexpr int kStageBlock16 = 64;
+
 template <int STORE>
-__global__ void __launch_bounds__(kBlock) k_stage_f16(jt_grid_field F, const jt_blend* __restrict__ ent,
+__global__ void __launch_bounds__(kStageBlock16, 16) k_stage_f16(jt_grid_field F, const jt_blend* __restrict__ ent,
                                                        const float* __restrict__ scales, int n,
                                                        uint4* __restrict__ out) {
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,18 +67,30 @@ __global__ void __launch_bounds__(kBlock) k_stage_f16(jt_grid_field F, const jt_
             load_quad<STORE>(F.pairs, part_b, (int64_t)pr * N + node, p00, p01, p10, p11);
             cur = pr;
         }
-        const bool w = e.form == JT_BLEND_WEIGHTED;
-        const float2 WA = splat(e.wa), WB = splat(e.wb);
-        const CV c00 = blend_cv<false, STORE>(p00, e, WA, WB, w), c01 = blend_cv<false, STORE>(p01, e, WA, WB, w);
-        const CV c10 = blend_cv<false, STORE>(p10, e, WA, WB, w), c11 = blend_cv<false, STORE>(p11, e, WA, WB, w);
-        const float inv = 1.0f / __ldg(scales + j);  // a power of two: exact
+        // the scale is a power of two, so dividing by it is exact and can be
+        // folded into the weights of the common (weighted) form
+        const float inv = __frcp_rn(__ldg(scales + j));
+        CV c00, c01, c10, c11;
+        if (e.form == JT_BLEND_WEIGHTED) {
+            const float2 WA = splat(e.wa * inv), WB = splat(e.wb * inv);
+            c00 = blend_cv<false, STORE>(p00, e, WA, WB, true);
+            c01 = blend_cv<false, STORE>(p01, e, WA, WB, true);
+            c10 = blend_cv<false, STORE>(p10, e, WA, WB, true);
+            c11 = blend_cv<false, STORE>(p11, e, WA, WB, true);
+        } else {
+            const float2 WA = splat(e.wa), WB = splat(e.wb);
+            c00 = scale_cv(blend_cv<false, STORE>(p00, e, WA, WB, false), inv);
+            c01 = scale_cv(blend_cv<false, STORE>(p01, e, WA, WB, false), inv);
+            c10 = scale_cv(blend_cv<false, STORE>(p10, e, WA, WB, false), inv);
+            c11 = scale_cv(blend_cv<false, STORE>(p11, e, WA, WB, false), inv);
+        }
         uint4 a, b;
-        a.x = pack_h2(c00.xy.x * inv, c00.xy.y * inv);
-        a.y = pack_h2(c01.xy.x * inv, c01.xy.y * inv);
-        a.z = pack_h2(c10.xy.x * inv, c10.xy.y * inv);
-        a.w = pack_h2(c11.xy.x * inv, c11.xy.y * inv);
-        b.x = pack_h2(c00.z * inv, c01.z * inv);
-        b.y = pack_h2(c10.z * inv, c11.z * inv);
+        a.x = pack_h2(c00.xy.x, c00.xy.y);
+        a.y = pack_h2(c01.xy.x, c01.xy.y);
+        a.z = pack_h2(c10.xy.x, c10.xy.y);
+        a.w = pack_h2(c11.xy.x, c11.xy.y);
+        b.x = pack_h2(c00.z, c01.z);
+        b.y = pack_h2(c10.z, c11.z);
         b.z = 0u;
         b.w = 0u;
         uint4* o = out + 2 * ((int64_t)j * N + node);
@@ -127,6 +148,7 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     const int64_t N = (int64_t)F.nx * F.ny * F.nz;
     if (F.pair_stride != N) return set_error(JT_ERR_INVALID, "pair_stride must equal the node count");
     const unsigned g = grid_blocks(N);
+    const unsigned g16 = (unsigned)((N + kStageBlock16 - 1) / kStageBlock16);
     cudaStream_t s = (cudaStream_t)stream;
     if (out_storage == JT_STORE_STAGE_F32) {
         if (F.storage != JT_STORE_F32)
@@ -135,9 +157,11 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     } else if (out_storage == JT_STORE_STAGE_F16) {
         if (out_scales == nullptr) return set_error(JT_ERR_INVALID, "float16 stage fields need out_scales");
         if (F.storage == JT_STORE_BF16)
-            k_stage_f16<JT_STORE_BF16><<<g, kBlock, 0, s>>>(F, entries, out_scales, n, reinterpret_cast<uint4*>(out));
+            k_stage_f16<JT_STORE_BF16><<<g16, kStageBlock16, 0, s>>>(F, entries, out_scales, n,
+                                                                     reinterpret_cast<uint4*>(out));
         else if (F.storage == JT_STORE_F16)
-            k_stage_f16<JT_STORE_F16><<<g, kBlock, 0, s>>>(F, entries, out_scales, n, reinterpret_cast<uint4*>(out));
+            k_stage_f16<JT_STORE_F16><<<g16, kStageBlock16, 0, s>>>(F, entries, out_scales, n,
+                                                                    reinterpret_cast<uint4*>(out));
         else
             return set_error(JT_ERR_UNSUPPORTED, "float16 stage fields come from 16-bit snapshots");
     } else {

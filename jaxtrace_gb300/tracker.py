@@ -60,6 +60,8 @@ class TrackerOptions:
                        of a chunk of ``stage_chunk`` steps before the tracking
                        launch, so it gathers one time level (the reference's
                        own order of operations; float32 stays bit-identical)
+    stage_overlap      blend the next chunk's stage fields on a side stream
+                       while the current chunk is tracked (a ring twice as deep)
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -92,6 +94,7 @@ class TrackerOptions:
     cuda_graph: bool = False
     stage_fields: bool = True
     stage_chunk: int = 32
+    stage_overlap: bool = True
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
         """tracker.py:142-153."""
@@ -445,12 +448,13 @@ class _Engine:
             from .fields import StructuredTimeSeriesField
             if isinstance(tracker._field, StructuredTimeSeriesField):
                 f = tracker._field
-                rec_bytes = 16 if f._storage == L.JT_STORE_F32 else 32
+                overlap = bool(tracker.options.stage_overlap)
+                rec_bytes = (16 if f._storage == L.JT_STORE_F32 else 32) * (2 if overlap else 1)
                 free = torch.cuda.mem_get_info(pos.device)[0]
                 chunk = _stage_chunk(int(tracker.options.stage_chunk), n_steps, len(f.grid_x) * len(f.grid_y) * len(f.grid_z),
                                      rec_bytes, free)
                 if chunk > 0:
-                    self.stage = _StageFields(f, sched_dev, n_steps, chunk)
+                    self.stage = _StageFields(f, sched_dev, n_steps, chunk, overlap=overlap)
 
     def _sort(self, first=False):
         src_pos = self.out if first else self.pos
@@ -470,18 +474,25 @@ class _Engine:
         if self.comp is not None:
             self.comp, self.comp_alt = self.comp_alt, self.comp
 
+    def _stop(self, s, e, staged):
+        """End of the launch that starts at step s: the next re-sort, the
+        stage-field chunk, or e."""
+        stop = e
+        if self.sort_every > 0:
+            stop = min(e, (s // self.sort_every + 1) * self.sort_every)
+        if staged:
+            stop = min(stop, s + self.stage.chunk)
+        return stop
+
     def advance(self, s, e, rec):
         """Steps [s, e) with optional recording (slab, vslab, k, compact, row0, rows)."""
         p = self.p
+        staged = self.stage is not None and not (rec is not None and rec[1] is not None)
         while s < e:
-            stop = e
-            if self.sort_every > 0:
-                if s > 0 and s % self.sort_every == 0:
-                    self._sort()
-                stop = min(e, (s // self.sort_every + 1) * self.sort_every)
-            staged = self.stage is not None and not (rec is not None and rec[1] is not None)
+            if self.sort_every > 0 and s > 0 and s % self.sort_every == 0:
+                self._sort()
+            stop = self._stop(s, e, staged)
             if staged:
-                stop = min(stop, s + self.stage.chunk)
                 self.kernels += self.stage.prepare(s, stop)
                 field_c = self.stage.field_c
                 p.schedule = self.stage.sched.data_ptr()
@@ -509,6 +520,8 @@ class _Engine:
                 self.timers.append(ev)
             self.launches += 1
             self.kernels += 1
+            if staged and stop < e:
+                self.kernels += self.stage.prefetch(stop, self._stop(stop, e, staged))
             s = stop
 
     def finish(self):
@@ -632,18 +645,25 @@ class _StageFields:
     2 at t + h) are numbered in order, and an entry equal to the one before it
     (the t + h entry of a step and the t entry of the next, when the float32
     times agree) takes the same number u.  Entry u lives in ring slot
-    u mod (3 * chunk); the entries of a launch of at most ``chunk`` steps span
-    at most 3 * chunk numbers, so ``prepare`` finds room for all of them.
-    Float32 snapshots give float32 node records blended with the exact
-    arithmetic; 16-bit snapshots give float16 yz-quads divided by a
+    u mod R; the entries of a launch of at most ``chunk`` steps span at most
+    3 * chunk numbers, so ``prepare`` finds room for all of them with
+    R = 3 * chunk.  Float32 snapshots give float32 node records blended with
+    the exact arithmetic; 16-bit snapshots give float16 yz-quads divided by a
     power-of-two bound of the blend.
+
+    Overlap (R = 6 * chunk): ``prefetch`` blends the next launch's fields on a
+    side stream while the current launch tracks.  Its writes go to the slots
+    of numbers below the current launch's first (two launches span at most
+    6 * chunk numbers), after the launches before the current one are done
+    (an event recorded just before the current launch).
     """
 
-    def __init__(self, field, sched_dev, n_steps: int, chunk: int):
+    def __init__(self, field, sched_dev, n_steps: int, chunk: int, overlap: bool = False):
         import torch
         from .schedule import BLEND_DTYPE
         self.lib = L.load()
         self.chunk = max(1, min(int(chunk), n_steps))
+        self.overlap = bool(overlap)
         host = np.ascontiguousarray(sched_dev.cpu().numpy()).view(BLEND_DTYPE).reshape(-1)
         n_ent = 4 * n_steps
         host = host[:n_ent].copy()
@@ -652,7 +672,7 @@ class _StageFields:
         first = np.ones(len(every), dtype=bool)
         first[1:] = self.uid[1:] != self.uid[:-1]
         src = every[first]                                                  # one entry per number
-        self.slots = 3 * self.chunk
+        self.slots = (6 if self.overlap else 3) * self.chunk
         self.ready = -1                                                     # last number blended
         self.f32 = field._storage == L.JT_STORE_F32
         self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
@@ -677,6 +697,10 @@ class _StageFields:
         rec = 4 if self.f32 else 8                                           # float32 words per node
         self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
         self.nodes, self.rec = nodes, rec
+        self.side = self.before = self.pending = None
+        if self.overlap:
+            self.side = torch.cuda.Stream(device=dev, priority=-1)
+            self.buf.record_stream(self.side)
         g = L.GridField()
         C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
         g.storage = self.out_storage
@@ -688,9 +712,33 @@ class _StageFields:
         self.src_field = field.jt_field()
 
     def prepare(self, s: int, stop: int) -> int:
-        """Blend the fields of steps [s, stop) into their slots; returns the
-        number of kernels launched."""
-        stream = L.stream_ptr()
+        """Put the fields of steps [s, stop) in their slots before the launch
+        that tracks them: wait for a prefetch, blend what is missing on the
+        current stream.  Returns the number of kernels launched."""
+        import torch
+        cur = torch.cuda.current_stream()
+        if self.pending is not None:
+            cur.wait_event(self.pending)
+            self.pending = None
+        n = self._blend(s, stop, L.stream_ptr())
+        if self.overlap:
+            self.before = torch.cuda.Event()
+            self.before.record(cur)
+        return n
+
+    def prefetch(self, s: int, stop: int) -> int:
+        """Blend the fields of the next launch, steps [s, stop), on the side
+        stream once the launches before the current one are done."""
+        import torch
+        if not self.overlap:
+            return 0
+        self.side.wait_event(self.before)
+        n = self._blend(s, stop, L.stream_ptr(self.side))
+        self.pending = torch.cuda.Event()
+        self.pending.record(self.side)
+        return n
+
+    def _blend(self, s: int, stop: int, stream) -> int:
         runs, self.ready = _stage_plan(self.uid, s, stop, self.ready, self.slots)
         for lo, run in runs:
             ent = self.src.data_ptr() + lo * 32

@@ -114,11 +114,14 @@ def test_stage_field_numbers_share_equal_consecutive_entries():
     assert not np.any(same[0::3])
 
 
+@pytest.mark.parametrize("overlap", [False, True])
 @pytest.mark.parametrize("chunk", [1, 2, 5, 32])
-def test_stage_field_ring_holds_every_field_of_each_launch(chunk):
+def test_stage_field_ring_holds_every_field_of_each_launch(chunk, overlap):
     """Simulate the slot ring: before each tracking launch, every stage field
     of its steps sits in its slot, for launches cut by chunks and sort
-    intervals, with coincident and constant-extrapolation entries."""
+    intervals, with coincident and constant-extrapolation entries.  With
+    overlap, the next launch's fields are written while the current launch
+    runs: none of those writes may land in a slot the current launch reads."""
     from jaxtrace_gb300.tracker import _stage_numbers, _stage_plan
     from jaxtrace_gb300.schedule import BLEND_DTYPE
     rng = np.random.default_rng(5)
@@ -129,24 +132,34 @@ def test_stage_field_ring_holds_every_field_of_each_launch(chunk):
         if (i % 3 == 0 and rng.uniform() < 0.7) or i > 250:
             ent[i] = ent[i - 1]
     uid = _stage_numbers(ent)
-    slots = 3 * chunk
+    slots = (6 if overlap else 3) * chunk
     ring = np.full(slots, -1)
-    ready = -1
+
+    def stop_of(s, sort_every):
+        stop = n_steps
+        if sort_every:
+            stop = min(stop, (s // sort_every + 1) * sort_every)
+        return min(stop, s + chunk)
+
+    def write(runs):
+        for lo, run in runs:
+            assert (lo % slots) + run <= slots
+            ring[np.arange(lo, lo + run) % slots] = np.arange(lo, lo + run)
+
     for sort_every in (0, 7, 10):
         s = 0
         ring[:] = -1
         ready = -1
         while s < n_steps:
-            stop = n_steps
-            if sort_every:
-                stop = min(stop, (s // sort_every + 1) * sort_every)
-            stop = min(stop, s + chunk)
+            stop = stop_of(s, sort_every)
             runs, ready = _stage_plan(uid, s, stop, ready, slots)
-            for lo, run in runs:
-                assert (lo % slots) + run <= slots
-                ring[np.arange(lo, lo + run) % slots] = np.arange(lo, lo + run)
+            write(runs)
             need = uid[3 * s:3 * stop]
             assert np.array_equal(ring[need % slots], need)
+            if overlap and stop < n_steps:        # prefetch while [s, stop) is tracked
+                runs, ready = _stage_plan(uid, stop, stop_of(stop, sort_every), ready, slots)
+                write(runs)
+                assert np.array_equal(ring[need % slots], need)
             s = stop
     with pytest.raises(ValueError):
         _stage_plan(np.arange(30), 0, 10, -1, 9)   # 30 numbers cannot fit 9 slots
