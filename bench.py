@@ -39,20 +39,25 @@ UNIT = "particle-steps/s"
 BYTES_PER_PSTEP = {"f32": 4 * 8 * 12 + 24, "bf16": 4 * 8 * 6 + 24, "f16": 4 * 8 * 6 + 24}
 
 
-def traffic_per_pstep(storage):
-    """DRAM bytes per particle-step of k_track from the committed ncu summary
-    (profiles/k_track_precision.md, line 'dram_bytes_per_particle_step <storage> <value>')."""
+def profile_figure(key, storage):
+    """A figure of the committed ncu summary of k_track
+    (profiles/k_track_precision.md, line '<key> <storage> <value>')."""
     f = ROOT / "profiles" / "k_track_precision.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
         parts = line.replace("|", " ").split()
-        if len(parts) >= 3 and parts[0] == "dram_bytes_per_particle_step" and parts[1] == storage:
+        if len(parts) >= 3 and parts[0] == key and parts[1] == storage:
             try:
                 return float(parts[2])
             except ValueError:
                 return None
     return None
+
+
+def traffic_per_pstep(storage):
+    """DRAM bytes per particle-step of k_track (ncu, full size)."""
+    return profile_figure("dram_bytes_per_particle_step", storage)
 
 
 def args_parse():
@@ -666,6 +671,15 @@ def main():
                                   "kernel": "k_track (RK4, grid field, %s)" % v,
                                   "launch_ms": per_launch_ms, "particle_steps_per_launch": units_per_launch,
                                   "bytes_per_particle_step": bpp}
+        wi = profile_figure("warp_inst_per_warp_step", v)
+        if wi is not None:
+            # instruction issue: the ncu count of warp instructions per particle-step
+            # against one warp instruction per cycle on each of the SMs' schedulers
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            results[v]["roofline"]["issue"] = {
+                "warp_inst_per_particle_step": wi / 32.0,
+                "achieved": units_per_launch * wi / 32.0 / (per_launch_ms / 1e3),
+                "peak_per_mhz": sms * 4 * 1e6, "unit": "warp-inst/s", "schedulers": sms * 4}
         finals[v] = pos.cpu().numpy()
         del field
         if a.profile:
@@ -722,6 +736,12 @@ def main():
                        "api": "create_tracker('rk4', field, continuous_inlet, record_final_only=True)"
                               ".track_particles(pinned host x0)"}
     line["clocks"] = clk.summary()
+    iss = line.get("roofline", {}).get("issue")
+    if iss is not None:
+        mhz = line["clocks"].get("sm_mhz") or 2070.0
+        iss["peak"] = iss.pop("peak_per_mhz") * mhz
+        iss["frac"] = iss["achieved"] / iss["peak"]
+        iss["clock_mhz"] = mhz
     if not a.profile and rank == 0:
         del trackers
         torch.cuda.empty_cache()
