@@ -764,12 +764,13 @@ def _stage_numbers(entries) -> np.ndarray:
 def _stage_chunk(chunk: int, n_steps: int, nodes: int, rec_bytes: int, free_bytes: int) -> int:
     """Steps per stage-field chunk: the requested chunk, shortened so that the
     ring (3 fields per step, ``rec_bytes`` per node) takes at most a quarter
-    of the free device memory; 0 (gather snapshot pairs instead) when fewer
-    than 4 steps would fit."""
-    chunk = max(1, min(int(chunk), int(n_steps)))
-    fit = (free_bytes // 4) // max(1, 3 * nodes * rec_bytes)
-    chunk = min(chunk, int(fit))
-    return chunk if chunk >= min(4, n_steps) and chunk > 0 else 0
+    of the free device memory; 0 (gather snapshot pairs instead) when the
+    memory shortens it below 4 steps."""
+    want = max(1, min(int(chunk), int(n_steps)))
+    fit = int((free_bytes // 4) // max(1, 3 * nodes * rec_bytes))
+    if fit >= want:
+        return want
+    return fit if fit >= 4 else 0
 
 
 def _stage_plan(uid: np.ndarray, s: int, stop: int, ready: int, slots: int):

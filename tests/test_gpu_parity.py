@@ -53,6 +53,34 @@ def test_nearest_field(golden):
         assert np.mean(np.all(out == g["outs"][i], axis=1)) > 0.99
 
 
+def test_nearest_node_search_matches_brute_force_argmin_with_ties():
+    """The cell-list search (row ranges, pruned first ring, ring stop) returns
+    np.argmin of the float32 squared distances, lowest index on ties: lattice
+    nodes make exact ties at cell centres, faces and edges; queries sit on
+    nodes, on cell faces, far outside and at random."""
+    g = np.arange(9, dtype=F32) / F32(8)
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(11)
+    nodes = np.concatenate([lat, rng.random((300, 3)).astype(F32)]).astype(F32)
+    n = len(nodes)
+    data = np.zeros((2, n, 3), dtype=F32)
+    data[:, :, 0] = np.arange(n, dtype=F32)
+    f = jt.TimeSeriesField(data, np.array([0.0, 1.0], dtype=F32), nodes)
+    half = (np.arange(8, dtype=F32) + F32(0.5)) / F32(8)
+    mids = np.stack(np.meshgrid(half, half, half, indexing="ij"), -1).reshape(-1, 3)
+    faces = mids.copy()
+    faces[:, 0] = np.round(faces[:, 0] * 8) / 8
+    q = np.concatenate([mids, faces, lat[::7], rng.random((4000, 3)), rng.uniform(-2, 3, (500, 3)),
+                        lat[::11] + F32(1e-7)]).astype(F32)
+    out = f.sample_at_positions(q, 0.0)[:, 0].astype(np.int64)
+    d = np.zeros((len(q), n), dtype=F32)
+    for a in range(3):
+        diff = (q[:, None, a] - nodes[None, :, a]).astype(F32)
+        d = (d + diff * diff).astype(F32) if a else (diff * diff).astype(F32)
+    ref = np.argmin(d, axis=1)
+    assert np.array_equal(out, ref)
+
+
 # ---------------------------------------------------------------- boundaries
 def _bc(name, B):
     conc = {"x": 9, "y": 17, "z": 5}
@@ -272,6 +300,24 @@ def test_stage_fields_float32_bit_identical_to_pair_gathers(mode, sort_every):
     obc = oracle.BoundarySpec(kinds=(("periodic",) if mode == "periodic" else ("reflective",)) * 3)
     ref, _, _ = oracle.track(spec, obc, x0, np.linspace(0.0, 0.23, 24, dtype=F32), 0.01)
     assert same(outs[1][-1], ref)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_stage_field_overlap_and_ring_depth_give_the_same_bits(storage):
+    """Blending the next chunk on the side stream (a ring twice as deep) gives
+    the same trajectory as blending each chunk before its launch, for chunk
+    sizes that make launches wrap the ring and cut at re-sorts."""
+    from jaxtrace_gb300 import workloads as W
+    c = W.precision_case(n=20, n_snap=6, seeds=(16, 16, 16), lattice=16, n_steps=41, dt=0.01)
+    g = c["grid"][0]
+    f = jt.StructuredTimeSeriesField(c["data"], c["times"], g, g, g, "clamp", storage=storage)
+    bc = jt.continuous_inlet_boundary_factory(W.UNIT, "x", "positive", "grid", c["concentrations"])
+    outs = []
+    for overlap, chunk in ((False, 5), (True, 5), (True, 3), (False, 32)):
+        tr = jt.create_tracker("rk4", f, bc, stage_overlap=overlap, stage_chunk=chunk, sort_every=7)
+        outs.append(tr.track_particles(c["x0"], c["time_span"], c["n_timesteps"], dt=c["dt"]).positions)
+    for o in outs[1:]:
+        assert same(outs[0], o)
 
 
 def test_stage_fields_with_velocity_recording_fall_back_to_pairs():

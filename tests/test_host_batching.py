@@ -174,6 +174,7 @@ def test_stage_chunk_fits_a_quarter_of_free_memory():
     assert _stage_chunk(32, 1000, nodes, 32, 8 << 30) == 10
     # too little room for 4 steps: gather snapshot pairs instead
     assert _stage_chunk(32, 1000, nodes, 32, 2 << 30) == 0
-    # short runs keep a chunk of their own length
+    # short runs keep a chunk of their own length, and a requested short chunk is kept
     assert _stage_chunk(32, 3, nodes, 16, 100 << 30) == 3
     assert _stage_chunk(32, 1, 8, 16, 1 << 20) == 1
+    assert _stage_chunk(3, 1000, nodes, 32, 100 << 30) == 3
