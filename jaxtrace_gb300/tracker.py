@@ -206,17 +206,23 @@ class ParticleTracker:
         n_rows = len(row_idx)
         # compact layouts write every row; the reference layout with a
         # recording interval leaves unrecorded rows at zero
-        alloc = np.empty if compact else np.zeros
-        positions = alloc((n_rows, n, 3), dtype=F32)
-        velocities = alloc((n_rows, n, 3), dtype=F32) if self.options.record_velocities else None
+        positions = _host_rows((n_rows, n, 3), zero=not compact)
+        velocities = _host_rows((n_rows, n, 3), zero=not compact) if self.options.record_velocities else None
         if n == 0 or T == 0:
             return self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, 0)
         host0 = src if src is not None else torch.from_numpy(x0)
         pos = host0.to("cuda", non_blocking=src is not None)
-        torch.from_numpy(positions[0]).copy_(host0)          # multi-threaded host copy
         if velocities is not None:
             torch.from_numpy(velocities[0]).copy_(self._field.sample_at_positions(pos, times[0]))
-        n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities)
+        # row 0 is a host copy of the input: made on a helper thread while
+        # the device tracks (torch releases the GIL inside copy_)
+        import threading
+        row0 = threading.Thread(target=lambda: torch.from_numpy(positions[0]).copy_(host0))
+        row0.start()
+        try:
+            n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities)
+        finally:
+            row0.join()
         if compact and self.options.record_final_only and T > 1:
             torch.from_numpy(positions[-1]).copy_(pos)        # device -> final row, no staging array
             if velocities is not None:
@@ -805,6 +811,26 @@ def _stage_scales(src) -> np.ndarray:
     bound = np.where(lerp, (sa + sb) * (1.0 + wb), wa + wb)
     bound = np.where(bound > 0, bound, 1.0)
     return np.exp2(np.ceil(np.log2(bound))).astype(F32)
+
+
+# Trajectory arrays up to this size live in pinned host memory: device
+# copies reach them at full speed, and torch's pinned-block cache hands the
+# pages of a dropped trajectory to the next call, so no run pays for first
+# touches of freshly mapped memory.  Larger arrays are plain NumPy memory.
+PINNED_TRAJECTORY_BYTES = 1 << 30
+
+
+def _host_rows(shape, zero: bool) -> np.ndarray:
+    """A float32 host array for trajectory rows (pinned when small enough)."""
+    nbytes = 4 * int(np.prod(shape))
+    if 0 < nbytes <= PINNED_TRAJECTORY_BYTES:
+        import torch
+        if torch.cuda.is_available():
+            t = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+            if zero:
+                t.zero_()
+            return t.numpy()
+    return np.zeros(shape, dtype=F32) if zero else np.empty(shape, dtype=F32)
 
 
 def create_tracker(integrator_name: str, field, boundary_condition, **options) -> ParticleTracker:
