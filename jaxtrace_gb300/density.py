@@ -75,6 +75,21 @@ def _device_bandwidth(P_dev, rule: str) -> float:
 
 
 # ---------------------------------------------------------------------------
+def _sph_cell(search: float, lo, hi, dims: int, n: int, per_cell: float = 8.0) -> float:
+    """Cell edge of the SPH candidate search: about ``per_cell`` particles per
+    cell on average, between search/8 and search/2.  Finer cells hug the
+    support sphere (the trimmed rows of a coarse grid scan about 3x the
+    sphere's particles) at the price of more rows per query, so the edge
+    follows the particle density."""
+    ext = [max(float(hi[a]) - float(lo[a]), 0.0) for a in range(dims)]
+    live = [e for e in ext if e > 0]
+    if not live or n <= 0:
+        return max(search / 2.0, 1e-6)
+    vol = float(np.prod(live))
+    edge = (vol * per_cell / n) ** (1.0 / len(live))
+    return max(min(edge, search / 2.0), search / 8.0, 1e-6)
+
+
 class CellList:
     """Particles sorted by row-major cells of a uniform grid (device)."""
 
@@ -394,10 +409,11 @@ class SPHDensityEstimator:
         d = self.D
         lo = [min(float(P3[:, a].min()), float(Q3[:, a].min())) for a in range(d)] + [0.0] * (3 - d)
         hi = [max(float(P3[:, a].max()), float(Q3[:, a].max())) for a in range(d)] + [0.0] * (3 - d)
-        cl = CellList(P3, lo, hi, max(search / 2.0, 1e-6), d)
+        cell = _sph_cell(search, lo, hi, d, int(P3.shape[0]))
+        cl = CellList(P3, lo, hi, cell, d)
         # queries in the same cell order, so a warp's queries walk the same
         # candidate cells together (broadcast loads); results scattered back
-        qcl = CellList(Q3, lo, hi, max(search / 2.0, 1e-6), d)
+        qcl = CellList(Q3, lo, hi, cell, d)
         idx = cl.ids.long()
         h_sorted = None if self._uniform_h is not None else self.smoothing_lengths[idx].contiguous()
         m_sorted = None if self.masses_dev is None else self.masses_dev[idx].contiguous()
