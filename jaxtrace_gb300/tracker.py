@@ -217,12 +217,22 @@ class ParticleTracker:
         # row 0 is a host copy of the input: made on a helper thread while
         # the device tracks (torch releases the GIL inside copy_)
         import threading
-        row0 = threading.Thread(target=lambda: torch.from_numpy(positions[0]).copy_(host0))
+        failed = []
+
+        def copy_row0():
+            try:
+                torch.from_numpy(positions[0]).copy_(host0)
+            except BaseException as exc:   # re-raised on the caller's thread
+                failed.append(exc)
+
+        row0 = threading.Thread(target=copy_row0)
         row0.start()
         try:
             n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities)
         finally:
             row0.join()
+        if failed:
+            raise failed[0]
         if compact and self.options.record_final_only and T > 1:
             torch.from_numpy(positions[-1]).copy_(pos)        # device -> final row, no staging array
             if velocities is not None:
