@@ -566,6 +566,44 @@ def density_part(P, profile):
             "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3", "kde_particles_per_s": n / (kde_ms / 1e3)}
 
 
+def analytics_part(a, case, g, bc, x0_dev, times, plain_ms, storage):
+    """Trajectory analytics on the device: one pass of the headline run with
+    the per-particle path length fused into the tracking kernel (its cost
+    against the plain pass), and the pair term of the mixing metrics over
+    100,000 particles (10^10 ordered pairs)."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    from jaxtrace_gb300.analysis import pair_log_ratio
+    field = jt.StructuredTimeSeriesField(case["data"], case["times"], g, g, g, "clamp", storage=storage)
+    tr = jt.create_tracker("rk4", field, bc, record_final_only=True, record_path_length=True)
+    sched = torch.from_numpy(tr._schedule(times, case["dt"]).view(np.int32).reshape(-1, 8)).cuda()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    comp = torch.zeros_like(x0_dev) if tr._arith() == 1 else None
+    pos = torch.empty_like(x0_dev)
+
+    def one():
+        pos.copy_(x0_dev)
+        if comp is not None:
+            comp.zero_()
+        tr.track_device(pos, times, case["dt"], status, comp, sched)
+
+    one()
+    path_ms = _timed(one, 1)
+    rng = np.random.default_rng(5)
+    p0 = rng.random((100_000, 3)).astype(np.float32)
+    p1 = (p0 + rng.normal(0, 0.01, p0.shape)).astype(np.float32)
+    pair_log_ratio(p0[:1000], p1[:1000])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    s, cnt = pair_log_ratio(p0, p1, 0.1)
+    pair_ms = (time.perf_counter() - t) * 1e3
+    return {"path_length_pass_ms": path_ms, "plain_pass_ms": plain_ms,
+            "path_length_overhead": path_ms / plain_ms - 1.0,
+            "pair_term_ms": pair_ms, "pair_term_particles": 100_000, "pair_term_pairs_in_cutoff": cnt,
+            "pair_term_pairs_per_s": 100_000 * 99_999 / (pair_ms / 1e3)}
+
+
 def workload_name(a):
     return (f"precision: {a.grid}^3 clamp grid, 64 snapshots ABC+(1,0,0)+N(0,0.01^2) over [0,2], "
             f"{a.seeds ** 3} lattice seeds, continuous inlet x (lattice {a.seeds}x{a.seeds}), "
@@ -737,6 +775,8 @@ def main():
                        "api": "create_tracker('rk4', field, continuous_inlet, record_final_only=True)"
                               ".track_particles(pinned host x0)"}
     line["clocks"] = clk.summary()
+    if not a.profile and rank == 0:
+        line["analytics"] = analytics_part(a, case, g, bc, x0_dev, times, results[head]["ms_per_step"], head)
     iss = line.get("roofline", {}).get("issue")
     if iss is not None:
         mhz = line["clocks"].get("sm_mhz") or 2070.0

@@ -283,6 +283,15 @@ typedef struct {
     const int32_t* ids;     /* device (N): particle index of slot i, used as the
                                row index of traj/vel writes after a locality
                                sort, or NULL (slot i is particle i)           */
+    float* path;            /* device (N) float32 per-particle path length or
+                               NULL: each step adds |x_after - x_before| (the
+                               positions after the boundary, float32
+                               sqrt((dx*dx + dy*dy) + dz*dz)) in step order,
+                               the sum Trajectory.compute_path_length forms
+                               over rows recorded every step
+                               (tracking/particles.py:296-313); indexed by
+                               particle (through ids after a sort), carried
+                               across launches                              */
 } jt_track_params;
 
 /* ABI / diagnostics */
@@ -523,6 +532,17 @@ int jt_octree_fetch(void* handle, jt_octree_node* nodes, int32_t* elems, float* 
                     float* tet_geom, float* node_bounds);
 
 void jt_octree_free(void* handle);
+
+/* ---- trajectory analytics ------------------------------------------------- */
+/* The pair term of compute_mixing_metrics (tracking/analysis.py:297-312):
+ * over every ordered pair (i, j) whose float32 initial distance
+ * d0 = |x0_i - x0_j| (sqrt((dx*dx + dy*dy) + dz*dz), each operation rounded)
+ * satisfies 0 < d0 < rmax, *out_sum receives the float64 sum of
+ * logf(d1 / d0) with d1 = |x1_i - x1_j|, and *out_count the number of such
+ * pairs.  x0, x1: device (n,3) float32 (the first and last recorded rows);
+ * out_sum, out_count: device scalars, overwritten. */
+int jt_pair_log_ratio(const float* x0, const float* x1, int32_t n, float rmax, double* out_sum,
+                      unsigned long long* out_count, void* stream);
 
 #ifdef __cplusplus
 }

@@ -11,7 +11,8 @@ from .boundary import (absorbing_boundary_factory, clamping_boundary, continuous
 from .fields import (FEMTimeSeriesField, FemHashGrid, OctreeFEMTimeSeriesFieldOptimized, OctreeMesh, StructuredGridSampler,
                      StructuredTimeSeriesField, TimeSeriesField)
 from .integrators import euler_step, rk2_step, rk4_step
-from .particles import Trajectory
+from .particles import Trajectory, compute_trajectory_statistics
+from .analysis import compute_mixing_metrics
 from .seeding import random_seeds, uniform_grid_seeds
 from .tracker import EnsembleBatch, ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
 from .autotune import Autotuner
@@ -24,5 +25,6 @@ __all__ = [
     "create_tracker", "track_particles_simple", "random_seeds", "uniform_grid_seeds", "periodic_boundary",
     "reflective_boundary", "clamping_boundary", "absorbing_boundary_factory", "mixed_boundary",
     "continuous_inlet_boundary_factory", "no_boundary", "unit_box_periodic", "unit_box_reflective",
-    "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid",
+    "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid", "compute_trajectory_statistics",
+    "compute_mixing_metrics",
 ]

@@ -94,7 +94,7 @@ class TrackParams(C.Structure):
                 ("schedule", vp), ("schedule_stride", i64), ("ens_offsets", vp), ("n_ens", i32),
                 ("block_size", i32), ("pos", vp), ("comp", vp), ("traj", vp), ("vel", vp),
                 ("record_every", i32), ("record_compact", i32), ("row_base", i32), ("n_rows", i32),
-                ("status", vp), ("ids", vp)]
+                ("status", vp), ("ids", vp), ("path", vp)]
 
 
 class SortGrid(C.Structure):
@@ -167,6 +167,7 @@ def load(build_if_missing: bool = True):
         "jt_integrator_step": (i32, [P(Field), P(Blend), i32, i32, f32, vp, vp, vp, i32, vp, vp]),
         "jt_octree_build": (i32, [vp, i32, vp, i32, i32, i32, P(vp), P(OctreeInfo)]),
         "jt_octree_fetch": (i32, [vp, vp, vp, vp, vp, vp]),
+        "jt_pair_log_ratio": (i32, [vp, vp, i32, f32, vp, vp, vp]),
         "jt_octree_free": (None, [vp]),
         "jt_cell_sort_workspace_bytes": (C.c_size_t, [i32, i32]),
         "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),

@@ -512,7 +512,9 @@ __device__ __forceinline__ int find_ensemble(const int32_t* off, int n_ens, int 
 
 // Persistent tracking kernel body: one particle per thread, the time loop in
 // registers, boundary fused after every step, optional strided recording.
-template <bool EXACT, int INTEG, class Field>
+// PATH: P.path is set (the per-particle path length is accumulated); a
+// template argument so that runs without it keep the register budget.
+template <bool EXACT, int INTEG, bool PATH, class Field>
 __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B, const InletFrame& I,
                                            const jt_track_params& P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -533,11 +535,25 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
     const StepConst k{P.dt, P.dt_half, P.dt_sixth};
     int flags = 0;
     const int64_t n = P.n_particles;
+    // per-particle path length (Trajectory.compute_path_length over rows
+    // recorded every step): float32 |x_after - x_before| summed in step order
+    float plen = 0.0f;
+    int64_t pid = 0;
+    if (PATH) {
+        pid = P.ids != nullptr ? (int64_t)P.ids[i] : (int64_t)i;
+        plen = P.path[pid];
+    }
     for (int s = P.step_begin; s < P.step_end; ++s) {
         const jt_blend* e = sched + 4 * (int64_t)s;
+        const V3 xo = x;
         if (comp) integrate<EXACT, INTEG, true>(f, e, k, x, c, flags);
         else integrate<EXACT, INTEG, false>(f, e, k, x, c, flags);
         apply_boundary<EXACT>(B, I, x.x, x.y, x.z);
+        if (PATH) {
+            const float dx = __fsub_rn(x.x, xo.x), dy = __fsub_rn(x.y, xo.y), dz = __fsub_rn(x.z, xo.z);
+            plen = __fadd_rn(plen, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                        __fmul_rn(dz, dz))));
+        }
         if (P.traj != nullptr) {
             const int cnt = s + 1;
             if (cnt % P.record_every == 0) {
@@ -557,6 +573,7 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
         }
     }
     pp[0] = x.x; pp[1] = x.y; pp[2] = x.z;
+    if (PATH) P.path[pid] = plen;
     if (comp) {
         float* cp = P.comp + 3 * (int64_t)i;
         cp[0] = c.x; cp[1] = c.y; cp[2] = c.z;

@@ -29,10 +29,10 @@ struct MinBlocksOf<F, decltype(void(F::kMinBlocks))> {
     static constexpr int value = F::kMinBlocks;
 };
 
-template <bool EXACT, int INTEG, class Field>
+template <bool EXACT, int INTEG, bool PATH, class Field>
 __global__ void __launch_bounds__(kBlock, MinBlocksOf<Field>::value)
     k_track(Field f, jt_boundary B, InletFrame I, jt_track_params P) {
-    track_body<EXACT, INTEG>(f, B, I, P);
+    track_body<EXACT, INTEG, PATH>(f, B, I, P);
 }
 
 // Field evaluation at M points with one blend: sample_at_positions(pos, t).
@@ -98,10 +98,17 @@ struct Launcher {
         const int bs = P.block_size > 0 ? P.block_size : kBlock;
         const unsigned g = (unsigned)((P.n_particles + bs - 1) / bs);
         const InletFrame I = inlet_frame(B);
+        if (P.path != nullptr) return launch_track<EXACT, true>(f, B, I, P, g, bs, st);
+        return launch_track<EXACT, false>(f, B, I, P, g, bs, st);
+    }
+
+    template <bool EXACT, bool PATH, class FF>
+    static cudaError_t launch_track(const FF& f, const jt_boundary& B, const InletFrame& I, const jt_track_params& P,
+                                    unsigned g, int bs, cudaStream_t st) {
         switch (P.integrator) {
-            case JT_EULER: k_track<EXACT, JT_EULER><<<g, bs, 0, st>>>(f, B, I, P); break;
-            case JT_RK2: k_track<EXACT, JT_RK2><<<g, bs, 0, st>>>(f, B, I, P); break;
-            default: k_track<EXACT, JT_RK4><<<g, bs, 0, st>>>(f, B, I, P); break;
+            case JT_EULER: k_track<EXACT, JT_EULER, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
+            case JT_RK2: k_track<EXACT, JT_RK2, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
+            default: k_track<EXACT, JT_RK4, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
         }
         return cudaGetLastError();
     }

@@ -1,9 +1,16 @@
 """Trajectory container with the reference layout (tracking/particles.py:82-129):
-positions (T,N,3) float32, times (T,) float32, optional velocities (T,N,3)."""
+positions (T,N,3) float32, times (T,) float32, optional velocities (T,N,3).
+
+The statistics follow Trajectory.compute_* and compute_trajectory_statistics
+(tracking/particles.py:279-340, :401-416, :862-924) in the same float32
+NumPy arithmetic.  ``path_length`` (optional) is the per-particle path length
+the tracking kernel accumulates over every step when the tracker was created
+with ``record_path_length=True``: the value compute_path_length gives on a
+trajectory recorded at every step, available without recording one."""
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-from typing import Any, Dict, Optional
+from typing import Any, Dict, Optional, Tuple
 
 import numpy as np
 
@@ -27,6 +34,7 @@ class Trajectory:
     times: np.ndarray
     velocities: Optional[np.ndarray] = None
     metadata: Dict[str, Any] = field(default_factory=dict)
+    path_length: Optional[np.ndarray] = None
 
     def __post_init__(self):
         self.positions = _ensure_trajectory_shape(self.positions)
@@ -49,8 +57,20 @@ class Trajectory:
         return self.T
 
     @property
+    def num_particles(self) -> int:
+        return self.N
+
+    @property
+    def num_timesteps(self) -> int:
+        return self.T
+
+    @property
     def duration(self) -> float:
         return float(self.times[-1] - self.times[0]) if self.T > 1 else 0.0
+
+    @property
+    def dt_mean(self) -> float:
+        return float(np.mean(np.diff(self.times))) if self.T > 1 else 0.0
 
     def get_positions_at_time(self, t: float) -> np.ndarray:
         return self.positions[int(np.argmin(np.abs(self.times - t)))]
@@ -71,4 +91,55 @@ class Trajectory:
         return n / 1024 ** 2
 
     def compute_displacement(self) -> np.ndarray:
-        return np.linalg.norm(self.positions[-1] - self.positions[0], axis=1)
+        """|x_T - x_0| per particle, float32 (particles.py:279-294)."""
+        if self.T < 2:
+            return np.zeros(self.N, dtype=F32)
+        return np.linalg.norm(self.positions[-1] - self.positions[0], axis=1).astype(F32)
+
+    def compute_path_length(self) -> np.ndarray:
+        """Sum over recorded rows of |x_{t+1} - x_t|, float32 (particles.py:296-313)."""
+        if self.T < 2:
+            return np.zeros(self.N, dtype=F32)
+        steps = np.linalg.norm(np.diff(self.positions, axis=0), axis=2)
+        return np.sum(steps, axis=0).astype(F32)
+
+    def compute_speeds(self) -> np.ndarray:
+        """(T-1, N) speeds: |v| of the stored velocities without the last row,
+        or |dx/dt| of consecutive rows (particles.py:315-340)."""
+        if self.T < 2:
+            return np.zeros((0, self.N), dtype=F32)
+        if self.velocities is not None:
+            return np.linalg.norm(self.velocities, axis=2)[:-1].astype(F32)
+        rates = np.diff(self.positions, axis=0) / np.diff(self.times)[:, None, None]
+        return np.linalg.norm(rates, axis=2).astype(F32)
+
+    def get_bounds(self) -> Tuple[np.ndarray, np.ndarray]:
+        """Per-axis minimum and maximum over every row (particles.py:401-416)."""
+        flat = self.positions.reshape(-1, 3)
+        return np.min(flat, axis=0), np.max(flat, axis=0)
+
+    def subsample_time(self, step: int = 2) -> "Trajectory":
+        return Trajectory(positions=self.positions[::step], times=self.times[::step],
+                          velocities=self.velocities[::step] if self.velocities is not None else None,
+                          metadata={**self.metadata, "subsampled": step})
+
+
+def _summary(a: np.ndarray) -> Dict[str, float]:
+    return {"mean": float(np.mean(a)), "std": float(np.std(a)), "min": float(np.min(a)), "max": float(np.max(a))}
+
+
+def compute_trajectory_statistics(trajectory: Trajectory) -> Dict[str, Any]:
+    """Basic sizes, displacement / path-length / speed summaries and bounds
+    (particles.py:862-924)."""
+    tr = trajectory
+    stats: Dict[str, Any] = {"basic": {"num_particles": tr.N, "num_timesteps": tr.T, "duration": tr.duration,
+                                       "dt_mean": tr.dt_mean, "memory_mb": tr.memory_usage_mb()}}
+    if tr.T > 1:
+        stats["displacement"] = _summary(tr.compute_displacement())
+        stats["path_length"] = _summary(tr.compute_path_length())
+        speeds = tr.compute_speeds()
+        if speeds.size > 0:
+            stats["speed"] = _summary(speeds)
+        lo, hi = tr.get_bounds()
+        stats["bounds"] = {"min": lo.tolist(), "max": hi.tolist(), "extent": (hi - lo).tolist()}
+    return stats

@@ -62,6 +62,9 @@ class TrackerOptions:
                        own order of operations; float32 stays bit-identical)
     stage_overlap      blend the next chunk's stage fields on a side stream
                        while the current chunk is tracked (a ring twice as deep)
+    record_path_length accumulate each particle's path length over every step
+                       in the tracking kernel (Trajectory.path_length; what
+                       compute_path_length gives on an every-step recording)
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -95,6 +98,7 @@ class TrackerOptions:
     stage_fields: bool = True
     stage_chunk: int = 32
     stage_overlap: bool = True
+    record_path_length: bool = False
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
         """tracker.py:142-153."""
@@ -237,7 +241,12 @@ class ParticleTracker:
             torch.from_numpy(positions[-1]).copy_(pos)        # device -> final row, no staging array
             if velocities is not None:
                 torch.from_numpy(velocities[-1]).copy_(self._field.sample_at_positions(pos, times[-1]))
-        return self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, n_chunks)
+        traj = self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, n_chunks)
+        if self.options.record_path_length:
+            traj.path_length = getattr(self, "_last_path_length", None)
+            if traj.path_length is None:       # no step ran
+                traj.path_length = np.zeros(n, dtype=F32)
+        return traj
 
     def _trajectory(self, positions, times, velocities, n, T, dt, batch_size, n_chunks):
         meta = {
@@ -344,6 +353,7 @@ class ParticleTracker:
                 cb(s / n_steps)
         eng.finish()
         self.last_status = int(eng.status.item())
+        self._last_path_length = eng.path.cpu().numpy() if eng.path is not None else None
         return eng.launches
 
     def track_device(self, pos, times, dt, status=None, comp=None, sched_dev=None, timers=None):
@@ -456,6 +466,11 @@ class _Engine:
             self.ws = torch.empty(ws, dtype=torch.uint8, device=pos.device)
             self._sort(first=True)
         self.p = tracker.make_params(self.pos, dt, n_steps, sched_dev, status, self.comp)
+        # per-particle path length (indexed by particle, so the sort leaves it be)
+        self.path = None
+        if ens is None and tracker.options.record_path_length and self.n > 0:
+            self.path = torch.zeros(self.n, dtype=torch.float32, device=pos.device)
+            self.p.path = self.path.data_ptr()
         if ens is not None:       # (device offsets (E+1,) int32, E, schedule entries per ensemble)
             self.ens = ens
             self.p.ens_offsets, self.p.n_ens, self.p.schedule_stride = ens[0].data_ptr(), ens[1], ens[2]

@@ -318,7 +318,38 @@ def phase_fem(ref: str):
     print("phase fem: done")
 
 
-PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem}
+def phase_analytics(ref: str):
+    """Trajectory statistics and mixing metrics of the reference on small
+    random-walk trajectories (with and without stored velocities)."""
+    sys.path.insert(0, ref)
+    from jaxtrace.tracking.analysis import compute_mixing_metrics
+    from jaxtrace.tracking.particles import Trajectory, compute_trajectory_statistics
+    rng = np.random.default_rng(21)
+    T, N = 40, 600
+    steps = rng.normal(0.0, 0.01, (T, N, 3)).astype(F32)
+    steps[0] = rng.random((N, 3)).astype(F32)
+    pos = np.cumsum(steps, axis=0, dtype=F32)
+    pos[T // 2:, : N // 10, 0] -= F32(1.0)                 # periodic-style jumps in x for a tenth
+    times = np.linspace(0.0, 2.0, T).astype(F32)
+    vel = rng.normal(0.0, 0.5, (T, N, 3)).astype(F32)
+    out = {"positions": pos, "times": times, "velocities": vel}
+    for tag, v in (("nov", None), ("vel", vel)):
+        tr = Trajectory(positions=pos.copy(), times=times.copy(), velocities=None if v is None else v.copy())
+        out[f"{tag}_displacement"] = tr.compute_displacement()
+        out[f"{tag}_path_length"] = tr.compute_path_length()
+        out[f"{tag}_speeds"] = tr.compute_speeds()
+        stats = compute_trajectory_statistics(tr)
+        for group, vals in stats.items():
+            for k, val in vals.items():
+                out[f"{tag}_stats_{group}_{k}"] = np.asarray(val, dtype=np.float64)
+    mix = compute_mixing_metrics(Trajectory(positions=pos.copy(), times=times.copy()))
+    for k, val in mix.items():
+        out[f"mix_{k}"] = np.asarray(val, dtype=np.float64)
+    np.savez_compressed(HERE / "analytics.npz", **out)
+    print("phase analytics: done")
+
+
+PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem, "analytics": phase_analytics}
 
 if __name__ == "__main__":
     if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
