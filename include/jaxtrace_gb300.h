@@ -533,6 +533,37 @@ int jt_octree_fetch(void* handle, jt_octree_node* nodes, int32_t* elems, float* 
 
 void jt_octree_free(void* handle);
 
+/* ---- FEM hash grid build (host) ----------------------------------------- */
+typedef struct {
+    int64_t n_cells;        /* grid_size[0]*grid_size[1]*grid_size[2]         */
+    int64_t n_entries;      /* length of the concatenated cell lists         */
+    int64_t n_sub_cells;    /* n_cells * sub_div^3 (0 without sub-cells)      */
+    int64_t n_sub_entries;  /* length of the concatenated sub-cell lists     */
+    int32_t max_per_cell;   /* the reference's padded table width            */
+    int32_t pad;
+} jt_fem_grid_info;
+
+/* Build the hash grid of build_tetrahedral_mesh
+ * (fields/fem_interpolator.py:36-143) on the host: every element in every
+ * cell its float32 box overlaps (float32 box minus float32 grid_min, divided
+ * by the float64 cell_edge, floored, clipped), elements ascending per cell;
+ * with sub_div > 0, the sub-cell lists of jt_fem_field (each cell split into
+ * sub_div^3, boxes widened by eps[axis], float64 sub-cell index).
+ * points: host (n_points,3) float32; conn: host (n_tets,4) int32;
+ * grid_size, grid_min (float32), cell_edge (float64), eps (float64): 3 each.
+ * On success *handle_out owns the lists until jt_fem_grid_free. */
+int jt_fem_grid_build(const float* points, int32_t n_points, const int32_t* conn, int32_t n_tets,
+                      const int32_t* grid_size, const float* grid_min, const double* cell_edge, int32_t sub_div,
+                      const double* eps, void** handle_out, jt_fem_grid_info* info);
+
+/* Copy the lists into caller host buffers (any may be NULL): cell_start
+ * (n_cells+1), cell_elems (n_entries), sub_start (n_sub_cells+1; one 0 without
+ * sub-cells), sub_elems (n_sub_entries). */
+int jt_fem_grid_fetch(void* handle, int32_t* cell_start, int32_t* cell_elems, int32_t* sub_start,
+                      int32_t* sub_elems);
+
+void jt_fem_grid_free(void* handle);
+
 /* ---- trajectory analytics ------------------------------------------------- */
 /* The pair term of compute_mixing_metrics (tracking/analysis.py:297-312):
  * over every ordered pair (i, j) whose float32 initial distance

@@ -122,6 +122,11 @@ class KdeParams(C.Structure):
                 ("grid", SortGrid), ("axis", vp * 3), ("particles", vp), ("cell_end", vp), ("out", vp)]
 
 
+class FemGridInfo(C.Structure):
+    _fields_ = [("n_cells", i64), ("n_entries", i64), ("n_sub_cells", i64), ("n_sub_entries", i64),
+                ("max_per_cell", i32), ("pad", i32)]
+
+
 class OctreeInfo(C.Structure):
     _fields_ = [("n_nodes", i32), ("n_elem_entries", i32), ("max_elems", i32), ("max_tree_depth", i32),
                 ("n_leaves", i32), ("pad", i32)]
@@ -168,6 +173,9 @@ def load(build_if_missing: bool = True):
         "jt_octree_build": (i32, [vp, i32, vp, i32, i32, i32, P(vp), P(OctreeInfo)]),
         "jt_octree_fetch": (i32, [vp, vp, vp, vp, vp, vp]),
         "jt_pair_log_ratio": (i32, [vp, vp, i32, f32, vp, vp, vp]),
+        "jt_fem_grid_build": (i32, [vp, i32, vp, i32, vp, vp, vp, i32, vp, P(vp), P(FemGridInfo)]),
+        "jt_fem_grid_fetch": (i32, [vp, vp, vp, vp, vp]),
+        "jt_fem_grid_free": (None, [vp]),
         "jt_octree_free": (None, [vp]),
         "jt_cell_sort_workspace_bytes": (C.c_size_t, [i32, i32]),
         "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),

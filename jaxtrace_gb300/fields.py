@@ -529,27 +529,7 @@ class FemHashGrid:
         V = P[T4]                                           # (M,4,3)
         emin, emax = V.min(axis=1), V.max(axis=1)
         self.element_bounds = np.stack([emin, emax], axis=1)
-        hi = np.array(self.grid_size) - 1
-        cmin = np.clip(np.floor((emin - bmin) / cell64).astype(int), 0, hi)
-        cmax = np.clip(np.floor((emax - bmin) / cell64).astype(int), 0, hi)
-        ext = cmax - cmin + 1
-        count = ext.prod(axis=1)
-        elem = np.repeat(np.arange(len(T4), dtype=np.int64), count)
-        first = np.repeat(np.cumsum(count) - count, count)
-        r = np.arange(len(elem), dtype=np.int64) - first
-        ez, ey = np.repeat(ext[:, 2], count), np.repeat(ext[:, 1], count)
-        k = np.repeat(cmin[:, 2], count) + r % ez
-        j = np.repeat(cmin[:, 1], count) + (r // ez) % ey
-        i = np.repeat(cmin[:, 0], count) + r // (ez * ey)
-        cell = (i * self.grid_size[1] + j) * self.grid_size[2] + k
-        order = np.argsort(cell, kind="stable")             # keeps ascending elements per cell
-        n_cells = int(np.prod(self.grid_size))
-        counts = np.bincount(cell, minlength=n_cells)
-        self.cell_elem_counts = counts.astype(np.int32)
-        self.cell_start = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
-        self.cell_elems = elem[order].astype(np.int32)
-        self.max_elems_per_cell = int(counts.max()) if n_cells else 0
-        self._build_sub_cells(int(sub_div), elem, np.stack([i, j, k], axis=1), emin, emax, bmin, cell64)
+        self._build_lists(int(sub_div), bmin, cell64)
         # device records: box (min xyz,0,max xyz,0) and geometry (v0, v1-v0, v2-v0, v3-v0, ids)
         M = len(T4)
         self.tet_box = np.zeros((M, 8), dtype=F32)
@@ -562,43 +542,42 @@ class FemHashGrid:
         self.tet_geom[:, 9:12] = V[:, 3] - v0
         self.tet_geom[:, 12:16] = T4.view(F32)
 
-    def _build_sub_cells(self, S, elem, cidx, emin, emax, bmin, cell64):
-        """Sub-cell lists (S^3 per hash cell): for each (element, cell) entry
-        the sub-cells of that cell its box meets, widened by a margin that
-        covers the float32 rounding of the device's sub-cell index; stable
-        ordering keeps the elements of every list ascending."""
-        self.sub_div = S
-        if S <= 0 or len(elem) == 0:
-            self.sub_div = 0
+    def _build_lists(self, S, bmin, cell64):
+        """Cell lists and sub-cell lists (S^3 per hash cell) through the
+        library's host builder (jt_fem_grid_build): the reference's float64
+        element-to-cell assignment, elements ascending per list; sub-cells
+        take each (element, cell) entry where its box, widened by a margin
+        that covers the float32 rounding of the device's sub-cell index,
+        meets them."""
+        sub = cell64 / max(S, 1)
+        scale = float(np.abs(self.points).max()) if len(self.points) else 1.0
+        eps = np.ascontiguousarray(1e-3 * sub + 4e-7 * max(scale, 1.0), dtype=np.float64)
+        gs = np.ascontiguousarray(self.grid_size, dtype=np.int32)
+        gmin = np.ascontiguousarray(bmin, dtype=F32)
+        edge = np.ascontiguousarray(cell64, dtype=np.float64)
+        P = np.ascontiguousarray(self.points, dtype=F32)
+        T4 = np.ascontiguousarray(self.connectivity, dtype=np.int32)
+        lib = L.load()
+        handle = C.c_void_p()
+        info = L.FemGridInfo()
+        L.check(lib.jt_fem_grid_build(P.ctypes.data, len(P), T4.ctypes.data, len(T4), gs.ctypes.data,
+                                      gmin.ctypes.data, edge.ctypes.data, max(int(S), 0), eps.ctypes.data,
+                                      C.byref(handle), C.byref(info)))
+        try:
+            self.cell_start = np.zeros(info.n_cells + 1, np.int32)
+            self.cell_elems = np.zeros(info.n_entries, np.int32)
+            self.sub_start = np.zeros(max(info.n_sub_cells + 1, 1), np.int32)
+            self.sub_elems = np.zeros(info.n_sub_entries, np.int32)
+            L.check(lib.jt_fem_grid_fetch(handle, self.cell_start.ctypes.data, self.cell_elems.ctypes.data,
+                                          self.sub_start.ctypes.data, self.sub_elems.ctypes.data))
+        finally:
+            lib.jt_fem_grid_free(handle)
+        self.cell_elem_counts = np.diff(self.cell_start).astype(np.int32)
+        self.max_elems_per_cell = int(info.max_per_cell)
+        self.sub_div = int(S) if (S > 0 and info.n_sub_cells > 0) else 0
+        if self.sub_div == 0:
             self.sub_start = np.zeros(1, np.int32)
             self.sub_elems = np.zeros(1, np.int32)
-            return
-        sub = cell64 / S
-        scale = float(np.abs(self.points).max()) if len(self.points) else 1.0
-        eps = 1e-3 * sub + 4e-7 * max(scale, 1.0)
-        lo = bmin.astype(np.float64) + cidx * cell64               # the entry's cell corner
-        e_lo = emin[elem].astype(np.float64) - eps
-        e_hi = emax[elem].astype(np.float64) + eps
-        slo = np.clip(np.floor((e_lo - lo) / np.where(sub > 0, sub, 1.0)), 0, S - 1).astype(np.int64)
-        shi = np.clip(np.floor((e_hi - lo) / np.where(sub > 0, sub, 1.0)), 0, S - 1).astype(np.int64)
-        slo = np.where(sub > 0, slo, 0)
-        shi = np.where(sub > 0, shi, S - 1)
-        ext = shi - slo + 1
-        count = ext.prod(axis=1)
-        el = np.repeat(elem, count)
-        first = np.repeat(np.cumsum(count) - count, count)
-        r = np.arange(len(el), dtype=np.int64) - first
-        ez, ey = np.repeat(ext[:, 2], count), np.repeat(ext[:, 1], count)
-        sz = np.repeat(slo[:, 2], count) + r % ez
-        sy = np.repeat(slo[:, 1], count) + (r // ez) % ey
-        sx = np.repeat(slo[:, 0], count) + r // (ez * ey)
-        cell = np.repeat((cidx[:, 0] * self.grid_size[1] + cidx[:, 1]) * self.grid_size[2] + cidx[:, 2], count)
-        sid = cell * (S ** 3) + (sx * S + sy) * S + sz
-        order = np.argsort(sid, kind="stable")
-        n_sub = int(np.prod(self.grid_size)) * S ** 3
-        cnt = np.bincount(sid, minlength=n_sub)
-        self.sub_start = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int32)
-        self.sub_elems = el[order].astype(np.int32)
 
     def cell_to_elements(self) -> np.ndarray:
         """The reference's (cells, max_per_cell) table, -1 padded."""

@@ -76,3 +76,58 @@ def test_sub_cell_lists_hold_every_candidate_the_cell_scan_can_pick():
         cand = h.cell_elems[h.cell_start[cell]:h.cell_start[cell + 1]]
         holds = cand[np.all((eb[cand, 0] <= p) & (p <= eb[cand, 1]), axis=1)]
         assert np.isin(holds, sub).all()
+
+
+def _numpy_lists(P, T4, grid_size, bmin, cell64, S):
+    """The hash-grid cell and sub-cell lists restated with NumPy array
+    operations (the checker of the library's host builder)."""
+    V = P[T4]
+    emin, emax = V.min(axis=1), V.max(axis=1)
+    hi = np.array(grid_size) - 1
+    cmin = np.clip(np.floor((emin - bmin) / cell64).astype(int), 0, hi)
+    cmax = np.clip(np.floor((emax - bmin) / cell64).astype(int), 0, hi)
+    ext = cmax - cmin + 1
+    count = ext.prod(axis=1)
+    elem = np.repeat(np.arange(len(T4), dtype=np.int64), count)
+    first = np.repeat(np.cumsum(count) - count, count)
+    r = np.arange(len(elem), dtype=np.int64) - first
+    ez, ey = np.repeat(ext[:, 2], count), np.repeat(ext[:, 1], count)
+    k = np.repeat(cmin[:, 2], count) + r % ez
+    j = np.repeat(cmin[:, 1], count) + (r // ez) % ey
+    i = np.repeat(cmin[:, 0], count) + r // (ez * ey)
+    cell = (i * grid_size[1] + j) * grid_size[2] + k
+    n_cells = int(np.prod(grid_size))
+    cell_start = np.concatenate([[0], np.cumsum(np.bincount(cell, minlength=n_cells))]).astype(np.int32)
+    cell_elems = elem[np.argsort(cell, kind="stable")].astype(np.int32)
+    sub = cell64 / S
+    eps = 1e-3 * sub + 4e-7 * max(float(np.abs(P).max()), 1.0)
+    cidx = np.stack([i, j, k], axis=1)
+    lo = bmin.astype(np.float64) + cidx * cell64
+    slo = np.clip(np.floor((emin[elem].astype(np.float64) - eps - lo) / sub), 0, S - 1).astype(np.int64)
+    shi = np.clip(np.floor((emax[elem].astype(np.float64) + eps - lo) / sub), 0, S - 1).astype(np.int64)
+    sext = shi - slo + 1
+    scount = sext.prod(axis=1)
+    el = np.repeat(elem, scount)
+    first = np.repeat(np.cumsum(scount) - scount, scount)
+    r = np.arange(len(el), dtype=np.int64) - first
+    ez, ey = np.repeat(sext[:, 2], scount), np.repeat(sext[:, 1], scount)
+    sz = np.repeat(slo[:, 2], scount) + r % ez
+    sy = np.repeat(slo[:, 1], scount) + (r // ez) % ey
+    sx = np.repeat(slo[:, 0], scount) + r // (ez * ey)
+    sid = np.repeat(cell, scount) * S ** 3 + (sx * S + sy) * S + sz
+    sub_start = np.concatenate([[0], np.cumsum(np.bincount(sid, minlength=n_cells * S ** 3))]).astype(np.int32)
+    sub_elems = el[np.argsort(sid, kind="stable")].astype(np.int32)
+    return cell_start, cell_elems, sub_start, sub_elems
+
+
+@pytest.mark.parametrize("res,sub_div", [(6, 4), (10, 3), (7, 2)])
+def test_host_builder_lists_equal_the_array_restatement(res, sub_div):
+    from jaxtrace_gb300 import workloads as W
+    P, T4 = W.kuhn_mesh(9, 0.2, res)
+    P = (P * np.array([1.0, 0.6, 1.7], dtype=np.float32)).astype(np.float32)   # aspect-ratio cell counts
+    h = jt.FemHashGrid(P, T4, res, sub_div=sub_div)
+    bmin = P.min(axis=0)
+    ref = _numpy_lists(P, T4, h.grid_size, bmin, h.cell_size64, sub_div)
+    for ours, theirs in zip((h.cell_start, h.cell_elems, h.sub_start, h.sub_elems), ref):
+        assert np.array_equal(ours, theirs)
+    assert h.max_elems_per_cell == int(np.diff(h.cell_start).max())
