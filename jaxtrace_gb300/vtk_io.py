@@ -1,0 +1,371 @@
+"""VTK XML unstructured-grid time series without the VTK library.
+
+Reads what VTKUnstructuredTimeSeriesReader (io/vtk_reader.py:426-940) reads
+through VTK -- serial ``.vtu`` and parallel ``.pvtu`` files, one per time step
+-- with a direct XML / appended-binary parser, and returns the same
+JAXTrace-format dictionary: velocity_data (T, N, 3) float32, positions (N, 3)
+float32, times = step indices (vtk_reader.py:697-765).  ``tetrahedra()`` gives
+the VTK_TETRA cells as (M, 4) int32 for the FEM fields.
+
+DataArray encodings: ascii, binary (base64) and appended raw data, UInt32
+or UInt64 headers, optionally vtkZLibDataCompressor blocks (base64-encoded
+appended data is refused).
+``write_vtu`` writes the same format (appended raw, base64 or ascii) for
+exporting trajectories and for tests.
+"""
+from __future__ import annotations
+
+import base64
+import glob
+import os
+import re
+import xml.etree.ElementTree as ET
+import zlib
+from typing import Any, Dict, List, Optional, Tuple
+
+import numpy as np
+
+F32 = np.float32
+VTK_TETRA = 10
+
+_TYPES = {"Int8": np.int8, "UInt8": np.uint8, "Int16": np.int16, "UInt16": np.uint16, "Int32": np.int32,
+          "UInt32": np.uint32, "Int64": np.int64, "UInt64": np.uint64, "Float32": np.float32,
+          "Float64": np.float64}
+_NAMES = {np.dtype(v): k for k, v in _TYPES.items()}
+
+# velocity field names tried in order when none is given (vtk_reader.py:565-575)
+VELOCITY_NAMES = ["velocity", "Velocity", "VELOCITY", "U", "u", "vel", "Vel", "VEL", "Displacement",
+                  "displacement", "DISPLACEMENT", "VelocityField", "velocity_field", "FlowVelocity",
+                  "flow_velocity", "v", "V", "fluid_velocity", "Result", "RESULT", "NodeVel", "NODEVEL"]
+
+
+def _natural_key(path: str) -> tuple:
+    nums = tuple(int(x) for x in re.findall(r"\d+", os.path.basename(path)))
+    return nums if nums else (os.path.basename(path),)
+
+
+class _Blob:
+    """The decoding context of one XML file: byte order, header type,
+    compressor and the appended-data block."""
+
+    def __init__(self, root: ET.Element, raw: bytes, app_at: int):
+        self.little = root.get("byte_order", "LittleEndian") == "LittleEndian"
+        self.header = np.dtype(np.uint64 if root.get("header_type", "UInt32") == "UInt64" else np.uint32)
+        self.compressed = root.get("compressor", "") == "vtkZLibDataCompressor"
+        self.appended = b""
+        self.appended_b64 = False
+        if app_at >= 0:
+            tag_end = raw.find(b">", app_at)
+            self.appended_b64 = b'encoding="base64"' in raw[app_at:tag_end]
+            # the bytes start after the '_' marker that follows the tag
+            j = raw.find(b"_", tag_end) + 1
+            end = raw.rfind(b"</AppendedData>")
+            self.appended = raw[j:end]
+
+    def _hdr(self) -> np.dtype:
+        return self.header.newbyteorder("<" if self.little else ">")
+
+    def _payload(self, data: bytes) -> bytes:
+        """One binary DataArray (header + data, or compressed blocks)."""
+        h = self._hdr()
+        hs = h.itemsize
+        if not self.compressed:
+            n = int(np.frombuffer(data[:hs], dtype=h)[0])
+            return data[hs:hs + n]
+        nb = int(np.frombuffer(data[:hs], dtype=h)[0])
+        head = np.frombuffer(data[:hs * (3 + nb)], dtype=h).astype(np.int64)
+        sizes = head[3:3 + nb]
+        pos = hs * (3 + nb)
+        out = []
+        for s in sizes:
+            out.append(zlib.decompress(data[pos:pos + int(s)]))
+            pos += int(s)
+        return b"".join(out)
+
+    def array(self, el: ET.Element) -> np.ndarray:
+        dt = np.dtype(_TYPES[el.get("type")]).newbyteorder("<" if self.little else ">")
+        ncomp = int(el.get("NumberOfComponents", "1"))
+        fmt = el.get("format", "ascii")
+        if fmt == "ascii":
+            a = np.array((el.text or "").split(), dtype=dt.newbyteorder("="))
+        elif fmt == "binary":
+            text = "".join((el.text or "").split()).encode()
+            if self.compressed:
+                # base64 of the header, then base64 of the compressed blocks
+                hs = self._hdr().itemsize
+                first = base64.b64decode(text[:((hs + 2) // 3) * 4])
+                nb = int(np.frombuffer(first[:hs], dtype=self._hdr())[0])
+                hlen = ((hs * (3 + nb) + 2) // 3) * 4
+                head = base64.b64decode(text[:hlen])[: hs * (3 + nb)]
+                body = base64.b64decode(text[hlen:])
+                a = np.frombuffer(self._payload(head + body), dtype=dt)
+            else:
+                a = np.frombuffer(self._payload(base64.b64decode(text)), dtype=dt)
+        elif fmt == "appended":
+            off = int(el.get("offset", "0"))
+            if self.appended_b64:
+                raise NotImplementedError("base64-encoded appended data is not supported; use raw or binary")
+            a = np.frombuffer(self._payload(self.appended[off:]), dtype=dt)
+        else:
+            raise ValueError(f"unknown DataArray format {fmt!r}")
+        a = a.astype(dt.newbyteorder("="), copy=False)
+        return a.reshape(-1, ncomp) if ncomp > 1 else a
+
+
+def _read_piece(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
+    """One .vtu file; without ``geometry`` the points and cells are left
+    undecoded, and with ``names`` only those point arrays are decoded."""
+    raw = open(path, "rb").read()
+    # raw appended data is not XML: parse the part before it, closed
+    app_at = raw.find(b"<AppendedData")
+    root = ET.fromstring(raw if app_at < 0 else raw[:app_at] + b"</VTKFile>")
+    if root.get("type") != "UnstructuredGrid":
+        raise ValueError(f"{path}: not an UnstructuredGrid file ({root.get('type')})")
+    blob = _Blob(root, raw, app_at)
+    piece = root.find("UnstructuredGrid/Piece")
+    n_points = int(piece.get("NumberOfPoints", "0"))
+    pts, cells = None, {}
+    if geometry:
+        pts = np.asarray(blob.array(piece.find("Points/DataArray")), dtype=F32).reshape(-1, 3)
+        for el in piece.findall("Cells/DataArray"):
+            cells[el.get("Name")] = blob.array(el)
+    pdata = {}
+    pd = piece.find("PointData")
+    if pd is not None:
+        for el in pd.findall("DataArray"):
+            if names is None or el.get("Name") in names:
+                pdata[el.get("Name")] = blob.array(el)
+            else:
+                pdata[el.get("Name")] = None          # present, not decoded
+    return {"points": pts, "n_points": n_points, "cells": cells, "point_data": pdata}
+
+
+def read_vtk_xml(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
+    """points (N,3) float32, cells {connectivity, offsets, types} and
+    point_data {name: (N,) or (N,C)} of a .vtu file, or of a .pvtu file's
+    pieces appended in order (point ids of later pieces shifted).  Without
+    ``geometry`` points and cells are skipped; with ``names`` only those
+    point arrays are decoded (the others map to None)."""
+    if path.lower().endswith(".vtk"):
+        raise NotImplementedError(f"{path}: legacy .vtk files are not read; convert to .vtu")
+    if not path.lower().endswith(".pvtu"):
+        return _read_piece(path, geometry, names)
+    root = ET.parse(path).getroot()
+    base = os.path.dirname(path)
+    pieces = [_read_piece(os.path.join(base, p.get("Source")), geometry, names)
+              for p in root.findall("PUnstructuredGrid/Piece")]
+    if not pieces:
+        raise ValueError(f"{path}: no pieces")
+    pts, conn, offs, types, pdata, shift, oshift = [], [], [], [], {}, 0, 0
+    for p in pieces:
+        if geometry:
+            pts.append(p["points"])
+            c = p["cells"]
+            if "connectivity" in c:
+                conn.append(np.asarray(c["connectivity"], dtype=np.int64) + shift)
+                offs.append(np.asarray(c["offsets"], dtype=np.int64) + oshift)
+                types.append(np.asarray(c["types"], dtype=np.uint8))
+                oshift += len(c["connectivity"])
+        shift += p["n_points"]
+        for k, v in p["point_data"].items():
+            pdata.setdefault(k, []).append(v)
+    cells = {}
+    if conn:
+        cells = {"connectivity": np.concatenate(conn), "offsets": np.concatenate(offs),
+                 "types": np.concatenate(types)}
+    return {"points": np.concatenate(pts) if geometry else None, "n_points": shift, "cells": cells,
+            "point_data": {k: (None if any(x is None for x in v) else np.concatenate(v)) for k, v in pdata.items()}}
+
+
+def _velocity3(v: np.ndarray) -> np.ndarray:
+    v = np.asarray(v, dtype=F32)
+    if v.ndim == 1:
+        v = v[:, None]
+    if v.shape[1] < 3:
+        v = np.concatenate([v, np.zeros((len(v), 3 - v.shape[1]), dtype=F32)], axis=1)
+    return np.ascontiguousarray(v[:, :3])
+
+
+class VTKUnstructuredTimeSeriesReader:
+    """One .vtu/.pvtu per time step (vtk_reader.py:426-940): files matched by
+    ``file_pattern``, .pvtu preferred over .vtu of the same name, naturally
+    sorted; the last ``max_time_steps`` kept."""
+
+    def __init__(self, file_pattern: str, max_time_steps: Optional[int] = None,
+                 velocity_field_name: Optional[str] = None, cache_size_limit: Optional[int] = None):
+        self.file_pattern = file_pattern
+        self.max_time_steps = max_time_steps
+        self.velocity_field_name = velocity_field_name
+        self.cache_size_limit = 15 if cache_size_limit is None else int(cache_size_limit)
+        self.time_files = self._find_time_files()
+        if not self.time_files:
+            raise ValueError(f"No VTK files found matching pattern: {file_pattern}")
+        self.grid_points: Optional[np.ndarray] = None
+        self._cells: Dict[str, np.ndarray] = {}
+        self.velocity_cache: Dict[int, np.ndarray] = {}
+
+    def _find_time_files(self) -> List[str]:
+        files = glob.glob(os.path.expanduser(self.file_pattern))
+        pvtu = [f for f in files if f.lower().endswith(".pvtu")]
+        vtu = [f for f in files if f.lower().endswith(".vtu")]
+        chosen = pvtu if pvtu else vtu
+        chosen.sort(key=_natural_key)
+        if self.max_time_steps is not None and len(chosen) > self.max_time_steps:
+            chosen = chosen[-self.max_time_steps:]
+        return chosen
+
+    def __len__(self) -> int:
+        return len(self.time_files)
+
+    def _field_name(self, pdata: Dict[str, np.ndarray]) -> str:
+        if self.velocity_field_name is not None:
+            return self.velocity_field_name
+        for name in VELOCITY_NAMES:
+            if name in pdata:
+                self.velocity_field_name = name
+                return name
+        raise ValueError(f"Velocity field not found. Available point data fields: {sorted(pdata)}")
+
+    def load_single_timestep(self, time_idx: int) -> np.ndarray:
+        if not 0 <= time_idx < len(self.time_files):
+            raise IndexError(f"Time index {time_idx} out of range [0, {len(self.time_files) - 1}]")
+        if time_idx in self.velocity_cache:
+            return self.velocity_cache[time_idx]
+        first = self.grid_points is None
+        want = None if self.velocity_field_name is None else [self.velocity_field_name]
+        d = read_vtk_xml(self.time_files[time_idx], geometry=first, names=want)
+        if first:
+            self.grid_points = np.ascontiguousarray(d["points"], dtype=F32)
+            self._cells = d["cells"]
+        name = self._field_name(d["point_data"])
+        if name not in d["point_data"]:
+            raise ValueError(f"Velocity field '{name}' not found in {self.time_files[time_idx]}")
+        if d["point_data"][name] is None:          # decoded lazily for the chosen name
+            d = read_vtk_xml(self.time_files[time_idx], geometry=False, names=[name])
+        v = _velocity3(d["point_data"][name])
+        if len(v) != len(self.grid_points):
+            raise ValueError(f"Velocity field size mismatch in {self.time_files[time_idx]}: "
+                             f"expected {len(self.grid_points)}, got {len(v)}")
+        self.velocity_cache[time_idx] = v
+        while len(self.velocity_cache) > self.cache_size_limit:
+            self.velocity_cache.pop(next(iter(self.velocity_cache)))
+        return v
+
+    def __getitem__(self, time_idx: int) -> np.ndarray:
+        return self.load_single_timestep(time_idx)
+
+    def load_time_series(self, start_idx: int = 0, end_idx: Optional[int] = None) -> Dict[str, Any]:
+        end = len(self.time_files) if end_idx is None else min(end_idx, len(self.time_files))
+        if end - start_idx <= 0:
+            raise ValueError(f"Invalid time range: [{start_idx}, {end})")
+        first = self.load_single_timestep(start_idx)
+        data = np.empty((end - start_idx, len(first), 3), dtype=F32)
+        for k, i in enumerate(range(start_idx, end)):
+            data[k] = self.load_single_timestep(i)
+        return {"velocity_data": data, "positions": self.grid_points,
+                "times": np.arange(start_idx, end, dtype=F32), "source": "vtk_unstructured_series",
+                "file_pattern": self.file_pattern, "velocity_field_name": self.velocity_field_name}
+
+    def tetrahedra(self) -> np.ndarray:
+        """(M, 4) int32 vertex ids of the VTK_TETRA cells of the first file."""
+        if self.grid_points is None:
+            self.load_single_timestep(0)
+        c = self._cells
+        if not c:
+            return np.zeros((0, 4), dtype=np.int32)
+        types = np.asarray(c["types"])
+        offs = np.asarray(c["offsets"], dtype=np.int64)
+        conn = np.asarray(c["connectivity"], dtype=np.int64)
+        starts = np.concatenate([[0], offs[:-1]])
+        sel = (types == VTK_TETRA) & (offs - starts == 4)
+        idx = starts[sel][:, None] + np.arange(4)[None, :]
+        return conn[idx].astype(np.int32)
+
+    def get_bounds(self) -> Tuple[float, ...]:
+        if self.grid_points is None:
+            self.load_single_timestep(0)
+        lo, hi = self.grid_points.min(axis=0), self.grid_points.max(axis=0)
+        return tuple(float(v) for v in (*lo, *hi))
+
+    def get_grid_info(self) -> Dict[str, Any]:
+        if self.grid_points is None:
+            self.load_single_timestep(0)
+        return {"n_points": int(len(self.grid_points)), "bounds": self.get_bounds(),
+                "n_timesteps": len(self.time_files), "velocity_field": self.velocity_field_name}
+
+
+def open_vtk_time_series(file_pattern: str, max_time_steps: Optional[int] = None,
+                         velocity_field_name: Optional[str] = None, validate_files: bool = True,
+                         **kwargs) -> Dict[str, Any]:
+    """vtk_reader.py:944-988: the whole series in JAXTrace format."""
+    reader = VTKUnstructuredTimeSeriesReader(file_pattern, max_time_steps=max_time_steps,
+                                             velocity_field_name=velocity_field_name, **kwargs)
+    return reader.load_time_series()
+
+
+def write_vtu(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
+              point_data: Optional[Dict[str, np.ndarray]] = None, encoding: str = "appended",
+              compress: bool = False, header: str = "UInt64") -> None:
+    """Write an UnstructuredGrid .vtu (tetrahedra only) with point data.
+    encoding: "appended" (raw), "binary" (base64) or "ascii"."""
+    pts = np.ascontiguousarray(points, dtype=F32).reshape(-1, 3)
+    t4 = np.zeros((0, 4), np.int64) if tets is None else np.asarray(tets, dtype=np.int64).reshape(-1, 4)
+    arrays: List[Tuple[str, str, np.ndarray, int]] = [("Points", "Points", pts, 3)]
+    arrays += [("Cells", "connectivity", t4.reshape(-1), 1),
+               ("Cells", "offsets", 4 * np.arange(1, len(t4) + 1, dtype=np.int64), 1),
+               ("Cells", "types", np.full(len(t4), VTK_TETRA, dtype=np.uint8), 1)]
+    for k, v in (point_data or {}).items():
+        v = np.ascontiguousarray(v)
+        arrays.append(("PointData", k, v.reshape(len(pts), -1) if v.ndim > 1 else v, v.shape[1] if v.ndim > 1 else 1))
+    hdt = np.dtype(np.uint64 if header == "UInt64" else np.uint32).newbyteorder("<")
+
+    def blob(a: np.ndarray) -> bytes:
+        data = np.ascontiguousarray(a).astype(a.dtype.newbyteorder("<")).tobytes()
+        if not compress:
+            return np.array([len(data)], dtype=hdt).tobytes() + data
+        comp = zlib.compress(data)
+        return np.array([1, len(data), len(data), len(comp)], dtype=hdt).tobytes() + comp
+
+    appended = bytearray()
+    sections: Dict[str, List[str]] = {"Points": [], "Cells": [], "PointData": []}
+    for sec, name, a, nc in arrays:
+        attrs = f'type="{_NAMES[np.dtype(a.dtype).newbyteorder("=")]}" Name="{name}" NumberOfComponents="{nc}"'
+        if encoding == "ascii":
+            body = " ".join(repr(x) if a.dtype.kind == "f" else str(x) for x in a.reshape(-1).tolist())
+            sections[sec].append(f'<DataArray {attrs} format="ascii">{body}</DataArray>')
+        elif encoding == "binary":
+            if compress:
+                b = blob(a)
+                hs = hdt.itemsize * 4
+                text = base64.b64encode(b[:hs]).decode() + base64.b64encode(b[hs:]).decode()
+            else:
+                text = base64.b64encode(blob(a)).decode()
+            sections[sec].append(f'<DataArray {attrs} format="binary">{text}</DataArray>')
+        else:
+            sections[sec].append(f'<DataArray {attrs} format="appended" offset="{len(appended)}"/>')
+            appended += blob(a)
+    comp = ' compressor="vtkZLibDataCompressor"' if compress else ""
+    head = (f'<?xml version="1.0"?>\n<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" '
+            f'header_type="{header}"{comp}>\n<UnstructuredGrid>\n'
+            f'<Piece NumberOfPoints="{len(pts)}" NumberOfCells="{len(t4)}">\n'
+            f'<PointData>{"".join(sections["PointData"])}</PointData>\n'
+            f'<Points>{"".join(sections["Points"])}</Points>\n<Cells>{"".join(sections["Cells"])}</Cells>\n'
+            f'</Piece>\n</UnstructuredGrid>\n')
+    with open(path, "wb") as fh:
+        fh.write(head.encode())
+        if encoding == "appended":
+            fh.write(b'<AppendedData encoding="raw">\n_')
+            fh.write(bytes(appended))
+            fh.write(b"\n</AppendedData>\n")
+        fh.write(b"</VTKFile>\n")
+
+
+def write_pvtu(path: str, sources: List[str], point_arrays: Dict[str, Tuple[str, int]]) -> None:
+    """A .pvtu naming existing .vtu pieces (paths relative to the .pvtu)."""
+    pd = "".join(f'<PDataArray type="{t}" Name="{n}" NumberOfComponents="{c}"/>' for n, (t, c) in point_arrays.items())
+    pieces = "".join(f'<Piece Source="{s}"/>' for s in sources)
+    with open(path, "w") as fh:
+        fh.write(f'<?xml version="1.0"?>\n<VTKFile type="PUnstructuredGrid" version="1.0" byte_order="LittleEndian">\n'
+                 f'<PUnstructuredGrid GhostLevel="0"><PPointData>{pd}</PPointData>'
+                 f'<PPoints><PDataArray type="Float32" NumberOfComponents="3"/></PPoints>{pieces}'
+                 f'</PUnstructuredGrid>\n</VTKFile>\n')
