@@ -16,6 +16,7 @@ from .analysis import compute_mixing_metrics
 from .seeding import random_seeds, uniform_grid_seeds
 from .tracker import EnsembleBatch, ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
 from .autotune import Autotuner
+from .vtk_io import VTKTrajectorySeries, VTKTrajectoryWriter, VTKUnstructuredTimeSeriesReader, open_vtk_time_series
 
 __version__ = "0.1.0"
 
@@ -26,5 +27,6 @@ __all__ = [
     "reflective_boundary", "clamping_boundary", "absorbing_boundary_factory", "mixed_boundary",
     "continuous_inlet_boundary_factory", "no_boundary", "unit_box_periodic", "unit_box_reflective",
     "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid", "compute_trajectory_statistics",
-    "compute_mixing_metrics",
+    "compute_mixing_metrics", "VTKTrajectoryWriter", "VTKTrajectorySeries", "VTKUnstructuredTimeSeriesReader",
+    "open_vtk_time_series",
 ]

@@ -118,6 +118,31 @@ class Trajectory:
         flat = self.positions.reshape(-1, 3)
         return np.min(flat, axis=0), np.max(flat, axis=0)
 
+    def export_to_vtk(self, filename: str, time_indices=None, encoding: str = "appended") -> None:
+        """Write the selected rows as one .vtu of vertex cells
+        (particles.py:448-539): points in row-major (row, particle) order,
+        point arrays Velocity (stored, or the float32 difference quotient to
+        the previous row, zero on row 0), Time, ParticleID and Speed.
+        Written by ``vtk_io.write_vtu``; no VTK library needed."""
+        from .vtk_io import write_vtu
+        idx = np.arange(self.T) if time_indices is None else np.asarray(list(time_indices), dtype=np.int64)
+        pos = self.positions[idx].reshape(-1, 3)
+        if self.velocities is not None:
+            vel = self.velocities[idx]
+        else:
+            vel = np.zeros((len(idx), self.N, 3), dtype=F32)
+            later = idx > 0
+            if later.any():
+                t = idx[later]
+                dt = (self.times[t] - self.times[t - 1]).astype(F32)
+                vel[later] = (self.positions[t] - self.positions[t - 1]) / dt[:, None, None]
+        vel = vel.reshape(-1, 3).astype(F32)
+        times = np.repeat(self.times[idx], self.N).astype(F32)
+        ids = np.tile(np.arange(self.N, dtype=np.int32), len(idx))
+        speed = np.linalg.norm(vel, axis=1).astype(F32)
+        write_vtu(filename, pos, point_data={"Velocity": vel, "Time": times, "ParticleID": ids, "Speed": speed},
+                  encoding=encoding, vertices=True)
+
     def subsample_time(self, step: int = 2) -> "Trajectory":
         return Trajectory(positions=self.positions[::step], times=self.times[::step],
                           velocities=self.velocities[::step] if self.velocities is not None else None,

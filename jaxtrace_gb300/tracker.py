@@ -8,6 +8,8 @@ written straight into a device trajectory slab that streams to the host.
 """
 from __future__ import annotations
 
+import collections
+
 import ctypes as C
 from dataclasses import dataclass, field as dc_field
 from typing import Any, Callable, Dict, List, Optional, Tuple
@@ -65,6 +67,13 @@ class TrackerOptions:
     record_path_length accumulate each particle's path length over every step
                        in the tracking kernel (Trajectory.path_length; what
                        compute_path_length gives on an every-step recording)
+    row_sink           callable(first_row, positions, velocities, row_times)
+                       handed every row of the trajectory once, in order, on a
+                       writer thread as soon as the row is in host memory
+                       (e.g. ``vtk_io.VTKTrajectorySeries``); recorded slabs
+                       are copied to the host on a side stream while the next
+                       time chunk runs, so with ``time_chunk`` set the export
+                       overlaps the tracking
     """
     max_memory_gb: float = 8.0
     batch_size: Optional[int] = None
@@ -98,6 +107,7 @@ class TrackerOptions:
     stage_fields: bool = True
     stage_chunk: int = 32
     stage_overlap: bool = True
+    row_sink: Optional[Callable[[int, np.ndarray, Optional[np.ndarray], np.ndarray], None]] = None
     record_path_length: bool = False
 
     def estimate_batch_size(self, n_particles: int, n_timesteps: int) -> int:
@@ -231,16 +241,28 @@ class ParticleTracker:
 
         row0 = threading.Thread(target=copy_row0)
         row0.start()
+        rows_out = None
+        if self.options.row_sink is not None:
+            rows_out = _RowStream(self.options.row_sink, positions, velocities, times[row_idx])
+            rows_out.put(0, 1, row0)
+        ran = False
         try:
-            n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities)
+            n_chunks = self._run(pos, times, dt, k, compact, n_rows, positions, velocities, rows_out)
+            ran = True
         finally:
             row0.join()
+            if rows_out is not None and (failed or not ran):
+                rows_out.close(raise_error=False)
         if failed:
             raise failed[0]
         if compact and self.options.record_final_only and T > 1:
             torch.from_numpy(positions[-1]).copy_(pos)        # device -> final row, no staging array
             if velocities is not None:
                 torch.from_numpy(velocities[-1]).copy_(self._field.sample_at_positions(pos, times[-1]))
+            if rows_out is not None:
+                rows_out.put(n_rows - 1, 1)
+        if rows_out is not None:
+            rows_out.close()
         traj = self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, n_chunks)
         if self.options.record_path_length:
             traj.path_length = getattr(self, "_last_path_length", None)
@@ -312,8 +334,10 @@ class ParticleTracker:
         return _Engine(self, pos, len(times) - 1, dt, sched_dev, status, comp, self._sort_every(pos.shape[0]),
                        ens=ens)
 
-    def _run(self, pos, times, dt, k, compact, n_rows, positions, velocities) -> int:
-        """Advance ``pos`` (device, (N,3)) through all steps, filling rows 1.. of the outputs."""
+    def _run(self, pos, times, dt, k, compact, n_rows, positions, velocities, rows_out=None) -> int:
+        """Advance ``pos`` (device, (N,3)) through all steps, filling rows 1..
+        of the outputs.  Each recorded slab is copied to the host on a side
+        stream while the next chunk runs; at most two slabs are alive."""
         import torch
         n = pos.shape[0]
         n_steps = len(times) - 1
@@ -329,28 +353,45 @@ class ParticleTracker:
         if self.options.time_chunk:
             chunk = max(1, min(chunk, int(self.options.time_chunk)))
         cb = self.options.progress_callback
-        s = 0
-        while s < n_steps:
-            e = min(s + chunk, n_steps)
-            slab = vslab = None
-            rec = None
-            if record:
-                # rows written by steps s..e-1 are the counts c in (s, e]
-                r0, r1 = (s // k + 1, e // k) if compact else (s + 1, e)
-                nr = max(r1 - r0 + 1, 0)
-                if nr > 0:
-                    slab = torch.zeros((nr, n, 3), dtype=torch.float32, device="cuda")
-                    if velocities is not None:
-                        vslab = torch.zeros_like(slab)
-                rec = (slab, vslab, k, compact, r0, nr)
-            eng.advance(s, e, rec)
-            if slab is not None:
-                torch.from_numpy(positions[r0:r0 + nr]).copy_(slab)
-                if vslab is not None:
-                    torch.from_numpy(velocities[r0:r0 + nr]).copy_(vslab)
-            s = e
+        copy_stream = torch.cuda.Stream() if record else None
+        inflight = collections.deque()       # (copy-done event or None, end step)
+
+        def land(ev, end):
+            if ev is not None:
+                ev.synchronize()
             if cb is not None:
-                cb(s / n_steps)
+                cb(end / n_steps)
+
+        s = 0
+        try:
+            while s < n_steps:
+                e = min(s + chunk, n_steps)
+                slab = vslab = None
+                rec = None
+                if record:
+                    # rows written by steps s..e-1 are the counts c in (s, e]
+                    r0, r1 = (s // k + 1, e // k) if compact else (s + 1, e)
+                    nr = max(r1 - r0 + 1, 0)
+                    if nr > 0:
+                        slab = torch.zeros((nr, n, 3), dtype=torch.float32, device="cuda")
+                        if velocities is not None:
+                            vslab = torch.zeros_like(slab)
+                    rec = (slab, vslab, k, compact, r0, nr)
+                eng.advance(s, e, rec)
+                ev = None
+                if slab is not None:
+                    ev = _copy_rows_async(slab, vslab, positions, velocities, r0, copy_stream)
+                    if rows_out is not None:
+                        rows_out.put(r0, nr, ev)
+                inflight.append((ev, e))
+                while len(inflight) > 1:
+                    land(*inflight.popleft())
+                s = e
+            while inflight:
+                land(*inflight.popleft())
+        finally:
+            if copy_stream is not None:
+                copy_stream.synchronize()
         eng.finish()
         self.last_status = int(eng.status.item())
         self._last_path_length = eng.path.cpu().numpy() if eng.path is not None else None
@@ -836,6 +877,65 @@ def _stage_scales(src) -> np.ndarray:
     bound = np.where(lerp, (sa + sb) * (1.0 + wb), wa + wb)
     bound = np.where(bound > 0, bound, 1.0)
     return np.exp2(np.ceil(np.log2(bound))).astype(F32)
+
+
+def _copy_rows_async(slab, vslab, positions, velocities, r0: int, copy_stream):
+    """Copy a recorded slab into host rows r0.. on ``copy_stream`` once the
+    current stream has written it; returns the copy's completion event."""
+    import torch
+    written = torch.cuda.Event()
+    written.record()
+    copy_stream.wait_event(written)
+    nr = slab.shape[0]
+    with torch.cuda.stream(copy_stream):
+        torch.from_numpy(positions[r0:r0 + nr]).copy_(slab, non_blocking=True)
+        slab.record_stream(copy_stream)
+        if vslab is not None:
+            torch.from_numpy(velocities[r0:r0 + nr]).copy_(vslab, non_blocking=True)
+            vslab.record_stream(copy_stream)
+    done = torch.cuda.Event()
+    done.record(copy_stream)
+    return done
+
+
+class _RowStream:
+    """Hands trajectory rows to ``TrackerOptions.row_sink`` on a writer
+    thread, in the order they are put, each once its copy has landed (a CUDA
+    event, or the thread that writes it)."""
+
+    def __init__(self, sink, positions, velocities, row_times):
+        import queue
+        import threading
+        self.sink, self.pos, self.vel, self.times = sink, positions, velocities, np.asarray(row_times, dtype=F32)
+        self.q = queue.Queue()
+        self.error = None
+        self.thread = threading.Thread(target=self._work, daemon=True)
+        self.thread.start()
+
+    def put(self, r0: int, nr: int, ready=None) -> None:
+        self.q.put((r0, nr, ready))
+
+    def _work(self):
+        while True:
+            item = self.q.get()
+            if item is None:
+                return
+            r0, nr, ready = item
+            try:
+                if ready is not None:
+                    ready.join() if hasattr(ready, "join") else ready.synchronize()
+                if self.error is None:
+                    self.sink(r0, self.pos[r0:r0 + nr], None if self.vel is None else self.vel[r0:r0 + nr],
+                              self.times[r0:r0 + nr])
+            except BaseException as exc:       # re-raised by close() on the caller's thread
+                if self.error is None:
+                    self.error = exc
+
+    def close(self, raise_error: bool = True) -> None:
+        self.q.put(None)
+        self.thread.join()
+        if raise_error and self.error is not None:
+            raise self.error
 
 
 # Trajectory arrays up to this size live in pinned host memory: device

@@ -19,6 +19,7 @@ import base64
 import glob
 import os
 import re
+import warnings
 import xml.etree.ElementTree as ET
 import zlib
 from typing import Any, Dict, List, Optional, Tuple
@@ -26,6 +27,7 @@ from typing import Any, Dict, List, Optional, Tuple
 import numpy as np
 
 F32 = np.float32
+VTK_VERTEX = 1
 VTK_TETRA = 10
 
 _TYPES = {"Int8": np.int8, "UInt8": np.uint8, "Int16": np.int16, "UInt16": np.uint16, "Int32": np.int32,
@@ -113,22 +115,30 @@ class _Blob:
 
 
 def _read_piece(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
-    """One .vtu file; without ``geometry`` the points and cells are left
-    undecoded, and with ``names`` only those point arrays are decoded."""
+    """One .vtu (or .vtp) file; without ``geometry`` the points and cells
+    are left undecoded, and with ``names`` only those point arrays are
+    decoded.  PolyData cells come as {"verts": {...}, "lines": {...}}."""
     raw = open(path, "rb").read()
     # raw appended data is not XML: parse the part before it, closed
     app_at = raw.find(b"<AppendedData")
     root = ET.fromstring(raw if app_at < 0 else raw[:app_at] + b"</VTKFile>")
-    if root.get("type") != "UnstructuredGrid":
-        raise ValueError(f"{path}: not an UnstructuredGrid file ({root.get('type')})")
+    kind = root.get("type")
+    if kind not in ("UnstructuredGrid", "PolyData"):
+        raise ValueError(f"{path}: not an UnstructuredGrid or PolyData file ({kind})")
     blob = _Blob(root, raw, app_at)
-    piece = root.find("UnstructuredGrid/Piece")
+    piece = root.find(f"{kind}/Piece")
     n_points = int(piece.get("NumberOfPoints", "0"))
     pts, cells = None, {}
     if geometry:
         pts = np.asarray(blob.array(piece.find("Points/DataArray")), dtype=F32).reshape(-1, 3)
-        for el in piece.findall("Cells/DataArray"):
-            cells[el.get("Name")] = blob.array(el)
+        if kind == "UnstructuredGrid":
+            for el in piece.findall("Cells/DataArray"):
+                cells[el.get("Name")] = blob.array(el)
+        else:
+            for sec in ("Verts", "Lines", "Strips", "Polys"):
+                d = {el.get("Name"): blob.array(el) for el in piece.findall(f"{sec}/DataArray")}
+                if d:
+                    cells[sec.lower()] = d
     pdata = {}
     pd = piece.find("PointData")
     if pd is not None:
@@ -137,7 +147,8 @@ def _read_piece(path: str, geometry: bool = True, names: Optional[List[str]] = N
                 pdata[el.get("Name")] = blob.array(el)
             else:
                 pdata[el.get("Name")] = None          # present, not decoded
-    return {"points": pts, "n_points": n_points, "cells": cells, "point_data": pdata}
+    cdata = {el.get("Name"): blob.array(el) for el in piece.findall("CellData/DataArray")}
+    return {"points": pts, "n_points": n_points, "cells": cells, "point_data": pdata, "cell_data": cdata}
 
 
 def read_vtk_xml(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
@@ -303,20 +314,12 @@ def open_vtk_time_series(file_pattern: str, max_time_steps: Optional[int] = None
     return reader.load_time_series()
 
 
-def write_vtu(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
-              point_data: Optional[Dict[str, np.ndarray]] = None, encoding: str = "appended",
-              compress: bool = False, header: str = "UInt64") -> None:
-    """Write an UnstructuredGrid .vtu (tetrahedra only) with point data.
-    encoding: "appended" (raw), "binary" (base64) or "ascii"."""
-    pts = np.ascontiguousarray(points, dtype=F32).reshape(-1, 3)
-    t4 = np.zeros((0, 4), np.int64) if tets is None else np.asarray(tets, dtype=np.int64).reshape(-1, 4)
-    arrays: List[Tuple[str, str, np.ndarray, int]] = [("Points", "Points", pts, 3)]
-    arrays += [("Cells", "connectivity", t4.reshape(-1), 1),
-               ("Cells", "offsets", 4 * np.arange(1, len(t4) + 1, dtype=np.int64), 1),
-               ("Cells", "types", np.full(len(t4), VTK_TETRA, dtype=np.uint8), 1)]
-    for k, v in (point_data or {}).items():
-        v = np.ascontiguousarray(v)
-        arrays.append(("PointData", k, v.reshape(len(pts), -1) if v.ndim > 1 else v, v.shape[1] if v.ndim > 1 else 1))
+def _write_xml(path: str, kind: str, counts: Dict[str, int], sections: List[Tuple[str, List[Tuple[str, np.ndarray]]]],
+               encoding: str, compress: bool, header: str) -> None:
+    """One-piece VTK XML file of type ``kind`` (UnstructuredGrid or
+    PolyData): ``sections`` in file order, each a list of (name, array) with
+    (M,) or (M,C) arrays; a section name may carry attributes
+    ('PointData Scalars="Time"')."""
     hdt = np.dtype(np.uint64 if header == "UInt64" else np.uint32).newbyteorder("<")
 
     def blob(a: np.ndarray) -> bytes:
@@ -327,30 +330,32 @@ def write_vtu(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
         return np.array([1, len(data), len(data), len(comp)], dtype=hdt).tobytes() + comp
 
     appended = bytearray()
-    sections: Dict[str, List[str]] = {"Points": [], "Cells": [], "PointData": []}
-    for sec, name, a, nc in arrays:
-        attrs = f'type="{_NAMES[np.dtype(a.dtype).newbyteorder("=")]}" Name="{name}" NumberOfComponents="{nc}"'
-        if encoding == "ascii":
-            body = " ".join(repr(x) if a.dtype.kind == "f" else str(x) for x in a.reshape(-1).tolist())
-            sections[sec].append(f'<DataArray {attrs} format="ascii">{body}</DataArray>')
-        elif encoding == "binary":
-            if compress:
+    body = []
+    for sec, arrays in sections:
+        parts = []
+        for name, a in arrays:
+            a = np.ascontiguousarray(a)
+            nc = a.shape[1] if a.ndim > 1 else 1
+            attrs = f'type="{_NAMES[np.dtype(a.dtype).newbyteorder("=")]}" Name="{name}" NumberOfComponents="{nc}"'
+            if encoding == "ascii":
+                text = " ".join(repr(x) if a.dtype.kind == "f" else str(x) for x in a.reshape(-1).tolist())
+                parts.append(f'<DataArray {attrs} format="ascii">{text}</DataArray>')
+            elif encoding == "binary":
                 b = blob(a)
-                hs = hdt.itemsize * 4
-                text = base64.b64encode(b[:hs]).decode() + base64.b64encode(b[hs:]).decode()
+                if compress:
+                    hs = hdt.itemsize * 4
+                    text = base64.b64encode(b[:hs]).decode() + base64.b64encode(b[hs:]).decode()
+                else:
+                    text = base64.b64encode(b).decode()
+                parts.append(f'<DataArray {attrs} format="binary">{text}</DataArray>')
             else:
-                text = base64.b64encode(blob(a)).decode()
-            sections[sec].append(f'<DataArray {attrs} format="binary">{text}</DataArray>')
-        else:
-            sections[sec].append(f'<DataArray {attrs} format="appended" offset="{len(appended)}"/>')
-            appended += blob(a)
+                parts.append(f'<DataArray {attrs} format="appended" offset="{len(appended)}"/>')
+                appended += blob(a)
+        body.append(f'<{sec}>{"".join(parts)}</{sec.split()[0]}>\n')
     comp = ' compressor="vtkZLibDataCompressor"' if compress else ""
-    head = (f'<?xml version="1.0"?>\n<VTKFile type="UnstructuredGrid" version="1.0" byte_order="LittleEndian" '
-            f'header_type="{header}"{comp}>\n<UnstructuredGrid>\n'
-            f'<Piece NumberOfPoints="{len(pts)}" NumberOfCells="{len(t4)}">\n'
-            f'<PointData>{"".join(sections["PointData"])}</PointData>\n'
-            f'<Points>{"".join(sections["Points"])}</Points>\n<Cells>{"".join(sections["Cells"])}</Cells>\n'
-            f'</Piece>\n</UnstructuredGrid>\n')
+    piece = " ".join(f'{k}="{v}"' for k, v in counts.items())
+    head = (f'<?xml version="1.0"?>\n<VTKFile type="{kind}" version="1.0" byte_order="LittleEndian" '
+            f'header_type="{header}"{comp}>\n<{kind}>\n<Piece {piece}>\n{"".join(body)}</Piece>\n</{kind}>\n')
     with open(path, "wb") as fh:
         fh.write(head.encode())
         if encoding == "appended":
@@ -358,6 +363,52 @@ def write_vtu(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
             fh.write(bytes(appended))
             fh.write(b"\n</AppendedData>\n")
         fh.write(b"</VTKFile>\n")
+
+
+def write_vtu(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
+              point_data: Optional[Dict[str, np.ndarray]] = None, encoding: str = "appended",
+              compress: bool = False, header: str = "UInt64", vertices: bool = False) -> None:
+    """Write an UnstructuredGrid .vtu with point data: tetrahedra ``tets``,
+    or with ``vertices`` one VTK_VERTEX cell per point.
+    encoding: "appended" (raw), "binary" (base64) or "ascii"."""
+    pts = np.ascontiguousarray(points, dtype=F32).reshape(-1, 3)
+    if vertices:
+        conn = np.arange(len(pts), dtype=np.int64)
+        offs = np.arange(1, len(pts) + 1, dtype=np.int64)
+        types = np.full(len(pts), VTK_VERTEX, dtype=np.uint8)
+    else:
+        t4 = np.zeros((0, 4), np.int64) if tets is None else np.asarray(tets, dtype=np.int64).reshape(-1, 4)
+        conn, offs = t4.reshape(-1), 4 * np.arange(1, len(t4) + 1, dtype=np.int64)
+        types = np.full(len(t4), VTK_TETRA, dtype=np.uint8)
+    pdata = [(k, np.asarray(v).reshape(len(pts), -1) if np.ndim(v) > 1 else np.asarray(v))
+             for k, v in (point_data or {}).items()]
+    _write_xml(path, "UnstructuredGrid", {"NumberOfPoints": len(pts), "NumberOfCells": len(types)},
+               [("PointData", pdata), ("Points", [("Points", pts)]),
+                ("Cells", [("connectivity", conn), ("offsets", offs), ("types", types)])],
+               encoding, compress, header)
+
+
+def write_vtp(path: str, points: np.ndarray, verts: Optional[Tuple[np.ndarray, np.ndarray]] = None,
+              lines: Optional[Tuple[np.ndarray, np.ndarray]] = None,
+              point_data: Optional[Dict[str, np.ndarray]] = None, cell_data: Optional[Dict[str, np.ndarray]] = None,
+              encoding: str = "appended", compress: bool = False, header: str = "UInt64",
+              point_scalars: Optional[str] = None, cell_scalars: Optional[str] = None) -> None:
+    """Write a PolyData .vtp: ``verts`` and ``lines`` are (connectivity,
+    offsets) pairs (offsets = running end of each cell's point list);
+    ``cell_data`` arrays run over the verts and then the lines;
+    ``point_scalars`` / ``cell_scalars`` name the active scalar arrays."""
+    pts = np.ascontiguousarray(points, dtype=F32).reshape(-1, 3)
+    empty = (np.zeros(0, np.int64), np.zeros(0, np.int64))
+    vc, vo = [np.asarray(a, dtype=np.int64) for a in (verts or empty)]
+    lc, lo = [np.asarray(a, dtype=np.int64) for a in (lines or empty)]
+    pdata = [(k, np.asarray(v)) for k, v in (point_data or {}).items()]
+    cdata = [(k, np.asarray(v)) for k, v in (cell_data or {}).items()]
+    _write_xml(path, "PolyData", {"NumberOfPoints": len(pts), "NumberOfVerts": len(vo), "NumberOfLines": len(lo),
+                                  "NumberOfStrips": 0, "NumberOfPolys": 0},
+               [("PointData" + (f' Scalars="{point_scalars}"' if point_scalars else ""), pdata),
+                ("CellData" + (f' Scalars="{cell_scalars}"' if cell_scalars else ""), cdata), ("Points", [("Points", pts)]),
+                ("Verts", [("connectivity", vc), ("offsets", vo)]), ("Lines", [("connectivity", lc), ("offsets", lo)])],
+               encoding, compress, header)
 
 
 def write_pvtu(path: str, sources: List[str], point_arrays: Dict[str, Tuple[str, int]]) -> None:
@@ -369,3 +420,126 @@ def write_pvtu(path: str, sources: List[str], point_arrays: Dict[str, Tuple[str,
                  f'<PUnstructuredGrid GhostLevel="0"><PPointData>{pd}</PPointData>'
                  f'<PPoints><PDataArray type="Float32" NumberOfComponents="3"/></PPoints>{pieces}'
                  f'</PUnstructuredGrid>\n</VTKFile>\n')
+
+
+class VTKTrajectoryWriter:
+    """Trajectory files for ParaView (io/vtk_writer.py:58-300), written
+    without the VTK library as zlib-compressed PolyData .vtp files."""
+
+    def __init__(self, output_dir: str):
+        self.output_dir = os.fspath(output_dir)
+        os.makedirs(self.output_dir, exist_ok=True)
+
+    def write_trajectory_points(self, trajectory_positions: np.ndarray, times: np.ndarray,
+                                filename: str = "particle_trajectories.vtp",
+                                particle_data: Optional[Dict[str, np.ndarray]] = None,
+                                time_subset: Optional[slice] = None) -> str:
+        """Every (row, particle) position as a vertex (vtk_writer.py:84-197):
+        point arrays Time, ParticleID and TimeStep (float32), plus each
+        ``particle_data`` array of shape (N,) (repeated per row) or (T, N);
+        other shapes are skipped with a warning.  ``time_subset`` slices
+        the rows, and the (T, N) arrays with them."""
+        pos = np.asarray(trajectory_positions, dtype=F32)
+        times = np.asarray(times)
+        T_all, N = pos.shape[0], pos.shape[1]
+        if time_subset is not None:
+            pos, times = pos[time_subset], times[time_subset]
+        T = pos.shape[0]
+        pts = pos.reshape(-1, 3)
+        if pts.ndim != 2 or pts.shape[1] != 3:
+            raise ValueError(f"Positions must have 3 coordinates, got shape {pos.shape}")
+        n = T * N
+        pdata = {"Time": np.repeat(times, N).astype(F32),
+                 "ParticleID": np.tile(np.arange(N, dtype=F32), T),
+                 "TimeStep": np.repeat(np.arange(T, dtype=F32), N)}
+        for name, data in (particle_data or {}).items():
+            d = np.asarray(data, dtype=F32)
+            if time_subset is not None and d.ndim == 2 and d.shape[0] == T_all:
+                d = d[time_subset]
+            if d.ndim == 1 and len(d) == N:
+                pdata[name] = np.tile(d, T)
+            elif d.ndim == 2 and d.shape == (T, N):
+                pdata[name] = d.ravel()
+            else:
+                warnings.warn(f"Skipping data '{name}' - incompatible shape {d.shape}")
+        path = os.path.join(self.output_dir, filename)
+        write_vtp(path, pts, verts=(np.arange(n), np.arange(1, n + 1)), point_data=pdata, compress=True,
+                  point_scalars="Time")
+        return path
+
+    def write_trajectory_lines(self, trajectory_positions: np.ndarray, times: np.ndarray,
+                               filename: str = "particle_paths.vtp", max_particles: Optional[int] = None,
+                               particle_subset: Optional[np.ndarray] = None) -> str:
+        """One polyline per particle through its rows (vtk_writer.py:199-300):
+        points row-major over the selected particles, point arrays Time and
+        ParticleID (float32), cell array PathLength (float32 sum of the
+        segment lengths).  ``max_particles`` keeps linspace(0, N-1, m)
+        particles; ``particle_subset`` names them."""
+        pos = np.asarray(trajectory_positions, dtype=F32)
+        T, N = pos.shape[0], pos.shape[1]
+        if particle_subset is not None:
+            idx = np.asarray(particle_subset)
+        elif max_particles is not None and N > max_particles:
+            idx = np.linspace(0, N - 1, max_particles, dtype=int)
+        else:
+            idx = np.arange(N)
+        ns = len(idx)
+        sel = pos[:, idx, :]
+        conn = (np.arange(T, dtype=np.int64)[None, :] * ns + np.arange(ns, dtype=np.int64)[:, None]).ravel()
+        offs = T * np.arange(1, ns + 1, dtype=np.int64)
+        # per particle, a contiguous float32 sum of its segment lengths
+        seg = np.linalg.norm(np.diff(sel, axis=0), axis=2)
+        plen = np.sum(np.ascontiguousarray(seg.T), axis=1).astype(F32) if T > 1 else np.zeros(ns, F32)
+        path = os.path.join(self.output_dir, filename)
+        write_vtp(path, sel.reshape(-1, 3), lines=(conn, offs),
+                  point_data={"Time": np.repeat(np.asarray(times), ns).astype(F32),
+                              "ParticleID": np.tile(idx.astype(F32), T)},
+                  cell_data={"PathLength": plen}, compress=True, point_scalars="Time", cell_scalars="PathLength")
+        return path
+
+
+def write_pvd(path: str, files: List[str], times) -> None:
+    """A .pvd collection of ``files`` (relative to the .pvd) at ``times``
+    (io/vtk_writer.py:609-626)."""
+    with open(path, "w") as fh:
+        fh.write('<?xml version="1.0"?>\n<VTKFile type="Collection" version="0.1">\n  <Collection>\n')
+        for f, t in zip(files, times):
+            fh.write(f'    <DataSet timestep="{float(t):.6f}" file="{f}"/>\n')
+        fh.write("  </Collection>\n</VTKFile>\n")
+
+
+class VTKTrajectorySeries:
+    """A ``TrackerOptions.row_sink`` that streams a trajectory to disk while
+    it is tracked: each row as ``{prefix}_{row:04d}.vtu`` (one vertex per
+    particle; point arrays Time, ParticleID and, when velocities are
+    recorded, Velocity and Speed -- the per-row content of
+    Trajectory.export_to_vtk) and, on ``close()``, the ``{prefix}.pvd``
+    collection over them."""
+
+    def __init__(self, output_dir: str, prefix: str = "particles", encoding: str = "appended",
+                 compress: bool = False):
+        self.output_dir = os.fspath(output_dir)
+        os.makedirs(self.output_dir, exist_ok=True)
+        self.prefix, self.encoding, self.compress = prefix, encoding, compress
+        self.files: List[str] = []
+        self.times: List[float] = []
+
+    def __call__(self, first_row: int, positions: np.ndarray, velocities: Optional[np.ndarray],
+                 row_times: np.ndarray) -> None:
+        for i in range(len(positions)):
+            n = positions.shape[1]
+            pdata = {"Time": np.full(n, row_times[i], dtype=F32), "ParticleID": np.arange(n, dtype=np.int32)}
+            if velocities is not None:
+                v = np.asarray(velocities[i], dtype=F32)
+                pdata["Velocity"] = v
+                pdata["Speed"] = np.linalg.norm(v, axis=1).astype(F32)
+            name = f"{self.prefix}_{first_row + i:04d}.vtu"
+            write_vtu(os.path.join(self.output_dir, name), positions[i], point_data=pdata, encoding=self.encoding,
+                      compress=self.compress, vertices=True)
+            self.files.append(name)
+            self.times.append(float(row_times[i]))
+
+    def close(self) -> str:
+        path = os.path.join(self.output_dir, f"{self.prefix}.pvd")
+        write_pvd(path, self.files, self.times)
+        return path

@@ -159,6 +159,52 @@ def test_time_chunks_and_compact_recording(golden):
 
 
 # ---------------------------------------------------------------- octree
+@pytest.mark.parametrize("opts", [dict(time_chunk=7), dict(time_chunk=5, record_every=3),
+                                  dict(record_final_only=True),
+                                  dict(time_chunk=4, record_velocities=True, recording_interval=2)])
+def test_row_sink_streams_every_row_once_in_order(golden, opts):
+    """Slabs copied on the side stream land in the same rows as the
+    reference trajectory, and the sink sees every row once, in order."""
+    g = golden("track_grid")
+    f = jt.StructuredTimeSeriesField(g["D"], g["st"], g["g"], g["g"], g["g"], "periodic")
+    bc = jt.periodic_boundary(((0, 0, 0), (1, 1, 1)))
+    got = []
+
+    def sink(r0, pos, vel, t):
+        got.append((r0, pos.copy(), None if vel is None else vel.copy(), t.copy()))
+
+    traj = jt.create_tracker("rk4", f, bc, row_sink=sink, **opts).track_particles(g["x0"][:64], (0.0, 0.3), 31,
+                                                                                   dt=0.01)
+    plain = jt.create_tracker("rk4", f, bc, **{k: v for k, v in opts.items() if k != "time_chunk"}) \
+        .track_particles(g["x0"][:64], (0.0, 0.3), 31, dt=0.01)
+    assert same(traj.positions, plain.positions)
+    starts = np.cumsum([0] + [len(p) for _, p, _, _ in got])[:-1]
+    assert [r for r, _, _, _ in got] == list(starts)
+    assert same(np.concatenate([p for _, p, _, _ in got]), traj.positions)
+    assert same(np.concatenate([t for _, _, _, t in got]), traj.times)
+    if traj.velocities is not None:
+        assert same(np.concatenate([v for _, _, v, _ in got]), traj.velocities)
+
+
+def test_vtk_series_sink_writes_the_trajectory(golden, tmp_path):
+    import xml.etree.ElementTree as ET
+    from jaxtrace_gb300 import vtk_io
+    g = golden("track_grid")
+    f = jt.StructuredTimeSeriesField(g["D"], g["st"], g["g"], g["g"], g["g"], "periodic")
+    bc = jt.periodic_boundary(((0, 0, 0), (1, 1, 1)))
+    series = vtk_io.VTKTrajectorySeries(tmp_path, compress=True)
+    traj = jt.create_tracker("rk4", f, bc, row_sink=series, time_chunk=10, record_every=2) \
+        .track_particles(g["x0"], (0.0, 0.3), 31, dt=0.01)
+    pvd = series.close()
+    sets = ET.parse(pvd).getroot().findall("Collection/DataSet")
+    assert len(sets) == traj.T
+    for r, ds in enumerate(sets):
+        d = vtk_io.read_vtk_xml(str(tmp_path / ds.get("file")))
+        assert same(d["points"], traj.positions[r])
+        assert np.all(d["point_data"]["Time"] == traj.times[r])
+        assert float(ds.get("timestep")) == pytest.approx(float(traj.times[r]), abs=1e-6)
+
+
 def _octree_field(g):
     return jt.OctreeFEMTimeSeriesFieldOptimized(g["D"], g["st"], g["P"], g["T4"], max_elements_per_leaf=32,
                                                 max_depth=12)

@@ -72,3 +72,77 @@ def test_time_series_order_field_detection_and_tetrahedra(tmp_path):
 def test_missing_files_raise(tmp_path):
     with pytest.raises(ValueError, match="No VTK files"):
         V.VTKUnstructuredTimeSeriesReader(str(tmp_path / "*.vtu"))
+
+
+def test_trajectory_export_matches_the_reference_layout(tmp_path):
+    """export_to_vtk writes the reference's arrays (particles.py:448-539),
+    restated here as its per-point loop."""
+    import jaxtrace_gb300 as jt
+    rng = np.random.default_rng(6)
+    T, N = 5, 7
+    pos = rng.random((T, N, 3)).astype(F32)
+    times = np.array([0.0, 0.1, 0.25, 0.3, 0.7], dtype=F32)
+    tr = jt.Trajectory(positions=pos, times=times)
+    f = tmp_path / "traj.vtu"
+    tr.export_to_vtk(str(f), time_indices=[0, 2, 4])
+    d = V.read_vtk_xml(str(f))
+    vel, tm, pid = [], [], []
+    for t in (0, 2, 4):
+        for p in range(N):
+            if t > 0:
+                dt = times[t] - times[t - 1]
+                vel.append((pos[t, p] - pos[t - 1, p]) / dt)
+            else:
+                vel.append(np.zeros(3, F32))
+            tm.append(times[t])
+            pid.append(p)
+    vel = np.array(vel, dtype=F32)
+    assert np.array_equal(d["points"], pos[[0, 2, 4]].reshape(-1, 3))
+    assert np.array_equal(d["point_data"]["Velocity"], vel)
+    assert np.array_equal(d["point_data"]["Time"], np.array(tm, F32))
+    assert np.array_equal(d["point_data"]["ParticleID"], np.array(pid, np.int32))
+    assert np.array_equal(d["point_data"]["Speed"], np.linalg.norm(vel, axis=1).astype(F32))
+    assert np.all(d["cells"]["types"] == V.VTK_VERTEX) and len(d["cells"]["types"]) == 3 * N
+
+
+def test_trajectory_writer_points_and_lines(tmp_path):
+    """VTKTrajectoryWriter's .vtp files hold the reference's arrays
+    (io/vtk_writer.py:84-300), restated here as its loops."""
+    rng = np.random.default_rng(8)
+    T, N = 40, 9            # T > 8 rows: the path-length sums are pairwise
+    pos = rng.random((T, N, 3)).astype(F32)
+    times = np.linspace(0.0, 1.0, T).astype(F32)
+    w = V.VTKTrajectoryWriter(tmp_path / "out")
+    speed = rng.random((T, N)).astype(F32)
+    tag = rng.random(N).astype(F32)
+    with pytest.warns(UserWarning, match="bad"):
+        f = w.write_trajectory_points(pos, times, particle_data={"speed": speed, "tag": tag,
+                                                                 "bad": np.zeros(3)}, time_subset=slice(2, 30, 3))
+    d = V.read_vtk_xml(f)
+    rows = np.arange(T)[2:30:3]
+    assert np.array_equal(d["points"], pos[rows].reshape(-1, 3))
+    pd = d["point_data"]
+    assert np.array_equal(pd["Time"], np.repeat(times[rows], N))
+    assert np.array_equal(pd["ParticleID"], np.tile(np.arange(N, dtype=F32), len(rows)))
+    assert np.array_equal(pd["TimeStep"], np.repeat(np.arange(len(rows), dtype=F32), N))
+    assert np.array_equal(pd["speed"], speed[rows].ravel()) and np.array_equal(pd["tag"], np.tile(tag, len(rows)))
+    assert "bad" not in pd
+    v = d["cells"]["verts"]
+    assert np.array_equal(v["connectivity"], np.arange(len(rows) * N))
+    assert np.array_equal(v["offsets"], np.arange(1, len(rows) * N + 1))
+
+    f = w.write_trajectory_lines(pos, times, max_particles=4)
+    d = V.read_vtk_xml(f)
+    idx = np.linspace(0, N - 1, 4, dtype=int)
+    sel = pos[:, idx, :]
+    ref_len = np.zeros(4, dtype=F32)
+    conn = []
+    for i in range(4):
+        ref_len[i] = np.sum(np.linalg.norm(np.diff(sel[:, i, :], axis=0), axis=1))
+        conn += [t * 4 + i for t in range(T)]
+    assert np.array_equal(d["points"], sel.reshape(-1, 3))
+    assert np.array_equal(d["cells"]["lines"]["connectivity"], np.array(conn))
+    assert np.array_equal(d["cells"]["lines"]["offsets"], T * np.arange(1, 5))
+    assert np.array_equal(d["cell_data"]["PathLength"], ref_len)
+    assert np.array_equal(d["point_data"]["ParticleID"], np.tile(idx.astype(F32), T))
+    assert np.array_equal(d["point_data"]["Time"], np.repeat(times, 4))
