@@ -604,6 +604,43 @@ def analytics_part(a, case, g, bc, x0_dev, times, plain_ms, storage):
             "pair_term_pairs_per_s": 100_000 * 99_999 / (pair_ms / 1e3)}
 
 
+def recording_part(case, bc, storage, every=100, chunk=100):
+    """Recorded trajectories through track_particles (pinned host x0 in, the
+    Trajectory out) on a quarter of the headline particles, every
+    ``every``-th step recorded: the final-only pass, one recorded slab copied
+    after the pass, ``chunk``-step slabs copied on a side stream while the
+    next chunk runs, and the same with a row sink receiving each slab."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    g = case["grid"][0]
+    field = jt.StructuredTimeSeriesField(case["data"], case["times"], g, g, g, "clamp", storage=storage)
+    x0 = torch.from_numpy(np.ascontiguousarray(case["x0"][: len(case["x0"]) // 4])).pin_memory()
+    handed = []
+
+    def run(**kw):
+        tr = jt.create_tracker("rk4", field, bc, **kw)
+        tr.track_particles(x0, case["time_span"], case["n_timesteps"], dt=case["dt"])
+        torch.cuda.synchronize()
+        handed.clear()
+        t = time.perf_counter()
+        traj = tr.track_particles(x0, case["time_span"], case["n_timesteps"], dt=case["dt"])
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) * 1e3, traj
+
+    out = {"particles": int(x0.shape[0]), "record_every": every, "time_chunk": chunk}
+    out["final_only_ms"], _ = run(record_final_only=True)
+    out["one_slab_ms"], t1 = run(record_every=every)
+    out["chunked_ms"], t2 = run(record_every=every, time_chunk=chunk)
+    out["chunked_sink_ms"], t3 = run(record_every=every, time_chunk=chunk,
+                                     row_sink=lambda r0, p, v, t: handed.append(len(p)))
+    out["rows"] = int(t1.T)
+    out["recorded_bytes"] = int(t1.positions.nbytes)
+    out["rows_handed_to_sink"] = int(sum(handed))
+    out["same_bits"] = bool(np.array_equal(t1.positions, t2.positions) and np.array_equal(t1.positions, t3.positions))
+    return out
+
+
 def workload_name(a):
     return (f"precision: {a.grid}^3 clamp grid, 64 snapshots ABC+(1,0,0)+N(0,0.01^2) over [0,2], "
             f"{a.seeds ** 3} lattice seeds, continuous inlet x (lattice {a.seeds}x{a.seeds}), "
@@ -777,6 +814,7 @@ def main():
     line["clocks"] = clk.summary()
     if not a.profile and rank == 0:
         line["analytics"] = analytics_part(a, case, g, bc, x0_dev, times, results[head]["ms_per_step"], head)
+        line["recording"] = recording_part(case, bc, head)
     iss = line.get("roofline", {}).get("issue")
     if iss is not None:
         mhz = line["clocks"].get("sm_mhz") or 2070.0
