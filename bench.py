@@ -426,7 +426,8 @@ def fem_leg(a, profile=False):
     same = np.all(final[sub].view(np.uint32) == o32.view(np.uint32), axis=1)
     rel = np.linalg.norm(final[sub] - o64, axis=1) / np.maximum(np.linalg.norm(o64, axis=1), 1e-30)
     hash_grid = {} if profile else fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc)
-    return {"workload": "unstructured FEM: 64^3 hexes x 6 jittered tets (1,572,864), 32 FP32 snapshots, octree + "
+    return {"octree_build": octree_build_times(c),
+            "workload": "unstructured FEM: 64^3 hexes x 6 jittered tets (1,572,864), 32 FP32 snapshots, octree + "
                         f"P1, 1,000,000 particles, x/z periodic y reflective, RK4 dt=0.005, {n_steps} steps",
             "hash_grid_variant": hash_grid,
             "value": n * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "status": int(status.item()),
@@ -441,6 +442,28 @@ def fem_leg(a, profile=False):
             "cpu_baseline": {"value": len(sub) * n_steps / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1,
                              "kind": "port", "sample": f"{len(sub)} particles (every 1000th) x {n_steps} steps, "
                                                        "float32 C restatement of the octree/P1 path, OpenMP"}}
+
+
+def octree_build_times(c):
+    """Octree build of the FEM mesh from host arrays: the host builder and the
+    device builder (host->device copy of points and connectivity included),
+    and whether their arrays agree bit for bit."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    t = time.perf_counter()
+    h = jt.OctreeMesh(c["points"], c["tets"], build="host")
+    host_s = time.perf_counter() - t
+    jt.OctreeMesh(c["points"], c["tets"], build="device")
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    d = jt.OctreeMesh(c["points"], c["tets"], build="device")
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t
+    same = bool(np.array_equal(d.nodes.view(np.int32), h.nodes.view(np.int32)) and
+                np.array_equal(d.elems, h.elems) and np.array_equal(d.tet_geom, h.tet_geom))
+    return {"host_ms": host_s * 1e3, "device_ms": dev_s * 1e3, "nodes": int(h.info.n_nodes),
+            "leaves": int(h.info.n_leaves), "depth": int(h.info.max_tree_depth), "same_arrays": same}
 
 
 def fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc):

@@ -533,6 +533,25 @@ int jt_octree_fetch(void* handle, jt_octree_node* nodes, int32_t* elems, float* 
 
 void jt_octree_free(void* handle);
 
+/* The same octree built on the device (identical arrays to jt_octree_build):
+ * points device (n_points,3) float32, conn device (n_tets,4) int32; elems
+ * (n_tets int32, every element lands in exactly one leaf) and, if not NULL,
+ * tet_box (n_tets,8) and tet_geom (n_tets,16) are caller device buffers
+ * filled on `stream`.  Node records and node bounds, whose count is known
+ * only after the build (info->n_nodes), stay in *handle_out (device memory)
+ * until jt_octree_fetch_device copies them and jt_octree_free_device
+ * releases them.  Returns after the build has finished on `stream`. */
+int jt_octree_build_device(const float* points, int32_t n_points, const int32_t* conn, int32_t n_tets,
+                           int32_t max_elements_per_leaf, int32_t max_depth, int32_t* elems,
+                           float* tet_box, float* tet_geom, void* stream, void** handle_out,
+                           jt_octree_info* info);
+
+/* Copy the device build's nodes (n_nodes) and node_bounds (n_nodes,6) into
+ * caller buffers (device or host; either may be NULL), ordered on `stream`. */
+int jt_octree_fetch_device(void* handle, jt_octree_node* nodes, float* node_bounds, void* stream);
+
+void jt_octree_free_device(void* handle, void* stream);
+
 /* ---- FEM hash grid build (host) ----------------------------------------- */
 typedef struct {
     int64_t n_cells;        /* grid_size[0]*grid_size[1]*grid_size[2]         */

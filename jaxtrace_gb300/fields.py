@@ -634,16 +634,35 @@ class FEMTimeSeriesField(TimeSeriesField):
 
 
 class OctreeMesh:
-    """Host copy of the octree in the reference's array layout
-    (OctreeMeshOptimized, octree_fem_interpolator_optimized.py:18-38)."""
+    """The octree in the reference's array layout (OctreeMeshOptimized,
+    octree_fem_interpolator_optimized.py:18-38).
 
-    def __init__(self, points, connectivity, max_elements_per_leaf=32, max_depth=12):
+    ``build``: "host" (jt_octree_build), "device" (jt_octree_build_device:
+    the same arrays, built on the GPU and kept there in ``dev``; the host
+    arrays are copied down on first use) or "auto" (device when CUDA is
+    visible)."""
+
+    _HOST = ("nodes", "elems", "tet_box", "tet_geom", "nodes_min", "nodes_max", "nodes_children", "nodes_is_leaf",
+             "nodes_elem_counts", "node_depth")
+
+    def __init__(self, points, connectivity, max_elements_per_leaf=32, max_depth=12, build: str = "auto"):
         points = np.ascontiguousarray(_as_f32(points))
         conn = np.ascontiguousarray(np.asarray(connectivity, dtype=np.int32))
         if points.ndim != 2 or points.shape[1] != 3:
             raise ValueError(f"points must be (N,3), got {points.shape}")
         if conn.ndim != 2 or conn.shape[1] != 4:
             raise ValueError(f"connectivity must be (M,4), got {conn.shape}")
+        if build not in ("auto", "host", "device"):
+            raise ValueError(f"build must be 'auto', 'host' or 'device', got {build!r}")
+        self.dev = None
+        if build == "auto":
+            import torch
+            build = "device" if torch.cuda.is_available() else "host"
+        self.points, self.connectivity = points, conn
+        self.max_elements_per_leaf, self.max_depth = int(max_elements_per_leaf), int(max_depth)
+        if build == "device":
+            self._build_device()
+            return
         lib = L.load()
         handle = C.c_void_p()
         info = L.OctreeInfo()
@@ -661,13 +680,50 @@ class OctreeMesh:
         finally:
             lib.jt_octree_free(handle)
         self.info = info
-        self.points, self.connectivity = points, conn
-        self.max_elements_per_leaf, self.max_depth = int(max_elements_per_leaf), int(max_depth)
+        self._host_views(bounds)
+
+    def _host_views(self, bounds):
         self.nodes_min, self.nodes_max = bounds[:, :3].copy(), bounds[:, 3:].copy()
         self.nodes_children = self.nodes["children"].copy()
         self.nodes_is_leaf = self.nodes["is_leaf"].astype(bool)
         self.nodes_elem_counts = self.nodes["elem_count"].copy()
         self.node_depth = self.nodes["pad"][:, 0].copy()
+
+    def _build_device(self):
+        torch = _torch_cuda()
+        lib = L.load()
+        M = self.connectivity.shape[0]
+        pts = torch.from_numpy(self.points).cuda()
+        conn = torch.from_numpy(self.connectivity).cuda()
+        d = {"elems": torch.empty(max(M, 1), dtype=torch.int32, device="cuda"),
+             "tet_box": torch.empty((M, 8), dtype=torch.float32, device="cuda"),
+             "tet_geom": torch.empty((M, 16), dtype=torch.float32, device="cuda")}
+        handle = C.c_void_p()
+        info = L.OctreeInfo()
+        stream = L.stream_ptr()
+        L.check(lib.jt_octree_build_device(pts.data_ptr(), self.points.shape[0], conn.data_ptr(), M,
+                                           self.max_elements_per_leaf, self.max_depth, d["elems"].data_ptr(),
+                                           d["tet_box"].data_ptr(), d["tet_geom"].data_ptr(), stream,
+                                           C.byref(handle), C.byref(info)))
+        try:
+            d["nodes"] = torch.empty((info.n_nodes, 16), dtype=torch.int32, device="cuda")
+            d["bounds"] = torch.empty((info.n_nodes, 6), dtype=torch.float32, device="cuda")
+            L.check(lib.jt_octree_fetch_device(handle, d["nodes"].data_ptr(), d["bounds"].data_ptr(), stream))
+        finally:
+            lib.jt_octree_free_device(handle, stream)
+        self.info, self.dev = info, d
+
+    def __getattr__(self, name):
+        # host arrays of a device build, copied down on first use
+        if name in OctreeMesh._HOST and self.__dict__.get("dev") is not None:
+            d = self.dev
+            self.nodes = np.ascontiguousarray(d["nodes"].cpu().numpy()).view(L.OCTREE_NODE_DTYPE).reshape(-1)
+            self.elems = d["elems"].cpu().numpy()
+            self.tet_box = d["tet_box"].cpu().numpy()
+            self.tet_geom = d["tet_geom"].cpu().numpy()
+            self._host_views(d["bounds"].cpu().numpy())
+            return self.__dict__[name]
+        raise AttributeError(name)
 
     @property
     def nodes_elements(self) -> np.ndarray:
@@ -691,7 +747,8 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
 
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
-                 max_elements_per_leaf: int = 32, max_depth: int = 12, *, storage: str = "f32"):
+                 max_elements_per_leaf: int = 32, max_depth: int = 12, *, storage: str = "f32",
+                 octree_build: str = "auto"):
         data = _as_f32(data)
         positions = ensure_positions_shape(positions)
         if data.ndim != 3 or data.shape[2] != 3:
@@ -705,7 +762,7 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         self.data, self.positions = data, positions
         self.T, self.N = T, N
         self._source_info = _source_info or {}
-        self.octree_mesh = OctreeMesh(positions, connectivity, max_elements_per_leaf, max_depth)
+        self.octree_mesh = OctreeMesh(positions, connectivity, max_elements_per_leaf, max_depth, octree_build)
 
     def _device(self):
         if self._dev is not None:
@@ -716,14 +773,17 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         self._scales = scales
         pts = np.zeros((self.N, 4), dtype=F32)
         pts[:, :3] = self.positions
-        d = {"pairs": pairs, "points": torch.from_numpy(pts).cuda(),
-             "tet_box": torch.from_numpy(m.tet_box).cuda(), "tet_geom": torch.from_numpy(m.tet_geom).cuda(),
-             "nodes": torch.from_numpy(m.nodes.view(np.int32).reshape(len(m.nodes), 16)).cuda(),
-             "elems": torch.from_numpy(m.elems).cuda()}
+        d = {"pairs": pairs, "points": torch.from_numpy(pts).cuda()}
+        if m.dev is not None:       # built on the device: no upload
+            d.update({k: m.dev[k] for k in ("tet_box", "tet_geom", "nodes", "elems")})
+        else:
+            d.update({"tet_box": torch.from_numpy(m.tet_box).cuda(), "tet_geom": torch.from_numpy(m.tet_geom).cuda(),
+                      "nodes": torch.from_numpy(m.nodes.view(np.int32).reshape(len(m.nodes), 16)).cuda(),
+                      "elems": torch.from_numpy(m.elems).cuda()})
         self._dev = d
         f = L.MeshField()
         f.n_points, f.n_tets = self.N, m.connectivity.shape[0]
-        f.n_nodes, f.max_depth = len(m.nodes), m.max_depth
+        f.n_nodes, f.max_depth = int(m.info.n_nodes), m.max_depth
         f.storage, f.n_pairs, f.pair_stride = self._storage, pairs.shape[0], self.N
         f.points, f.tet_box, f.tet_geom = d["points"].data_ptr(), d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
         f.nodes, f.elems, f.pairs = d["nodes"].data_ptr(), d["elems"].data_ptr(), pairs.data_ptr()

@@ -48,7 +48,7 @@ def test_errors_are_mapped():
 
 def test_octree_build_matches_reference(golden):
     g = golden("octree")
-    m = jt.OctreeMesh(g["P"], g["T4"], 32, 12)
+    m = jt.OctreeMesh(g["P"], g["T4"], 32, 12, build="host")
     assert len(m.nodes) == g["nodes_min"].shape[0]
     assert np.array_equal(m.nodes_min, g["nodes_min"])
     assert np.array_equal(m.nodes_max, g["nodes_max"])
@@ -63,13 +63,13 @@ def test_octree_build_matches_reference(golden):
 
 def test_octree_build_known_answer_mesh(golden):
     g = golden("octree")
-    m = jt.OctreeMesh(g["ka_pts"], g["ka_conn"], 1, 5)
+    m = jt.OctreeMesh(g["ka_pts"], g["ka_conn"], 1, 5, build="host")
     assert m.info.n_leaves >= 2
 
 
 def test_octree_rejects_bad_connectivity():
     with pytest.raises(ValueError, match="outside"):
-        jt.OctreeMesh(np.zeros((4, 3), F32), np.array([[0, 1, 2, 9]], np.int32))
+        jt.OctreeMesh(np.zeros((4, 3), F32), np.array([[0, 1, 2, 9]], np.int32), build="host")
 
 
 @pytest.mark.parametrize("ex", ["constant", "linear", "zero", "nan"])
