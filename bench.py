@@ -466,6 +466,28 @@ def octree_build_times(c):
             "leaves": int(h.info.n_leaves), "depth": int(h.info.max_tree_depth), "same_arrays": same}
 
 
+def fem_grid_build_times(c):
+    """Hash grid (32^3 cells, 4^3 sub-cells each) of the FEM mesh from host
+    arrays: the host builder with its NumPy element records, and the device
+    builder (host->device copy of points and connectivity included)."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    t = time.perf_counter()
+    h = jt.FemHashGrid(c["points"], c["tets"], build="host")
+    host_s = time.perf_counter() - t
+    jt.FemHashGrid(c["points"], c["tets"], build="device")
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    d = jt.FemHashGrid(c["points"], c["tets"], build="device")
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t
+    same = bool(all(np.array_equal(getattr(d, k), getattr(h, k))
+                    for k in ("cell_start", "cell_elems", "sub_start", "sub_elems", "tet_geom")))
+    return {"host_ms": host_s * 1e3, "device_ms": dev_s * 1e3, "cell_entries": int(len(h.cell_elems)),
+            "sub_cell_entries": int(len(h.sub_elems)), "same_arrays": same}
+
+
 def fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc):
     """The same run through the hash-grid FEM field (FEMTimeSeriesField,
     32^3 cells, global nearest-node fallback)."""
@@ -493,6 +515,7 @@ def fem_hash_grid_variant(c, bc, times, x0, n_steps, sub, obc):
     o32, _, info = oracle.track(spec, obc, c["x0"][sub], times, c["dt"])
     same = np.all(final[sub].view(np.uint32) == o32.view(np.uint32), axis=1)
     return {"value": n * n_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "status": int(status.item()),
+            "grid_build": fem_grid_build_times(c),
             "hash_grid": list(h.grid_size), "max_elements_per_cell": h.max_elems_per_cell,
             "parity_f32_oracle": {"bit_exact_fraction": float(np.mean(same)), "particles": len(sub),
                                   "oracle_fallbacks": info["fallback_count"]}}

@@ -583,6 +583,28 @@ int jt_fem_grid_fetch(void* handle, int32_t* cell_start, int32_t* cell_elems, in
 
 void jt_fem_grid_free(void* handle);
 
+/* The same lists built on the device (identical arrays to jt_fem_grid_build):
+ * points device (n_points,3), conn device (n_tets,4); grid_size, grid_min,
+ * cell_edge and eps are host arrays of 3.  tet_box (n_tets,8, required) and
+ * tet_geom (n_tets,16, or NULL) are caller device buffers filled with the
+ * box (min xyz,0,max xyz,0) and geometry (v0, v1-v0, v2-v0, v3-v0, vertex
+ * ids) records.  The lists stay in *handle_out (device memory) until
+ * jt_fem_grid_fetch_device copies them and jt_fem_grid_free_device releases
+ * them.  JT_ERR_UNSUPPORTED when the grid has more than 4,194,303 cells or
+ * sub-cells or a cell lists more than 4096 elements (the host builder covers
+ * those).  Returns after the build has finished on `stream`. */
+int jt_fem_grid_build_device(const float* points, int32_t n_points, const int32_t* conn, int32_t n_tets,
+                             const int32_t* grid_size, const float* grid_min, const double* cell_edge,
+                             int32_t sub_div, const double* eps, float* tet_box, float* tet_geom,
+                             void* stream, void** handle_out, jt_fem_grid_info* info);
+
+/* Copy the device build's lists into caller buffers (device or host; any may
+ * be NULL), ordered on `stream`. */
+int jt_fem_grid_fetch_device(void* handle, int32_t* cell_start, int32_t* cell_elems, int32_t* sub_start,
+                             int32_t* sub_elems, void* stream);
+
+void jt_fem_grid_free_device(void* handle, void* stream);
+
 /* ---- trajectory analytics ------------------------------------------------- */
 /* The pair term of compute_mixing_metrics (tracking/analysis.py:297-312):
  * over every ordered pair (i, j) whose float32 initial distance

@@ -179,6 +179,9 @@ def load(build_if_missing: bool = True):
         "jt_fem_grid_build": (i32, [vp, i32, vp, i32, vp, vp, vp, i32, vp, P(vp), P(FemGridInfo)]),
         "jt_fem_grid_fetch": (i32, [vp, vp, vp, vp, vp]),
         "jt_fem_grid_free": (None, [vp]),
+        "jt_fem_grid_build_device": (i32, [vp, i32, vp, i32, vp, vp, vp, i32, vp, vp, vp, vp, P(vp), P(FemGridInfo)]),
+        "jt_fem_grid_fetch_device": (i32, [vp, vp, vp, vp, vp, vp]),
+        "jt_fem_grid_free_device": (None, [vp, vp]),
         "jt_octree_free": (None, [vp]),
         "jt_cell_sort_workspace_bytes": (C.c_size_t, [i32, i32]),
         "jt_cell_sort": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp]),

@@ -16,6 +16,12 @@ int cuda_status(cudaError_t e, const char* what);
 // and fewer than 2^31 nodes (32-bit node offsets within a snapshot).
 int check_grid_shape(const jt_grid_field& g);
 
+// Exclusive scan of n uint32 values in place (n <= scan_capacity()); sums
+// holds scan_partials(n) values, sums2 one.
+int64_t scan_capacity();
+int64_t scan_partials(int64_t n);
+int exclusive_scan_u32(uint32_t* data, int64_t n, uint32_t* sums, uint32_t* sums2, cudaStream_t st);
+
 struct StageBlends;
 struct StepConst;
 

@@ -506,7 +506,16 @@ class FemHashGrid:
     the reference's -1-padded table.
     """
 
-    def __init__(self, points, connectivity, grid_resolution: int = 32, sub_div: int = 4):
+    _HOST = ("cell_start", "cell_elems", "sub_start", "sub_elems", "cell_elem_counts", "tet_box", "tet_geom",
+             "element_bounds")
+
+    def __init__(self, points, connectivity, grid_resolution: int = 32, sub_div: int = 4, build: str = "auto"):
+        """``build``: "host" (jt_fem_grid_build and NumPy element records),
+        "device" (jt_fem_grid_build_device: the same arrays, kept on the GPU
+        in ``dev``, host copies made on first use) or "auto" (device when
+        CUDA is visible and the grid is within the device build's limits)."""
+        if build not in ("auto", "host", "device"):
+            raise ValueError(f"build must be 'auto', 'host' or 'device', got {build!r}")
         P = np.asarray(points, dtype=F32)
         T4 = np.asarray(connectivity, dtype=np.int32)
         if P.ndim != 2 or P.shape[1] != 3:
@@ -526,6 +535,18 @@ class FemHashGrid:
         self.grid_min = bmin.astype(F32)
         self.cell_size64 = cell64
         self.grid_cell_size = cell64.astype(F32)
+        self.dev = None
+        use_device = build == "device"
+        if build == "auto":
+            import torch
+            use_device = torch.cuda.is_available() and len(T4) > 0
+        if use_device:
+            try:
+                self._build_device(int(sub_div), bmin, cell64)
+                return
+            except NotImplementedError:
+                if build == "device":
+                    raise          # auto: beyond the device build's limits, build on the host
         V = P[T4]                                           # (M,4,3)
         emin, emax = V.min(axis=1), V.max(axis=1)
         self.element_bounds = np.stack([emin, emax], axis=1)
@@ -542,6 +563,66 @@ class FemHashGrid:
         self.tet_geom[:, 9:12] = V[:, 3] - v0
         self.tet_geom[:, 12:16] = T4.view(F32)
 
+    def _eps(self, S, cell64):
+        """Per-axis margin of the sub-cell lists: covers the float32 rounding
+        of the device's sub-cell index."""
+        sub = cell64 / max(S, 1)
+        scale = float(np.abs(self.points).max()) if len(self.points) else 1.0
+        return np.ascontiguousarray(1e-3 * sub + 4e-7 * max(scale, 1.0), dtype=np.float64)
+
+    def _build_device(self, S, bmin, cell64):
+        torch = _torch_cuda()
+        lib = L.load()
+        M = len(self.connectivity)
+        eps = self._eps(S, cell64)
+        gs = np.ascontiguousarray(self.grid_size, dtype=np.int32)
+        gmin = np.ascontiguousarray(bmin, dtype=F32)
+        edge = np.ascontiguousarray(cell64, dtype=np.float64)
+        pts = torch.from_numpy(np.ascontiguousarray(self.points)).cuda()
+        conn = torch.from_numpy(np.ascontiguousarray(self.connectivity)).cuda()
+        d = {"tet_box": torch.empty((M, 8), dtype=torch.float32, device="cuda"),
+             "tet_geom": torch.empty((M, 16), dtype=torch.float32, device="cuda")}
+        handle = C.c_void_p()
+        info = L.FemGridInfo()
+        stream = L.stream_ptr()
+        L.check(lib.jt_fem_grid_build_device(pts.data_ptr(), len(self.points), conn.data_ptr(), M, gs.ctypes.data,
+                                             gmin.ctypes.data, edge.ctypes.data, max(int(S), 0), eps.ctypes.data,
+                                             d["tet_box"].data_ptr(), d["tet_geom"].data_ptr(), stream,
+                                             C.byref(handle), C.byref(info)))
+        try:
+            i32 = dict(dtype=torch.int32, device="cuda")
+            d["cell_start"] = torch.empty(info.n_cells + 1, **i32)
+            d["cell_elems"] = torch.zeros(max(info.n_entries, 1), **i32)
+            d["sub_start"] = torch.zeros(max(info.n_sub_cells + 1, 1), **i32)
+            d["sub_elems"] = torch.zeros(max(info.n_sub_entries, 1), **i32)
+            L.check(lib.jt_fem_grid_fetch_device(handle, d["cell_start"].data_ptr(), d["cell_elems"].data_ptr(),
+                                                 d["sub_start"].data_ptr(), d["sub_elems"].data_ptr(), stream))
+        finally:
+            lib.jt_fem_grid_free_device(handle, stream)
+        self.dev = d
+        self._n_entries, self._n_sub_entries = int(info.n_entries), int(info.n_sub_entries)
+        self.max_elems_per_cell = int(info.max_per_cell)
+        self.sub_div = int(S) if (S > 0 and info.n_sub_cells > 0) else 0
+
+    def __getattr__(self, name):
+        # host arrays of a device build, copied down on first use
+        if name in FemHashGrid._HOST and self.__dict__.get("dev") is not None:
+            d = self.dev
+            self.cell_start = d["cell_start"].cpu().numpy()
+            self.cell_elems = d["cell_elems"][:self._n_entries].cpu().numpy()
+            if self.sub_div:
+                self.sub_start = d["sub_start"].cpu().numpy()
+                self.sub_elems = d["sub_elems"][:self._n_sub_entries].cpu().numpy()
+            else:
+                self.sub_start = np.zeros(1, np.int32)
+                self.sub_elems = np.zeros(1, np.int32)
+            self.cell_elem_counts = np.diff(self.cell_start).astype(np.int32)
+            self.tet_box = d["tet_box"].cpu().numpy()
+            self.tet_geom = d["tet_geom"].cpu().numpy()
+            self.element_bounds = np.stack([self.tet_box[:, 0:3], self.tet_box[:, 4:7]], axis=1)
+            return self.__dict__[name]
+        raise AttributeError(name)
+
     def _build_lists(self, S, bmin, cell64):
         """Cell lists and sub-cell lists (S^3 per hash cell) through the
         library's host builder (jt_fem_grid_build): the reference's float64
@@ -549,9 +630,7 @@ class FemHashGrid:
         take each (element, cell) entry where its box, widened by a margin
         that covers the float32 rounding of the device's sub-cell index,
         meets them."""
-        sub = cell64 / max(S, 1)
-        scale = float(np.abs(self.points).max()) if len(self.points) else 1.0
-        eps = np.ascontiguousarray(1e-3 * sub + 4e-7 * max(scale, 1.0), dtype=np.float64)
+        eps = self._eps(S, cell64)
         gs = np.ascontiguousarray(self.grid_size, dtype=np.int32)
         gmin = np.ascontiguousarray(bmin, dtype=F32)
         edge = np.ascontiguousarray(cell64, dtype=np.float64)
@@ -596,10 +675,12 @@ class FEMTimeSeriesField(TimeSeriesField):
 
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
-                 fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: int = 4):
+                 fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: int = 4,
+                 grid_build: str = "auto"):
         super().__init__(data, times, positions, interpolation, extrapolation, _source_info, storage=storage,
                          time_semantics="jax")
-        self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution, sub_div=sub_div)
+        self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution, sub_div=sub_div,
+                                    build=grid_build)
 
     def _device(self):
         if self._dev is not None:
@@ -608,12 +689,16 @@ class FEMTimeSeriesField(TimeSeriesField):
         super()._device()
         h = self.fem_mesh
         d = self._dev
-        d["tet_box"] = torch.from_numpy(h.tet_box).cuda()
-        d["tet_geom"] = torch.from_numpy(h.tet_geom).cuda()
-        d["cell_start"] = torch.from_numpy(h.cell_start).cuda()
-        d["cell_elems"] = torch.from_numpy(h.cell_elems if len(h.cell_elems) else np.zeros(1, np.int32)).cuda()
-        d["sub_start"] = torch.from_numpy(h.sub_start).cuda()
-        d["sub_elems"] = torch.from_numpy(h.sub_elems if len(h.sub_elems) else np.zeros(1, np.int32)).cuda()
+        if h.dev is not None:       # built on the device: no upload
+            d.update({k: h.dev[k] for k in ("tet_box", "tet_geom", "cell_start", "cell_elems", "sub_start",
+                                            "sub_elems")})
+        else:
+            d["tet_box"] = torch.from_numpy(h.tet_box).cuda()
+            d["tet_geom"] = torch.from_numpy(h.tet_geom).cuda()
+            d["cell_start"] = torch.from_numpy(h.cell_start).cuda()
+            d["cell_elems"] = torch.from_numpy(h.cell_elems if len(h.cell_elems) else np.zeros(1, np.int32)).cuda()
+            d["sub_start"] = torch.from_numpy(h.sub_start).cuda()
+            d["sub_elems"] = torch.from_numpy(h.sub_elems if len(h.sub_elems) else np.zeros(1, np.int32)).cuda()
         f = L.FemField()
         f.nearest = self._cnear
         f.n_tets = len(h.connectivity)

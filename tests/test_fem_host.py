@@ -11,7 +11,7 @@ F32 = np.float32
 
 def test_hash_grid_matches_reference_build(golden):
     g = golden("fem")
-    h = jt.FemHashGrid(g["P"], g["T4"], grid_resolution=8)
+    h = jt.FemHashGrid(g["P"], g["T4"], grid_resolution=8, build="host")
     assert h.grid_size == tuple(int(v) for v in g["grid_size"])
     assert np.array_equal(h.grid_min.view(np.uint32), g["grid_min"].view(np.uint32))
     assert np.array_equal(h.grid_cell_size.view(np.uint32), g["grid_cell_size"].view(np.uint32))
@@ -22,7 +22,7 @@ def test_hash_grid_matches_reference_build(golden):
 
 def test_hash_grid_known_answer_mesh(golden):
     g = golden("fem")
-    h = jt.FemHashGrid(g["ka_pts"], g["ka_conn"], grid_resolution=4)
+    h = jt.FemHashGrid(g["ka_pts"], g["ka_conn"], grid_resolution=4, build="host")
     assert h.grid_size == (4, 4, 4)
     # the oracle on our build reproduces the module's printed example
     D = np.stack([g["ka_pts"], g["ka_pts"]])
@@ -36,7 +36,7 @@ def test_hash_grid_anisotropic_and_degenerate_inputs():
     rng = np.random.default_rng(0)
     P = (rng.random((50, 3)) * np.array([4.0, 1.0, 0.25])).astype(F32)
     T4 = rng.integers(0, 50, (40, 4)).astype(np.int32)
-    h = jt.FemHashGrid(P, T4, grid_resolution=16)
+    h = jt.FemHashGrid(P, T4, grid_resolution=16, build="host")
     assert h.grid_size[0] > h.grid_size[1] > h.grid_size[2] >= 1
     # every element is listed in the cell holding its box's lower corner
     for e in range(len(T4)):
@@ -45,9 +45,9 @@ def test_hash_grid_anisotropic_and_degenerate_inputs():
         cid = (c[0] * h.grid_size[1] + c[1]) * h.grid_size[2] + c[2]
         assert e in h.cell_elems[h.cell_start[cid]:h.cell_start[cid + 1]]
     with pytest.raises(ValueError):
-        jt.FemHashGrid(P, np.array([[0, 1, 2, 99]], np.int32))
+        jt.FemHashGrid(P, np.array([[0, 1, 2, 99]], np.int32), build="host")
     with pytest.raises(ValueError):
-        jt.FemHashGrid(P[:, :2], T4)
+        jt.FemHashGrid(P[:, :2], T4, build="host")
 
 
 def test_sub_cell_lists_hold_every_candidate_the_cell_scan_can_pick():
@@ -57,7 +57,7 @@ def test_sub_cell_lists_hold_every_candidate_the_cell_scan_can_pick():
     containing element found is the one the reference's cell scan finds."""
     from jaxtrace_gb300 import workloads as W
     P, T4 = W.kuhn_mesh(10, 0.2, 3)
-    h = jt.FemHashGrid(P, T4, 12, sub_div=4)
+    h = jt.FemHashGrid(P, T4, 12, sub_div=4, build="host")
     S = h.sub_div
     rng = np.random.default_rng(5)
     q = np.concatenate([rng.random((4000, 3)), rng.uniform(-0.2, 1.2, (500, 3)),
@@ -125,7 +125,7 @@ def test_host_builder_lists_equal_the_array_restatement(res, sub_div):
     from jaxtrace_gb300 import workloads as W
     P, T4 = W.kuhn_mesh(9, 0.2, res)
     P = (P * np.array([1.0, 0.6, 1.7], dtype=np.float32)).astype(np.float32)   # aspect-ratio cell counts
-    h = jt.FemHashGrid(P, T4, res, sub_div=sub_div)
+    h = jt.FemHashGrid(P, T4, res, sub_div=sub_div, build="host")
     bmin = P.min(axis=0)
     ref = _numpy_lists(P, T4, h.grid_size, bmin, h.cell_size64, sub_div)
     for ours, theirs in zip((h.cell_start, h.cell_elems, h.sub_start, h.sub_elems), ref):
