@@ -163,7 +163,7 @@ typedef struct {
     int32_t n_pairs;
     int64_t pair_stride;    /* records per pair (= n_points)                  */
     const float* points;    /* device (n_points,4): x,y,z,0                   */
-    const float* tet_box;   /* device (n_tets,8): min xyz,0, max xyz,0        */
+    const float* tet_box;   /* device (n_tets,8): min xyz,flag, max xyz,0 (flag: jt_mark_near_degenerate) */
     const float* tet_geom;  /* device (n_tets,16): v0, v1-v0, v2-v0, v3-v0 (xyz each), conn as int32 bits */
     const jt_octree_node* nodes; /* device (n_nodes)                        */
     const int32_t* elems;   /* device element lists                           */
@@ -200,7 +200,7 @@ typedef struct {
     int32_t grid_size[3];   /* hash cells per axis; cell id (i*gy + j)*gz + k */
     float grid_min[3];      /* float32 node bounding-box minimum              */
     float cell_size[3];     /* float32 cell edges of the lookup               */
-    const float* tet_box;   /* device (n_tets,8): min xyz,0, max xyz,0        */
+    const float* tet_box;   /* device (n_tets,8): min xyz,flag, max xyz,0 (flag: jt_mark_near_degenerate) */
     const float* tet_geom;  /* device (n_tets,16) as jt_mesh_field            */
     const int32_t* cell_start; /* device (cells+1) CSR offsets                 */
     const int32_t* cell_elems; /* device element ids, ascending within a cell */
@@ -545,6 +545,16 @@ int jt_octree_build_device(const float* points, int32_t n_points, const int32_t*
                            int32_t max_elements_per_leaf, int32_t max_depth, int32_t* elems,
                            float* tet_box, float* tet_geom, void* stream, void** handle_out,
                            jt_octree_info* info);
+
+/* Flag near-degenerate tetrahedra for the compensated arithmetic: sets the
+ * pad slot after the box minimum (tet_box[8t+3]) to 1 where |det| of
+ * (v1-v0, v2-v0, v3-v0) is below 1e-2 |v1-v0| |v2-v0| |v3-v0| (float32, from
+ * tet_geom), else 0.  jt_track / jt_field_sample in JT_ARITH_COMPENSATED
+ * re-solve the barycentric weights of a flagged tetrahedron in float64;
+ * JT_ARITH_EXACT ignores the flag.  Device buffers; *count_out (host, may be
+ * NULL) receives the number flagged.  Returns after the pass has finished. */
+int jt_mark_near_degenerate(float* tet_box, const float* tet_geom, int32_t n_tets, int32_t* count_out,
+                            void* stream);
 
 /* Copy the device build's nodes (n_nodes) and node_bounds (n_nodes,6) into
  * caller buffers (device or host; either may be NULL), ordered on `stream`. */

@@ -175,6 +175,7 @@ def load(build_if_missing: bool = True):
         "jt_octree_build_device": (i32, [vp, i32, vp, i32, i32, i32, vp, vp, vp, vp, P(vp), P(OctreeInfo)]),
         "jt_octree_fetch_device": (i32, [vp, vp, vp, vp]),
         "jt_octree_free_device": (None, [vp, vp]),
+        "jt_mark_near_degenerate": (i32, [vp, vp, i32, P(i32), vp]),
         "jt_pair_log_ratio": (i32, [vp, vp, i32, f32, vp, vp, vp]),
         "jt_fem_grid_build": (i32, [vp, i32, vp, i32, vp, vp, vp, i32, vp, P(vp), P(FemGridInfo)]),
         "jt_fem_grid_fetch": (i32, [vp, vp, vp, vp, vp]),

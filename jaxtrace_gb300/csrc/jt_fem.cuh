@@ -69,7 +69,10 @@ struct FemField {
         for (int s = b0; s < b1; ++s) {
             float4 b;
             int4 cn;
-            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(list + s), b, cn)) continue;
+            bool near;
+            const int t = __ldg(list + s);
+            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
+            if (!EXACT && near) b = bary_f64(q, F.tet_geom, t);
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
                                      node_value(cn.w, e));
         }

@@ -26,6 +26,48 @@ __device__ __forceinline__ float det3(const V3& c0, const V3& c1, const V3& c2) 
     return A::sub(A::sub(A::sub(A::add(A::add(t1, t2), t3), t4), t5), t6);
 }
 
+// float64 determinant of three float32 columns (same expansion as det3)
+__device__ __forceinline__ double det3_f64(double a00, double a10, double a20, double a01, double a11, double a21,
+                                           double a02, double a12, double a22) {
+    return a00 * a11 * a22 + a01 * a12 * a20 + a02 * a10 * a21 - a02 * a11 * a20 - a00 * a12 * a21 -
+           a01 * a10 * a22;
+}
+
+// Near-degenerate tetrahedra: |det| below this fraction of
+// |v1-v0| |v2-v0| |v3-v0| (about 0.7 for a regular tetrahedron) loses float32
+// digits in cancellation.  jt_mark_near_degenerate flags them in the pad slot
+// after the box minimum (tet_box[8t+3] = 1); in the compensated arithmetic the
+// float32 solve still decides which tetrahedron holds the query (the
+// reference's decision) and the weights of a flagged one are solved again in
+// float64.
+constexpr float kNearDegenerate = 1e-2f;
+
+__device__ __forceinline__ bool near_degenerate(const float* g12) {
+    const V3 v01{g12[3], g12[4], g12[5]}, v02{g12[6], g12[7], g12[8]}, v03{g12[9], g12[10], g12[11]};
+    const float det = det3<true>(v01, v02, v03);
+    const float l1 = __fadd_rn(__fadd_rn(__fmul_rn(v01.x, v01.x), __fmul_rn(v01.y, v01.y)), __fmul_rn(v01.z, v01.z));
+    const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(v02.x, v02.x), __fmul_rn(v02.y, v02.y)), __fmul_rn(v02.z, v02.z));
+    const float l3 = __fadd_rn(__fadd_rn(__fmul_rn(v03.x, v03.x), __fmul_rn(v03.y, v03.y)), __fmul_rn(v03.z, v03.z));
+    return __fmul_rn(det, det) < __fmul_rn(kNearDegenerate * kNearDegenerate, __fmul_rn(__fmul_rn(l1, l2), l3));
+}
+
+// Barycentrics (b1, b2, b3 in y, z, w; b0 in x) of tetrahedron t in float64
+// from its stored float32 geometry, rounded once to float32; |det| < 1e-10
+// gives det = 1 as in the float32 solve.
+static __device__ __noinline__ float4 bary_f64(const V3 q, const float* tet_geom, int t) {
+    const float4* g = reinterpret_cast<const float4*>(tet_geom) + 4 * (int64_t)t;
+    const float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
+    const V3 v0{g0.x, g0.y, g0.z};
+    const V3 a{g0.w, g1.x, g1.y}, b{g1.z, g1.w, g2.x}, c{g2.y, g2.z, g2.w};
+    const double px = (double)q.x - (double)v0.x, py = (double)q.y - (double)v0.y, pz = (double)q.z - (double)v0.z;
+    double det = det3_f64(a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z);
+    if (fabs(det) < 1e-10) det = 1.0;
+    const double y = det3_f64(px, py, pz, b.x, b.y, b.z, c.x, c.y, c.z) / det;
+    const double z = det3_f64(a.x, a.y, a.z, px, py, pz, c.x, c.y, c.z) / det;
+    const double w = det3_f64(a.x, a.y, a.z, b.x, b.y, b.z, px, py, pz) / det;
+    return make_float4((float)(1.0 - y - z - w), (float)y, (float)z, (float)w);
+}
+
 // Barycentric test of tetrahedron t (point_in_tetrahedron_fast,
 // …optimized.py:218-250, and point_in_tetrahedron, fem_interpolator.py:146-207,
 // which compute the same thing): true when the query's box test and the
@@ -33,7 +75,7 @@ __device__ __forceinline__ float det3(const V3& c0, const V3& c1, const V3& c2) 
 // the vertex ids.
 template <bool EXACT>
 __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, const float* tet_geom, int t,
-                                         float4& b, int4& cn) {
+                                         float4& b, int4& cn, bool& near) {
     typedef Ar<EXACT> A;
     const float4* bx = reinterpret_cast<const float4*>(tet_box) + 2 * (int64_t)t;
     const float4 mn = __ldg(bx), mx = __ldg(bx + 1);
@@ -44,6 +86,7 @@ __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, cons
     const V3 v01{g0.w, g1.x, g1.y}, v02{g1.z, g1.w, g2.x}, v03{g2.y, g2.z, g2.w};
     const V3 v0p{A::sub(q.x, v0.x), A::sub(q.y, v0.y), A::sub(q.z, v0.z)};
     float det = det3<EXACT>(v01, v02, v03);
+    near = !EXACT && mn.w != 0.0f;
     if (fabsf(det) < 1e-10f) det = 1.0f;
     b.y = A::div(det3<EXACT>(v0p, v02, v03), det);
     b.z = A::div(det3<EXACT>(v01, v0p, v03), det);
@@ -105,7 +148,10 @@ struct MeshField {
         for (int s = 0; s < cnt; ++s) {
             float4 b;
             int4 cn;
-            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, __ldg(L + s), b, cn)) continue;
+            bool near;
+            const int t = __ldg(L + s);
+            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
+            if (!EXACT && near) b = bary_f64(q, F.tet_geom, t);
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
                                      node_value(cn.w, e));
         }

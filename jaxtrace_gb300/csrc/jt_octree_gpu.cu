@@ -26,10 +26,21 @@
 #include <vector>
 
 #include "jt_internal.h"
+#include "jt_mesh.cuh"
 
 namespace jt {
 
 constexpr int kOctBlock = 256;
+
+__global__ void __launch_bounds__(kOctBlock) k_mark_near_degenerate(float* __restrict__ tet_box,
+                                                                    const float* __restrict__ tet_geom, int n_tets,
+                                                                    int* __restrict__ count) {
+    const int t = blockIdx.x * kOctBlock + threadIdx.x;
+    if (t >= n_tets) return;
+    const bool near = near_degenerate(tet_geom + 16 * (int64_t)t);
+    tet_box[8 * (int64_t)t + 3] = near ? 1.0f : 0.0f;
+    if (near) atomicAdd(count, 1);
+}
 
 __device__ __forceinline__ float oct_centre(float mn, float mx) { return __fmul_rn(__fadd_rn(mn, mx), 0.5f); }
 
@@ -554,4 +565,27 @@ extern "C" void jt_octree_free_device(void* handle, void* stream) {
     cudaFreeAsync(T->nodes, s);
     cudaFreeAsync(T->bounds, s);
     delete T;
+}
+
+extern "C" int jt_mark_near_degenerate(float* tet_box, const float* tet_geom, int32_t n_tets, int32_t* count_out,
+                                       void* stream) {
+    if (n_tets < 0) return set_error(JT_ERR_INVALID, "n_tets must be >= 0");
+    if (n_tets > 0 && (tet_box == nullptr || tet_geom == nullptr))
+        return set_error(JT_ERR_INVALID, "tet_box and tet_geom are required");
+    cudaStream_t s = (cudaStream_t)stream;
+    int* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(int), s);
+    if (e == cudaSuccess && n_tets > 0) {
+        k_mark_near_degenerate<<<(unsigned)((n_tets + kOctBlock - 1) / kOctBlock), kOctBlock, 0, s>>>(tet_box, tet_geom,
+                                                                                                   n_tets, d);
+        e = cudaGetLastError();
+    }
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (d != nullptr) cudaFreeAsync(d, s);
+    if (e != cudaSuccess) return cuda_status(e, "near-degenerate marking");
+    if (count_out != nullptr) *count_out = h;
+    return JT_OK;
 }

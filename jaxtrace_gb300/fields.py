@@ -35,6 +35,15 @@ def _torch_cuda():
     return torch
 
 
+def _mark_near_degenerate(tet_box, tet_geom) -> int:
+    """Flag the near-degenerate tetrahedra of a field's device box records
+    (jt_mark_near_degenerate); returns how many there are."""
+    n = C.c_int32(0)
+    L.check(L.load().jt_mark_near_degenerate(tet_box.data_ptr(), tet_geom.data_ptr(), tet_box.shape[0],
+                                             C.byref(n), L.stream_ptr()))
+    return int(n.value)
+
+
 def _as_f32(a) -> np.ndarray:
     return np.asarray(a, dtype=F32)
 
@@ -689,9 +698,9 @@ class FEMTimeSeriesField(TimeSeriesField):
         super()._device()
         h = self.fem_mesh
         d = self._dev
-        if h.dev is not None:       # built on the device: no upload
-            d.update({k: h.dev[k] for k in ("tet_box", "tet_geom", "cell_start", "cell_elems", "sub_start",
-                                            "sub_elems")})
+        if h.dev is not None:       # built on the device: no upload (the box records get their own copy)
+            d.update({k: h.dev[k] for k in ("tet_geom", "cell_start", "cell_elems", "sub_start", "sub_elems")})
+            d["tet_box"] = h.dev["tet_box"].clone()
         else:
             d["tet_box"] = torch.from_numpy(h.tet_box).cuda()
             d["tet_geom"] = torch.from_numpy(h.tet_geom).cuda()
@@ -699,6 +708,7 @@ class FEMTimeSeriesField(TimeSeriesField):
             d["cell_elems"] = torch.from_numpy(h.cell_elems if len(h.cell_elems) else np.zeros(1, np.int32)).cuda()
             d["sub_start"] = torch.from_numpy(h.sub_start).cuda()
             d["sub_elems"] = torch.from_numpy(h.sub_elems if len(h.sub_elems) else np.zeros(1, np.int32)).cuda()
+        self.n_near_degenerate = _mark_near_degenerate(d["tet_box"], d["tet_geom"])
         f = L.FemField()
         f.nearest = self._cnear
         f.n_tets = len(h.connectivity)
@@ -859,13 +869,15 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         pts = np.zeros((self.N, 4), dtype=F32)
         pts[:, :3] = self.positions
         d = {"pairs": pairs, "points": torch.from_numpy(pts).cuda()}
-        if m.dev is not None:       # built on the device: no upload
-            d.update({k: m.dev[k] for k in ("tet_box", "tet_geom", "nodes", "elems")})
+        if m.dev is not None:       # built on the device: no upload (the box records get their own copy)
+            d.update({k: m.dev[k] for k in ("tet_geom", "nodes", "elems")})
+            d["tet_box"] = m.dev["tet_box"].clone()
         else:
             d.update({"tet_box": torch.from_numpy(m.tet_box).cuda(), "tet_geom": torch.from_numpy(m.tet_geom).cuda(),
                       "nodes": torch.from_numpy(m.nodes.view(np.int32).reshape(len(m.nodes), 16)).cuda(),
                       "elems": torch.from_numpy(m.elems).cuda()})
         self._dev = d
+        self.n_near_degenerate = _mark_near_degenerate(d["tet_box"], d["tet_geom"])
         f = L.MeshField()
         f.n_points, f.n_tets = self.N, m.connectivity.shape[0]
         f.n_nodes, f.max_depth = int(m.info.n_nodes), m.max_depth
