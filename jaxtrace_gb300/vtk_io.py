@@ -151,14 +151,185 @@ def _read_piece(path: str, geometry: bool = True, names: Optional[List[str]] = N
     return {"points": pts, "n_points": n_points, "cells": cells, "point_data": pdata, "cell_data": cdata}
 
 
+_LEGACY_TYPES = {"float": ">f4", "double": ">f8", "int": ">i4", "unsigned_int": ">u4", "long": ">i8",
+                 "unsigned_long": ">u8", "short": ">i2", "unsigned_short": ">u2", "char": ">i1",
+                 "unsigned_char": ">u1", "vtktypeint64": ">i8", "vtktypeint32": ">i4", "vtkidtype": ">i8"}
+
+
+class _Legacy:
+    """Cursor over a legacy VTK file: header lines and ASCII or big-endian
+    binary value blocks."""
+
+    def __init__(self, raw: bytes):
+        self.raw, self.pos, self.binary = raw, 0, False
+
+    def line(self, skip_blank: bool = True) -> Optional[str]:
+        while self.pos < len(self.raw):
+            end = self.raw.find(b"\n", self.pos)
+            end = len(self.raw) if end < 0 else end
+            text = self.raw[self.pos:end].decode("latin-1").strip()
+            self.pos = end + 1
+            if text or not skip_blank:
+                return text
+        return None
+
+    def values(self, count: int, vtype: str) -> np.ndarray:
+        dt = np.dtype(_LEGACY_TYPES.get(vtype.lower(), ""))
+        if self.binary:
+            nb = count * dt.itemsize
+            a = np.frombuffer(self.raw, dtype=dt, count=count, offset=self.pos)
+            self.pos += nb
+            if self.raw[self.pos:self.pos + 1] == b"\n":
+                self.pos += 1
+            return a.astype(dt.newbyteorder("="))
+        toks: List[bytes] = []
+        while len(toks) < count:
+            end = self.raw.find(b"\n", self.pos)
+            end = len(self.raw) if end < 0 else end
+            toks += self.raw[self.pos:end].split()
+            self.pos = end + 1
+            if end >= len(self.raw) and len(toks) < count:
+                raise ValueError("legacy VTK file ends inside a data block")
+        return np.array(toks[:count], dtype=dt.newbyteorder("="))
+
+
+def _read_legacy(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
+    """A legacy .vtk UNSTRUCTURED_GRID (what vtkUnstructuredGridReader reads,
+    io/vtk_reader.py:633-634): ASCII or BINARY, classic CELLS or the 5.1
+    OFFSETS/CONNECTIVITY layout, point arrays from SCALARS, VECTORS, NORMALS
+    and FIELD blocks; METADATA blocks are skipped."""
+    cur = _Legacy(open(path, "rb").read())
+    if not (cur.line() or "").lower().startswith("# vtk datafile"):
+        raise ValueError(f"{path}: not a legacy VTK file")
+    cur.line(skip_blank=False)                       # title
+    cur.binary = (cur.line() or "").upper() == "BINARY"
+    ds = (cur.line() or "").split()
+    if len(ds) < 2 or ds[0].upper() != "DATASET" or ds[1].upper() != "UNSTRUCTURED_GRID":
+        raise ValueError(f"{path}: only DATASET UNSTRUCTURED_GRID is read ({' '.join(ds)})")
+    pts, cells, pdata, cdata = None, {}, {}, {}
+    n_points, target = 0, None
+    while True:
+        ln = cur.line()
+        if ln is None:
+            break
+        tok = ln.split()
+        key = tok[0].upper()
+        if key == "METADATA":
+            while cur.line(skip_blank=False):
+                pass
+        elif key == "POINTS":
+            n_points = int(tok[1])
+            pts = cur.values(3 * n_points, tok[2]).astype(F32).reshape(-1, 3)
+        elif key == "CELLS":
+            n0, n1 = int(tok[1]), int(tok[2])
+            nxt = cur.pos
+            sub = (cur.line() or "").split()
+            if sub and sub[0].upper() == "OFFSETS":        # 5.1 layout: n0 offsets, n1 ids
+                offs = cur.values(n0, sub[1]).astype(np.int64)
+                sub = (cur.line() or "").split()
+                conn = cur.values(n1, sub[1]).astype(np.int64)
+                cells.update(connectivity=conn, offsets=offs[1:])
+            else:                                          # classic: n0 records, n1 ints
+                cur.pos = nxt
+                rec = cur.values(n1, "int").astype(np.int64)
+                ks, at = [], 0
+                while at < len(rec):
+                    ks.append(at)
+                    at += int(rec[at]) + 1
+                ks = np.array(ks, dtype=np.int64)
+                cnt = rec[ks]
+                keep = np.ones(len(rec), bool)
+                keep[ks] = False
+                cells.update(connectivity=rec[keep], offsets=np.cumsum(cnt))
+        elif key == "CELL_TYPES":
+            cells["types"] = cur.values(int(tok[1]), "int").astype(np.uint8)
+        elif key in ("POINT_DATA", "CELL_DATA"):
+            target = (pdata, int(tok[1])) if key == "POINT_DATA" else (cdata, int(tok[1]))
+        elif key in ("SCALARS", "VECTORS", "NORMALS") and target is not None:
+            d, n = target
+            nc = (int(tok[3]) if len(tok) > 3 else 1) if key == "SCALARS" else 3
+            if key == "SCALARS":
+                lt = cur.pos
+                if not (cur.line() or "").upper().startswith("LOOKUP_TABLE"):
+                    cur.pos = lt
+            a = cur.values(n * nc, tok[2])
+            d[tok[1]] = a.reshape(n, nc) if nc > 1 else a
+        elif key == "FIELD" and target is not None:
+            d, _ = target
+            for _ in range(int(tok[2])):
+                ft = (cur.line() or "").split()
+                while ft and ft[0].upper() == "METADATA":
+                    while cur.line(skip_blank=False):
+                        pass
+                    ft = (cur.line() or "").split()
+                nm, nc, nt = ft[0], int(ft[1]), int(ft[2])
+                a = cur.values(nc * nt, ft[3])
+                d[nm] = a.reshape(nt, nc) if nc > 1 else a
+        elif key == "LOOKUP_TABLE":
+            cur.values(4 * int(tok[2]), "float")
+        else:
+            raise ValueError(f"{path}: unsupported legacy VTK section {tok[0]!r}")
+    if names is not None:
+        pdata = {k: (v if k in names else None) for k, v in pdata.items()}
+    return {"points": pts if geometry else None, "n_points": n_points, "cells": cells if geometry else {},
+            "point_data": pdata, "cell_data": cdata}
+
+
+def write_vtk_legacy(path: str, points: np.ndarray, tets: Optional[np.ndarray] = None,
+                     point_data: Optional[Dict[str, np.ndarray]] = None, binary: bool = True,
+                     layout: str = "classic") -> None:
+    """A legacy .vtk UNSTRUCTURED_GRID of tetrahedra with point data (1- or
+    3-component arrays as SCALARS / VECTORS, others in a FIELD block);
+    ``layout`` "classic" (CELLS n size) or "5.1" (OFFSETS/CONNECTIVITY)."""
+    pts = np.ascontiguousarray(points, dtype=F32).reshape(-1, 3)
+    t4 = np.zeros((0, 4), np.int64) if tets is None else np.asarray(tets, dtype=np.int64).reshape(-1, 4)
+    out = [f"# vtk DataFile Version {'5.1' if layout == '5.1' else '3.0'}\nwritten by jaxtrace_gb300\n"
+           f"{'BINARY' if binary else 'ASCII'}\nDATASET UNSTRUCTURED_GRID\n".encode()]
+
+    def block(a: np.ndarray, be: str) -> bytes:
+        if binary:
+            return np.ascontiguousarray(a).astype(be).tobytes() + b"\n"
+        flat = a.reshape(-1).tolist()
+        return (" ".join(repr(x) if a.dtype.kind == "f" else str(x) for x in flat) + "\n").encode()
+
+    out.append(f"POINTS {len(pts)} float\n".encode() + block(pts, ">f4"))
+    if layout == "5.1":
+        offs = 4 * np.arange(len(t4) + 1, dtype=np.int64)
+        out.append(f"CELLS {len(offs)} {t4.size}\nOFFSETS vtktypeint64\n".encode() + block(offs, ">i8"))
+        out.append(b"CONNECTIVITY vtktypeint64\n" + block(t4.reshape(-1), ">i8"))
+    else:
+        rec = np.concatenate([np.full((len(t4), 1), 4, np.int64), t4], axis=1).astype(np.int32)
+        out.append(f"CELLS {len(t4)} {rec.size}\n".encode() + block(rec, ">i4"))
+    out.append(f"CELL_TYPES {len(t4)}\n".encode() + block(np.full(len(t4), VTK_TETRA, np.int32), ">i4"))
+    fields = []
+    if point_data:
+        out.append(f"POINT_DATA {len(pts)}\n".encode())
+        for k, v in point_data.items():
+            v = np.asarray(v)
+            nc = v.shape[1] if v.ndim > 1 else 1
+            tname, be = ("float", ">f4") if v.dtype.kind == "f" else ("int", ">i4")
+            if nc == 3 and v.dtype.kind == "f":
+                out.append(f"VECTORS {k} {tname}\n".encode() + block(v.astype(be[1:]), be))
+            elif nc == 1:
+                out.append(f"SCALARS {k} {tname} 1\nLOOKUP_TABLE default\n".encode() + block(v.astype(be[1:]), be))
+            else:
+                fields.append((k, v, nc, tname, be))
+        if fields:
+            out.append(f"FIELD FieldData {len(fields)}\n".encode())
+            for k, v, nc, tname, be in fields:
+                out.append(f"{k} {nc} {len(v)} {tname}\n".encode() + block(v.astype(be[1:]), be))
+    with open(path, "wb") as fh:
+        fh.write(b"".join(out))
+
+
 def read_vtk_xml(path: str, geometry: bool = True, names: Optional[List[str]] = None) -> Dict[str, Any]:
     """points (N,3) float32, cells {connectivity, offsets, types} and
-    point_data {name: (N,) or (N,C)} of a .vtu file, or of a .pvtu file's
+    point_data {name: (N,) or (N,C)} of a .vtu (or .vtp, or legacy .vtk) file, or of a .pvtu file's
     pieces appended in order (point ids of later pieces shifted).  Without
     ``geometry`` points and cells are skipped; with ``names`` only those
     point arrays are decoded (the others map to None)."""
     if path.lower().endswith(".vtk"):
-        raise NotImplementedError(f"{path}: legacy .vtk files are not read; convert to .vtu")
+        return _read_legacy(path, geometry, names)
     if not path.lower().endswith(".pvtu"):
         return _read_piece(path, geometry, names)
     root = ET.parse(path).getroot()

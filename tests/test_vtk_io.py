@@ -146,3 +146,40 @@ def test_trajectory_writer_points_and_lines(tmp_path):
     assert np.array_equal(d["cell_data"]["PathLength"], ref_len)
     assert np.array_equal(d["point_data"]["ParticleID"], np.tile(idx.astype(F32), T))
     assert np.array_equal(d["point_data"]["Time"], np.repeat(times, 4))
+
+
+@pytest.mark.parametrize("binary", [True, False])
+@pytest.mark.parametrize("layout", ["classic", "5.1"])
+def test_legacy_vtk_round_trip(tmp_path, binary, layout):
+    """Legacy .vtk (vtkUnstructuredGridReader's format, io/vtk_reader.py:633)
+    in ASCII and big-endian binary, both cell layouts, SCALARS, VECTORS and
+    FIELD arrays."""
+    rng = np.random.default_rng(2)
+    P = rng.random((30, 3)).astype(F32)
+    T4 = rng.integers(0, 30, size=(12, 4))
+    vel = rng.normal(size=(30, 3)).astype(F32)
+    p = rng.random(30).astype(F32)
+    six = rng.random((30, 6)).astype(F32)
+    ids = np.arange(30, dtype=np.int32)
+    f = tmp_path / "mesh.vtk"
+    V.write_vtk_legacy(str(f), P, T4, {"velocity": vel, "p": p, "tensor": six, "id": ids}, binary=binary,
+                       layout=layout)
+    d = V.read_vtk_xml(str(f))
+    assert np.array_equal(d["points"], P)
+    assert np.array_equal(d["cells"]["connectivity"], T4.reshape(-1))
+    assert np.array_equal(d["cells"]["offsets"], 4 * np.arange(1, 13))
+    assert np.all(d["cells"]["types"] == V.VTK_TETRA)
+    pd = d["point_data"]
+    assert np.array_equal(pd["velocity"], vel) and np.array_equal(pd["p"], p)
+    assert np.array_equal(pd["tensor"], six) and np.array_equal(pd["id"], ids)
+
+
+def test_legacy_vtk_skips_metadata_blocks(tmp_path):
+    f = tmp_path / "m.vtk"
+    f.write_text("# vtk DataFile Version 5.1\nt\nASCII\nDATASET UNSTRUCTURED_GRID\n"
+                 "POINTS 2 float\n0 0 0 1 1 1\nMETADATA\nINFORMATION 0\n\n"
+                 "CELLS 2 1\nOFFSETS vtktypeint64\n0 1\nCONNECTIVITY vtktypeint64\n0\n"
+                 "CELL_TYPES 1\n1\nPOINT_DATA 2\nVECTORS U float\n1 2 3 4 5 6\nMETADATA\nINFORMATION 0\n\n")
+    d = V.read_vtk_xml(str(f))
+    assert np.array_equal(d["point_data"]["U"], np.array([[1, 2, 3], [4, 5, 6]], F32))
+    assert np.array_equal(d["cells"]["offsets"], [1]) and np.array_equal(d["cells"]["types"], [1])
