@@ -161,6 +161,8 @@ typedef struct {
     int32_t max_depth;      /* traversal iterations (reference default 12)   */
     int32_t storage;        /* JT_STORE_* of the node values                  */
     int32_t n_pairs;
+    int32_t near_degenerate; /* nonzero: tet_box flags some tetrahedra (jt_mark_near_degenerate) */
+    int32_t pad;
     int64_t pair_stride;    /* records per pair (= n_points)                  */
     const float* points;    /* device (n_points,4): x,y,z,0                   */
     const float* tet_box;   /* device (n_tets,8): min xyz,flag, max xyz,0 (flag: jt_mark_near_degenerate) */
@@ -211,7 +213,7 @@ typedef struct {
      * sub-cell list, and every element before it there is before it in the
      * cell list too.  sub_div 0: scan the cell lists. */
     int32_t sub_div;
-    int32_t pad;
+    int32_t near_degenerate; /* nonzero: tet_box flags some tetrahedra (jt_mark_near_degenerate) */
     const int32_t* sub_start;  /* device (cells*sub_div^3 + 1) CSR offsets     */
     const int32_t* sub_elems;  /* device element ids                          */
 } jt_fem_field;

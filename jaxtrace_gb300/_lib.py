@@ -59,7 +59,7 @@ OCTREE_NODE_DTYPE = np.dtype([("c", "<f4", (3,)), ("is_leaf", "<i4"), ("children
 
 class MeshField(C.Structure):
     _fields_ = [("n_points", i32), ("n_tets", i32), ("n_nodes", i32), ("max_depth", i32),
-                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64),
+                ("storage", i32), ("n_pairs", i32), ("near_degenerate", i32), ("pad", i32), ("pair_stride", i64),
                 ("points", vp), ("tet_box", vp), ("tet_geom", vp), ("nodes", vp), ("elems", vp),
                 ("pairs", vp)]
 
@@ -73,7 +73,7 @@ class NearestField(C.Structure):
 class FemField(C.Structure):
     _fields_ = [("nearest", NearestField), ("n_tets", i32), ("grid_size", i32 * 3), ("grid_min", f32 * 3),
                 ("cell_size", f32 * 3), ("tet_box", vp), ("tet_geom", vp), ("cell_start", vp), ("cell_elems", vp),
-                ("sub_div", i32), ("pad", i32), ("sub_start", vp), ("sub_elems", vp)]
+                ("sub_div", i32), ("near_degenerate", i32), ("sub_start", vp), ("sub_elems", vp)]
 
 
 class Field(C.Structure):

@@ -13,13 +13,14 @@
 
 namespace jt {
 
-template <bool EXACT, int STORE>
-struct FemField {
+// NEAR as in MeshFieldT
+template <bool EXACT, int STORE, bool NEAR = false>
+struct FemFieldT {
     static constexpr int kMinBlocks = JT_MESH_MIN_BLOCKS;
     jt_fem_field F;
     float h_min;  // smallest nearest-node cell edge (ring-stop bound)
 
-    static FemField create(const jt_fem_field& d, float h) { return FemField{d, h}; }
+    static FemFieldT create(const jt_fem_field& d, float h) { return FemFieldT{d, h}; }
 
     __device__ __forceinline__ V3 node_value(int node, const jt_blend& e) const {
         const int64_t base = (int64_t)min(max(e.pair, 0), F.nearest.n_pairs - 1) * F.nearest.pair_stride;
@@ -72,7 +73,7 @@ struct FemField {
             bool near;
             const int t = __ldg(list + s);
             if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
-            if (!EXACT && near) b = bary_f64(q, F.tet_geom, t);
+            if (NEAR && !EXACT && near) b = bary_f64(q, F.tet_geom, t);
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
                                      node_value(cn.w, e));
         }
@@ -81,5 +82,10 @@ struct FemField {
         return node_value(nearest_id<EXACT>(F.nearest, h_min, q), e);
     }
 };
+
+template <bool EXACT, int STORE>
+using FemField = FemFieldT<EXACT, STORE, false>;
+template <bool EXACT, int STORE>
+using FemFieldNear = FemFieldT<EXACT, STORE, true>;
 
 }  // namespace jt

@@ -37,6 +37,12 @@ int mesh_step(const jt_mesh_field& f, int arith, const StageBlends& sb, int inte
 int mesh_sample(const jt_mesh_field& f, int arith, const jt_blend& e, const float* pos, float* out,
                 int m, int32_t* status, cudaStream_t s);
 
+int mesh_track_near(const jt_mesh_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+int mesh_step_near(const jt_mesh_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+                   const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
+int mesh_sample_near(const jt_mesh_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+                     int m, int32_t* status, cudaStream_t s);
+
 int nearest_track(const jt_nearest_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
 int nearest_step(const jt_nearest_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
                  const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
@@ -50,5 +56,10 @@ int fem_step(const jt_fem_field& f, int arith, const StageBlends& sb, int integ,
              const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
 int fem_sample(const jt_fem_field& f, int arith, const jt_blend& e, const float* pos, float* out,
                int m, int32_t* status, cudaStream_t s);
+int fem_track_near(const jt_fem_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
+int fem_step_near(const jt_fem_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
+                  const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);
+int fem_sample_near(const jt_fem_field& f, int arith, const jt_blend& e, const float* pos, float* out,
+                    int m, int32_t* status, cudaStream_t s);
 
 }  // namespace jt

@@ -112,14 +112,17 @@ __device__ __forceinline__ V3 p1_combine(const float4& b, const V3& n0, const V3
 #define JT_MESH_MIN_BLOCKS 4
 #endif
 
-template <bool EXACT, int STORE>
-struct MeshField {
+// NEAR: re-solve flagged near-degenerate tetrahedra in float64 (compensated
+// arithmetic only); launched only for fields that have flagged ones, so the
+// out-of-line call costs nothing elsewhere.
+template <bool EXACT, int STORE, bool NEAR = false>
+struct MeshFieldT {
     // the dependent gather chain is latency-bound: 4 blocks of 256 (64
     // registers, no spills) keep more warps in flight than the default 3
     static constexpr int kMinBlocks = JT_MESH_MIN_BLOCKS;
     jt_mesh_field F;
 
-    static MeshField create(const jt_mesh_field& d, int) { return MeshField{d}; }
+    static MeshFieldT create(const jt_mesh_field& d, int) { return MeshFieldT{d}; }
 
     __device__ __forceinline__ V3 node_value(int node, const jt_blend& e) const {
         const int64_t base = (int64_t)min(max(e.pair, 0), F.n_pairs - 1) * F.pair_stride;
@@ -151,7 +154,7 @@ struct MeshField {
             bool near;
             const int t = __ldg(L + s);
             if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
-            if (!EXACT && near) b = bary_f64(q, F.tet_geom, t);
+            if (NEAR && !EXACT && near) b = bary_f64(q, F.tet_geom, t);
             return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
                                      node_value(cn.w, e));
         }
@@ -175,5 +178,10 @@ struct MeshField {
         return node_value(best, e);
     }
 };
+
+template <bool EXACT, int STORE>
+using MeshField = MeshFieldT<EXACT, STORE, false>;
+template <bool EXACT, int STORE>
+using MeshFieldNear = MeshFieldT<EXACT, STORE, true>;
 
 }  // namespace jt

@@ -719,6 +719,7 @@ class FEMTimeSeriesField(TimeSeriesField):
         f.cell_start, f.cell_elems = d["cell_start"].data_ptr(), d["cell_elems"].data_ptr()
         f.sub_div = h.sub_div
         f.sub_start, f.sub_elems = d["sub_start"].data_ptr(), d["sub_elems"].data_ptr()
+        f.near_degenerate = int(self.n_near_degenerate > 0)
         self._cfem = f
         self._cfield = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(f))
 
@@ -884,6 +885,7 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         f.storage, f.n_pairs, f.pair_stride = self._storage, pairs.shape[0], self.N
         f.points, f.tet_box, f.tet_geom = d["points"].data_ptr(), d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
         f.nodes, f.elems, f.pairs = d["nodes"].data_ptr(), d["elems"].data_ptr(), pairs.data_ptr()
+        f.near_degenerate = int(self.n_near_degenerate > 0)
         self._cmesh = f
         self._cfield = L.Field(kind=L.JT_FIELD_MESH, mesh=C.pointer(f))
 
