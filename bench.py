@@ -87,7 +87,7 @@ def args_parse():
     p.add_argument("--adj-lattice", default="256,256,64", help="seed lattice of the adjoint leg")
     p.add_argument("--adj-steps", type=int, default=500)
     p.add_argument("--density-particles", type=int, default=16_000_000)
-    p.add_argument("--leg", default=None, choices=["fem", "batch", "adjoint", "density"],
+    p.add_argument("--leg", default=None, choices=["fem", "fem_hash", "batch", "adjoint", "density"],
                    help="run one configuration leg alone and print its JSON (with --profile: the leg's timed "
                         "region bracketed by cudaProfilerStart/Stop)")
     p.add_argument("--profile", action="store_true",
@@ -466,6 +466,40 @@ def octree_build_times(c):
             "leaves": int(h.info.n_leaves), "depth": int(h.info.max_tree_depth), "same_arrays": same}
 
 
+def fem_hash_leg(a, profile=False):
+    """The unstructured FEM configuration through the hash-grid field alone
+    (FEMTimeSeriesField, 32^3 cells, 4^3 sub-cells): one timed pass of
+    ``--fem-steps`` steps (with --profile bracketed by cudaProfilerStart/Stop)."""
+    import torch
+
+    import jaxtrace_gb300 as jt
+    from jaxtrace_gb300 import workloads as W
+    c = W.fem_case(n_steps=a.fem_steps)
+    f = jt.FEMTimeSeriesField(c["data"], c["times"], c["points"], c["tets"])
+    bc = jt.mixed_boundary(W.UNIT, c["conditions"])
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
+    times = np.linspace(c["time_span"][0], c["time_span"][1], c["n_timesteps"], dtype=np.float32)
+    x0 = torch.from_numpy(c["x0"]).cuda()
+    pos = torch.empty_like(x0)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sched = torch.from_numpy(tr._schedule(times, c["dt"]).view(np.int32).reshape(-1, 8)).cuda()
+
+    def one():
+        pos.copy_(x0)
+        return tr.track_device(pos, times, c["dt"], status, None, sched)
+
+    one()
+    torch.cuda.synchronize()
+    if profile:
+        torch.cuda.profiler.start()
+    ms = _timed(one, 1)
+    if profile:
+        torch.cuda.profiler.stop()
+    n = len(c["x0"])
+    return {"value": n * a.fem_steps / (ms / 1e3), "unit": UNIT, "ms_per_pass": ms, "steps": a.fem_steps,
+            "status": int(status.item())}
+
+
 def fem_grid_build_times(c):
     """Hash grid (32^3 cells, 4^3 sub-cells each) of the FEM mesh from host
     arrays: the host builder with its NumPy element records, and the device
@@ -707,7 +741,7 @@ def main():
         if a.leg == "adjoint":
             out = adjoint_leg(a, profile=a.profile)
         else:
-            out = {"fem": fem_leg, "batch": batch_leg,
+            out = {"fem": fem_leg, "fem_hash": fem_hash_leg, "batch": batch_leg,
                    "density": lambda a, profile: batch_leg(a, profile, part="density")}[a.leg](a, profile=a.profile)
         if rank == 0:
             print(json.dumps({"leg": a.leg} | out), flush=True)
