@@ -11,7 +11,9 @@ from .boundary import (absorbing_boundary_factory, clamping_boundary, continuous
 from .fields import (FEMTimeSeriesField, FemHashGrid, OctreeFEMTimeSeriesFieldOptimized, OctreeMesh, StructuredGridSampler,
                      StructuredTimeSeriesField, TimeSeriesField)
 from .integrators import euler_step, rk2_step, rk4_step
-from .particles import Trajectory, compute_trajectory_statistics
+from .particles import (Trajectory, compute_trajectory_statistics, create_empty_trajectory,
+                        create_single_particle_trajectory, create_trajectory_from_positions, merge_trajectories,
+                        validate_trajectory_data)
 from .analysis import compute_mixing_metrics
 from .seeding import random_seeds, uniform_grid_seeds
 from .tracker import EnsembleBatch, ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
@@ -28,5 +30,6 @@ __all__ = [
     "continuous_inlet_boundary_factory", "no_boundary", "unit_box_periodic", "unit_box_reflective",
     "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid", "compute_trajectory_statistics",
     "compute_mixing_metrics", "VTKTrajectoryWriter", "VTKTrajectorySeries", "VTKUnstructuredTimeSeriesReader",
-    "open_vtk_time_series",
+    "open_vtk_time_series", "create_trajectory_from_positions", "create_single_particle_trajectory",
+    "create_empty_trajectory", "merge_trajectories", "validate_trajectory_data",
 ]
