@@ -16,7 +16,8 @@ from .particles import (Trajectory, compute_trajectory_statistics, create_empty_
                         validate_trajectory_data)
 from .analysis import compute_mixing_metrics
 from .seeding import random_seeds, uniform_grid_seeds
-from .tracker import EnsembleBatch, ParticleTracker, TrackerOptions, create_tracker, track_particles_simple
+from .tracker import (EnsembleBatch, ParticleTracker, TrackerOptions, compare_integrators, create_tracker,
+                      track_particles_simple)
 from .autotune import Autotuner
 from .vtk_io import VTKTrajectorySeries, VTKTrajectoryWriter, VTKUnstructuredTimeSeriesReader, open_vtk_time_series
 
@@ -31,5 +32,5 @@ __all__ = [
     "EnsembleBatch", "Autotuner", "FEMTimeSeriesField", "FemHashGrid", "compute_trajectory_statistics",
     "compute_mixing_metrics", "VTKTrajectoryWriter", "VTKTrajectorySeries", "VTKUnstructuredTimeSeriesReader",
     "open_vtk_time_series", "create_trajectory_from_positions", "create_single_particle_trajectory",
-    "create_empty_trajectory", "merge_trajectories", "validate_trajectory_data",
+    "create_empty_trajectory", "merge_trajectories", "validate_trajectory_data", "compare_integrators",
 ]

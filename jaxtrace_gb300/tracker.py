@@ -461,6 +461,94 @@ class ParticleTracker:
                                 "record_velocities": self.options.record_velocities}
         return res
 
+    def benchmark_performance(self, test_sizes=(100, 500, 1000, 5000), n_timesteps: int = 100) -> Dict[str, Any]:
+        """Wall time of track_particles at each size, particle-steps/s, the
+        trajectory's size and the fitted scaling exponent (tracker.py:590-657)."""
+        import math
+        import time
+        res: Dict[str, Any] = {"test_sizes": list(test_sizes), "n_timesteps": int(n_timesteps), "timing_results": {},
+                               "memory_usage": {}, "throughput": {}, "scalability": {}}
+        for n in test_sizes:
+            x0 = np.random.uniform(-1, 1, size=(n, 3)).astype(F32)
+            t0 = time.time()
+            try:
+                traj = self.track_particles(x0, (0.0, 1.0), n_timesteps)
+                el = time.time() - t0
+                res["timing_results"][n] = el
+                res["memory_usage"][n] = traj.memory_usage_mb()
+                res["throughput"][n] = n * n_timesteps / max(el, 1e-9)
+            except Exception:  # noqa: BLE001 -- recorded as a failed size, as the reference does
+                res["timing_results"][n] = res["memory_usage"][n] = res["throughput"][n] = None
+        ok = [s for s in test_sizes if res["timing_results"][s] is not None]
+        if len(ok) >= 2:
+            xs = [math.log(ok[i + 1] / ok[i]) for i in range(len(ok) - 1)]
+            tr = [res["timing_results"][ok[i + 1]] / res["timing_results"][ok[i]] for i in range(len(ok) - 1)]
+            if all(r > 0 for r in tr):
+                ys = [math.log(r) for r in tr]
+                mx, my = sum(xs) / len(xs), sum(ys) / len(ys)
+                den = sum((x - mx) ** 2 for x in xs)
+                if den > 0:
+                    k = sum((x - mx) * (y - my) for x, y in zip(xs, ys)) / den
+                    res["scalability"] = {"scaling_exponent": k, "complexity": f"O(N^{k:.2f})"}
+        return res
+
+    def analyze_field_sampling(self, test_positions, time_points) -> Dict[str, Any]:
+        """Sampling time per call and velocity statistics of the field at the
+        given positions and times (tracker.py:659-718)."""
+        import time
+        q = ensure_positions_shape(test_positions)
+        tp = np.asarray(time_points, dtype=F32)
+        res: Dict[str, Any] = {"num_positions": q.shape[0], "num_times": len(tp), "sampling_stats": {},
+                               "performance": {}, "field_properties": {}}
+        vels, secs = [], []
+        for t in tp:
+            t0 = time.time()
+            try:
+                v = np.asarray(self._field.sample_at_positions(q, float(t)), dtype=F32)
+            except Exception as e:  # noqa: BLE001
+                res["field_properties"]["sampling_error"] = str(e)
+                return res
+            secs.append(time.time() - t0)
+            vels.append(v)
+        if secs:
+            m = float(np.mean(secs))
+            res["performance"] = {"mean_sampling_time": m, "sampling_rate_per_second": q.shape[0] / max(m, 1e-9),
+                                  "total_samples": q.shape[0] * len(tp)}
+            a = np.concatenate(vels, axis=0)
+            mags = np.linalg.norm(a, axis=1)
+            res["field_properties"] = {
+                "velocity_magnitude": {"mean": float(np.mean(mags)), "std": float(np.std(mags)),
+                                       "min": float(np.min(mags)), "max": float(np.max(mags))},
+                "velocity_components": {ax: {"mean": float(np.mean(a[:, k])), "std": float(np.std(a[:, k]))}
+                                        for k, ax in enumerate("xyz")},
+                "finite_values": int(np.sum(np.isfinite(a).all(axis=1))),
+                "infinite_values": int(np.sum(np.isinf(a).any(axis=1))),
+                "nan_values": int(np.sum(np.isnan(a).any(axis=1)))}
+        return res
+
+    def get_memory_info(self) -> Dict[str, Any]:
+        """Host memory of this process (tracker.py:789-805), plus the GPU's
+        free and total memory."""
+        out: Dict[str, Any]
+        try:
+            import psutil
+            proc = psutil.Process()
+            mem = proc.memory_info()
+            vm = psutil.virtual_memory()
+            out = {"available": True, "rss_mb": mem.rss / 1024 ** 2, "vms_mb": mem.vms / 1024 ** 2,
+                   "percent": proc.memory_percent(), "system_available_mb": vm.available / 1024 ** 2,
+                   "system_total_mb": vm.total / 1024 ** 2}
+        except Exception:  # noqa: BLE001
+            out = {"available": False, "message": "psutil not available"}
+        try:
+            import torch
+            if torch.cuda.is_available():
+                free, total = torch.cuda.mem_get_info()
+                out["device_free_mb"], out["device_total_mb"] = free / 1024 ** 2, total / 1024 ** 2
+        except Exception:  # noqa: BLE001
+            pass
+        return out
+
     def estimate_runtime(self, n_particles: int, n_timesteps: int, calibration_particles: int = 1000,
                          calibration_steps: int = 10) -> Dict[str, Any]:
         """tracker.py:538-588 with a GPU calibration run."""
@@ -989,3 +1077,31 @@ def track_particles_simple(initial_positions, velocity_field, time_span, n_times
 
 
 __all__ = ["TrackerOptions", "ParticleTracker", "create_tracker", "track_particles_simple"]
+
+
+def compare_integrators(initial_positions, velocity_field, time_span: Tuple[float, float], n_timesteps: int,
+                        integrators=("euler", "rk2", "rk4"), dt: Optional[float] = None, **options) -> Dict[str, Any]:
+    """Each integrator over the same run without boundaries: trajectories,
+    wall times and final-position differences against the first
+    (tracker.py:882-951)."""
+    import time
+    from .boundary import no_boundary
+    res: Dict[str, Any] = {"integrators": list(integrators), "trajectories": {}, "timing": {}, "comparison": {}}
+    for name in integrators:
+        try:
+            tr = create_tracker(name, velocity_field, no_boundary(), **options)
+            t0 = time.time()
+            traj = tr.track_particles(initial_positions, time_span, n_timesteps, dt=dt)
+            res["trajectories"][name], res["timing"][name] = traj, time.time() - t0
+        except Exception:  # noqa: BLE001 -- recorded as a failed integrator, as the reference does
+            res["trajectories"][name] = res["timing"][name] = None
+    ok = {k: v for k, v in res["trajectories"].items() if v is not None}
+    if len(ok) >= 2:
+        names = list(ok)
+        ref = ok[names[0]].positions[-1]
+        for name in names[1:]:
+            d = np.linalg.norm(ok[name].positions[-1] - ref, axis=1)
+            res["comparison"][f"{name}_vs_{names[0]}"] = {"mean_difference": float(np.mean(d)),
+                                                          "max_difference": float(np.max(d)),
+                                                          "std_difference": float(np.std(d))}
+    return res

@@ -63,3 +63,23 @@ def test_pair_term_counts_ordered_pairs_within_the_cutoff():
     assert n == int(mask.sum())
     assert s / n == pytest.approx(np.log(1.5), rel=1e-5)
     assert pair_log_ratio(x0[:0], x1[:0]) == (0.0, 0)
+
+
+def test_tracker_diagnostics(golden):
+    """benchmark_performance, analyze_field_sampling, get_memory_info and
+    compare_integrators (tracking/tracker.py:590-805, :882-951)."""
+    g = golden("track_grid")
+    f = jt.StructuredTimeSeriesField(g["D"], g["st"], g["g"], g["g"], g["g"], "periodic")
+    tr = jt.create_tracker("rk4", f, jt.periodic_boundary(((0, 0, 0), (1, 1, 1))))
+    b = tr.benchmark_performance((64, 256), n_timesteps=11)
+    assert all(b["throughput"][n] > 0 for n in (64, 256)) and "scaling_exponent" in b["scalability"]
+    q = np.random.default_rng(0).random((100, 3)).astype(np.float32)
+    a = tr.analyze_field_sampling(q, [0.0, 0.05])
+    assert a["performance"]["total_samples"] == 200 and a["field_properties"]["finite_values"] == 200
+    ref = np.concatenate([f.sample_at_positions(q, 0.0), f.sample_at_positions(q, 0.05)])
+    assert a["field_properties"]["velocity_magnitude"]["max"] == float(np.linalg.norm(ref, axis=1).max())
+    m = tr.get_memory_info()
+    assert m["device_total_mb"] > 0
+    c = jt.compare_integrators(g["x0"][:50], f, (0.0, 0.1), 11, dt=0.01)
+    assert set(c["timing"]) == {"euler", "rk2", "rk4"} and "rk2_vs_euler" in c["comparison"]
+    assert c["comparison"]["rk4_vs_euler"]["max_difference"] > 0
