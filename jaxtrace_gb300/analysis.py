@@ -66,3 +66,29 @@ def compute_mixing_metrics(trajectory) -> Dict[str, float]:
     out["lyapunov_approximation"] = lyap
     out["mixing_efficiency"] = out["variance_growth_rate"] / (N * trajectory.duration)
     return out
+
+
+def analyze_trajectory_results(trajectory, strategy_info=None, verbose: bool = True):
+    """(statistics, validation) of a trajectory with the spatial spread
+    summary (tracking/analysis.py:13-105)."""
+    from .particles import compute_trajectory_statistics, validate_trajectory_data
+    validation = validate_trajectory_data(trajectory)
+    try:
+        stats = compute_trajectory_statistics(trajectory)
+        s0 = np.std(trajectory.positions[0], axis=0)
+        s1 = np.std(trajectory.positions[-1], axis=0)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            change = np.where(s0 > 0, (s1 / s0 - 1) * 100, np.inf)
+        disp = stats.get("displacement", {})
+        eff = (float(np.sum(disp["values"])) / (trajectory.duration * trajectory.N)
+               if "values" in disp else 0.0)
+        stats["spatial"] = {"initial_spread": s0, "final_spread": s1, "spread_change_percent": change,
+                            "mixing_efficiency": eff}
+        if verbose:
+            print(f"Trajectory {trajectory.positions.shape} (T,N,3), duration {trajectory.duration:.2f}, "
+                  f"validation {'PASSED' if validation['valid'] else 'FAILED'}")
+    except Exception as e:  # noqa: BLE001 -- the reference reports and returns None
+        if verbose:
+            print(f"Statistics failed: {e}")
+        stats = None
+    return stats, validation

@@ -196,3 +196,15 @@ def continuous_inlet_boundary_factory(bounds, flow_axis: str = "x", flow_directi
 __all__ = ["periodic_boundary", "reflective_boundary", "clamping_boundary", "absorbing_boundary_factory",
            "mixed_boundary", "continuous_inlet_boundary_factory", "no_boundary", "unit_box_periodic",
            "unit_box_reflective", "BoundaryDescriptor"]
+
+
+def clamp_to_bounds(x, bounds):
+    """Positions clipped to [lo, hi] per axis (boundary.py:127-144), on the
+    device through the clamping boundary kernel."""
+    return clamping_boundary(bounds)(x)
+
+
+def reflect_boundary(x, bounds):
+    """Sawtooth reflection into [lo, hi] per axis (boundary.py:147-172), on
+    the device through the reflective boundary kernel (the same mapping)."""
+    return reflective_boundary(bounds)(x)

@@ -387,7 +387,10 @@ class VTKUnstructuredTimeSeriesReader:
         self.velocity_cache: Dict[int, np.ndarray] = {}
 
     def _find_time_files(self) -> List[str]:
-        files = glob.glob(os.path.expanduser(self.file_pattern))
+        if isinstance(self.file_pattern, (list, tuple)):       # an explicit file list (open_dataset)
+            files = [os.path.expanduser(f) for f in self.file_pattern]
+        else:
+            files = glob.glob(os.path.expanduser(self.file_pattern))
         pvtu = [f for f in files if f.lower().endswith(".pvtu")]
         vtu = [f for f in files if f.lower().endswith(".vtu")]
         chosen = pvtu if pvtu else vtu
@@ -714,3 +717,25 @@ class VTKTrajectorySeries:
         path = os.path.join(self.output_dir, f"{self.prefix}.pvd")
         write_pvd(path, self.files, self.times)
         return path
+
+
+def open_dataset(path_spec, format_type: Optional[str] = None, **kwargs):
+    """io/registry.py:252-343 for the formats this package reads: VTK
+    (.vtu/.pvtu/.vtk, a pattern or a list of files) opens a
+    VTKUnstructuredTimeSeriesReader; HDF5 reports its backend unavailable
+    (h5py is not installed)."""
+    files = sorted(glob.glob(os.path.expanduser(path_spec))) if isinstance(path_spec, str) else list(path_spec)
+    files = [f for f in files if os.path.exists(f)]
+    if not files:
+        raise FileNotFoundError(f"No files found matching: {path_spec}")
+    ext = os.path.splitext(files[0].lower())[1]
+    if format_type is None:
+        format_type = {".vtu": "vtk", ".pvtu": "vtk", ".vtk": "vtk", ".vtp": "vtk", ".h5": "hdf5", ".hdf5": "hdf5",
+                       ".hdf": "hdf5"}.get(ext)
+        if format_type is None:
+            raise ValueError(f"Unknown file format '{ext}' for file: {files[0]}")
+    if format_type == "hdf5":
+        raise ImportError("HDF5 backend not available. Install required package for HDF5 (h5py)")
+    if format_type != "vtk":
+        raise ValueError(f"Unsupported format: {format_type}")
+    return VTKUnstructuredTimeSeriesReader(path_spec if isinstance(path_spec, str) else files, **kwargs)

@@ -83,3 +83,11 @@ def test_tracker_diagnostics(golden):
     c = jt.compare_integrators(g["x0"][:50], f, (0.0, 0.1), 11, dt=0.01)
     assert set(c["timing"]) == {"euler", "rk2", "rk4"} and "rk2_vs_euler" in c["comparison"]
     assert c["comparison"]["rk4_vs_euler"]["max_difference"] > 0
+
+
+def test_reflect_and_clamp_helpers_match_the_reference(golden):
+    """reflect_boundary / clamp_to_bounds (tracking/boundary.py:127-172)
+    against the reference's outputs."""
+    g = golden("boundary")
+    assert np.array_equal(np.asarray(jt.reflect_boundary(g["P"], g["B"])), g["reflective"])
+    assert np.array_equal(np.asarray(jt.clamp_to_bounds(g["P"], g["B"])), g["clamping"])

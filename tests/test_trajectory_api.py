@@ -92,3 +92,32 @@ def test_constructors_merge_and_validation():
     bad.times[:] = [0, 0.5, 0.4, 1.0]
     r = jt.validate_trajectory_data(bad)
     assert not r["valid"] and any("non-finite" in x for x in r["errors"]) and any("monoton" in x for x in r["errors"])
+
+
+def test_analyze_trajectory_results():
+    tr = _traj()
+    stats, val = jt.analyze_trajectory_results(tr, verbose=False)
+    assert val["valid"] and stats["displacement"]["mean"] == float(np.mean(tr.compute_displacement()))
+    s0, s1 = np.std(tr.positions[0], axis=0), np.std(tr.positions[-1], axis=0)
+    assert np.array_equal(stats["spatial"]["spread_change_percent"], (s1 / s0 - 1) * 100)
+    assert stats["spatial"]["mixing_efficiency"] == 0.0
+
+
+def test_open_dataset(tmp_path):
+    from jaxtrace_gb300 import vtk_io as V
+    rng = np.random.default_rng(1)
+    P = rng.random((8, 3)).astype(F32)
+    for k in range(3):
+        V.write_vtu(str(tmp_path / f"s_{k}.vtu"), P, None, {"velocity": rng.random((8, 3)).astype(F32)})
+    r = jt.open_dataset(str(tmp_path / "s_*.vtu"))
+    assert len(r) == 3 and r.load_time_series()["velocity_data"].shape == (3, 8, 3)
+    r2 = jt.open_dataset([str(tmp_path / "s_2.vtu"), str(tmp_path / "s_0.vtu")])
+    assert len(r2) == 2
+    (tmp_path / "a.h5").write_bytes(b"")
+    with pytest.raises(ImportError, match="HDF5"):
+        jt.open_dataset(str(tmp_path / "a.h5"))
+    (tmp_path / "a.xyz").write_bytes(b"")
+    with pytest.raises(ValueError, match="Unknown file format"):
+        jt.open_dataset(str(tmp_path / "a.xyz"))
+    with pytest.raises(FileNotFoundError):
+        jt.open_dataset(str(tmp_path / "none_*.vtu"))
