@@ -71,8 +71,8 @@ def test_tracker_diagnostics(golden):
     g = golden("track_grid")
     f = jt.StructuredTimeSeriesField(g["D"], g["st"], g["g"], g["g"], g["g"], "periodic")
     tr = jt.create_tracker("rk4", f, jt.periodic_boundary(((0, 0, 0), (1, 1, 1))))
-    b = tr.benchmark_performance((64, 256), n_timesteps=11)
-    assert all(b["throughput"][n] > 0 for n in (64, 256)) and "scaling_exponent" in b["scalability"]
+    b = tr.benchmark_performance((64, 256, 2048), n_timesteps=11)   # the slope needs unequal size ratios
+    assert all(b["throughput"][n] > 0 for n in (64, 256, 2048)) and "scaling_exponent" in b["scalability"]
     q = np.random.default_rng(0).random((100, 3)).astype(np.float32)
     a = tr.analyze_field_sampling(q, [0.0, 0.05])
     assert a["performance"]["total_samples"] == 200 and a["field_properties"]["finite_values"] == 200
