@@ -20,8 +20,9 @@ from .seeding import random_seeds, uniform_grid_seeds
 from .tracker import (EnsembleBatch, ParticleTracker, TrackerOptions, compare_integrators, create_tracker,
                       track_particles_simple)
 from .autotune import Autotuner
-from .vtk_io import (VTKTrajectorySeries, VTKTrajectoryWriter, VTKUnstructuredTimeSeriesReader, open_dataset,
-                     open_vtk_time_series)
+from .vtk_io import (VTKTrajectorySeries, VTKTrajectoryWriter, VTKUnstructuredTimeSeriesReader,
+                     create_field_from_vtk, create_time_series_from_vtk_files, open_dataset, open_vtk_time_series)
+from .fields import TimeDependentVelocityField, TimeVaryingField
 
 __version__ = "0.1.0"
 
@@ -36,5 +37,6 @@ __all__ = [
     "open_vtk_time_series", "create_trajectory_from_positions", "create_single_particle_trajectory",
     "create_empty_trajectory", "merge_trajectories", "validate_trajectory_data", "compare_integrators",
     "analyze_trajectory_results", "KDEEstimator", "SPHDensityEstimator", "clamp_to_bounds", "reflect_boundary",
-    "open_dataset",
+    "open_dataset", "create_field_from_vtk", "create_time_series_from_vtk_files", "TimeDependentVelocityField",
+    "TimeVaryingField",
 ]

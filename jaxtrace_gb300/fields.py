@@ -902,3 +902,8 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
                 f"positions={self.positions.shape}, elements={m.connectivity.shape[0]}, "
                 f"octree_nodes={len(m.nodes)}, octree_leaves={int(m.nodes_is_leaf.sum())}, "
                 f"interpolation='{self.interpolation}', extrapolation='{self.extrapolation}')")
+
+
+# names the reference keeps for TimeSeriesField (fields/time_series.py:631-633)
+TimeDependentVelocityField = TimeSeriesField
+TimeVaryingField = TimeSeriesField

@@ -739,3 +739,54 @@ def open_dataset(path_spec, format_type: Optional[str] = None, **kwargs):
     if format_type != "vtk":
         raise ValueError(f"Unsupported format: {format_type}")
     return VTKUnstructuredTimeSeriesReader(path_spec if isinstance(path_spec, str) else files, **kwargs)
+
+
+def create_time_series_from_vtk_files(file_pattern: str, velocity_field_name: Optional[str] = "velocity",
+                                      max_time_steps: Optional[int] = None, **kwargs):
+    """TimeSeriesField over a VTK time series (fields/time_series.py:606-628);
+    a velocity name absent from the files falls back to detection."""
+    from .fields import TimeSeriesField
+    reader = VTKUnstructuredTimeSeriesReader(file_pattern, max_time_steps=max_time_steps)
+    first = read_vtk_xml(reader.time_files[0], geometry=False, names=[])
+    if velocity_field_name is not None and velocity_field_name in first["point_data"]:
+        reader.velocity_field_name = velocity_field_name
+    d = reader.load_time_series()
+    return TimeSeriesField(data=d["velocity_data"], times=d["times"], positions=d["positions"],
+                           _source_info=d.get("source_info", {}), **kwargs)
+
+
+def create_field_from_vtk(file_pattern: str, field_type: str = "auto", **kwargs):
+    """fields/__init__.py:114-207 for unstructured VTK data: several files
+    (or field_type "time_series") give a time series, one .vtu/.pvtu/.vtk
+    file a single-snapshot nearest-node field; structured image/grid files
+    (.vti/.vts/.vtr) are not read here."""
+    if os.path.isdir(file_pattern):
+        files = sorted(f for ext in ("*.vtu", "*.pvtu", "*.vtk", "*.vti", "*.vts", "*.vtr")
+                       for f in glob.glob(os.path.join(file_pattern, ext)))
+        pattern = os.path.join(file_pattern, "*.pvtu" if any(f.endswith(".pvtu") for f in files) else "*.vtu")
+    else:
+        files = sorted(glob.glob(os.path.expanduser(file_pattern)))
+        pattern = file_pattern
+    if not files:
+        raise FileNotFoundError(f"No VTK files found: {file_pattern}")
+    if field_type == "auto":
+        if len(files) > 1:
+            field_type = "time_series"
+        elif files[0].lower().endswith((".vti", ".vts", ".vtr")):
+            field_type = "structured"
+        else:
+            field_type = "unstructured"
+    if field_type == "time_series":
+        return create_time_series_from_vtk_files(pattern, **kwargs)
+    if field_type == "structured":
+        raise NotImplementedError("structured VTK files (.vti/.vts/.vtr) are not read; use "
+                                  "StructuredTimeSeriesField with the grid arrays")
+    if field_type == "unstructured":
+        from .fields import TimeSeriesField
+        d = read_vtk_xml(files[0])
+        name = next((n for n in VELOCITY_NAMES if n in d["point_data"]), None)
+        if name is None:
+            raise ValueError(f"{files[0]}: no velocity array among {list(d['point_data'])}")
+        v = _velocity3(np.asarray(d["point_data"][name]))
+        return TimeSeriesField(data=v[None], times=np.zeros(1, F32), positions=d["points"], **kwargs)
+    raise ValueError(f"Unknown field type: {field_type}")

@@ -183,3 +183,27 @@ def test_legacy_vtk_skips_metadata_blocks(tmp_path):
     d = V.read_vtk_xml(str(f))
     assert np.array_equal(d["point_data"]["U"], np.array([[1, 2, 3], [4, 5, 6]], F32))
     assert np.array_equal(d["cells"]["offsets"], [1]) and np.array_equal(d["cells"]["types"], [1])
+
+
+def test_fields_from_vtk_files(tmp_path):
+    """create_field_from_vtk / create_time_series_from_vtk_files
+    (fields/__init__.py:114-207, fields/time_series.py:606-628)."""
+    import jaxtrace_gb300 as jt
+    rng = np.random.default_rng(4)
+    P = rng.random((20, 3)).astype(F32)
+    U = rng.normal(size=(3, 20, 3)).astype(F32)
+    for k in range(3):
+        V.write_vtu(str(tmp_path / f"flow_{k}.vtu"), P, None, {"velocity": U[k]})
+    f = jt.create_field_from_vtk(str(tmp_path / "flow_*.vtu"))
+    assert isinstance(f, jt.TimeSeriesField) and np.array_equal(f.data, U)
+    assert np.array_equal(f.times, np.arange(3, dtype=F32)) and np.array_equal(f.positions, P)
+    d = jt.create_field_from_vtk(str(tmp_path))
+    assert np.array_equal(d.data, U)
+    one = jt.create_field_from_vtk(str(tmp_path / "flow_1.vtu"))
+    assert one.data.shape == (1, 20, 3) and np.array_equal(one.data[0], U[1])
+    g = jt.create_time_series_from_vtk_files(str(tmp_path / "flow_*.vtu"), velocity_field_name="U",
+                                             max_time_steps=2)
+    assert np.array_equal(g.data, U[1:])
+    assert jt.TimeVaryingField is jt.TimeSeriesField
+    with pytest.raises(FileNotFoundError):
+        jt.create_field_from_vtk(str(tmp_path / "nothing_*.vtu"))
