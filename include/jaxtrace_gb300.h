@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JT_ABI_VERSION 1
+#define JT_ABI_VERSION 2
 
 /* ---- return codes ------------------------------------------------------ */
 #define JT_OK 0
@@ -59,6 +59,30 @@ extern "C" {
 #define JT_STORE_STAGE_F32 3 /* float32 {x,y,z,0} per node (16 B)               */
 #define JT_STORE_STAGE_F16 4 /* float16 yz-quads per node (32 B); entry.wa holds
                                 the field's power-of-two scale                 */
+/* Affine-tile snapshots of a regular grid (input of jt_stage_tile_fields).
+ * The grid's cells are cut into tiles of JT_TILE^3 cells; tile (tx,ty,tz)
+ * covers cells [JT_TILE*t, JT_TILE*t + JT_TILE) per axis and its
+ * (JT_TILE+1)^3 nodes.  Local node l (0..JT_TILE) of axis a is grid node
+ * min(JT_TILE*t + l, n-1) (clamp, zero, nan) or (JT_TILE*t + l) mod n
+ * (periodic), at continuous index coordinate min(JT_TILE*t + l, n-1) or
+ * JT_TILE*t + l.  Per snapshot and tile a float32 affine base
+ * b(f) = o + Gx*fx + Gy*fy + Gz*fz in the continuous index coordinates f is
+ * stored (jt_tile_base layout below), and every tile node holds the 16-bit
+ * residual v - b at its coordinate: 4 halves {x, y, z, 0} (8 B), nodes in
+ * order (lx*(JT_TILE+1) + ly)*(JT_TILE+1) + lz. */
+#define JT_STORE_TILE_BF16 5 /* bfloat16 residuals                            */
+#define JT_STORE_TILE_F16 6  /* float16 residuals                             */
+/* Pre-blended affine-tile stage field (tracking only): per slot and tile the
+ * blended float32 base, and (JT_TILE+1)*JT_TILE*JT_TILE float16 residual
+ * yz-quads of 32 B: quad (lx*JT_TILE + ly)*JT_TILE + lz holds local nodes
+ * (lx,ly,lz), (lx,ly,lz+1), (lx,ly+1,lz), (lx,ly+1,lz+1); words 0-3 their
+ * (x,y) half pairs, words 4-5 their z in pairs, words 6-7 zero. */
+#define JT_STORE_STAGE_TILE 7
+#define JT_TILE 4
+#define JT_TILE_NODES 125 /* (JT_TILE+1)^3 residual nodes per snapshot tile   */
+#define JT_TILE_QUADS 80  /* (JT_TILE+1)*JT_TILE^2 residual quads per stage tile */
+/* Tile base record, 16 floats: {ox, oy, Gx.x, Gx.y, Gy.x, Gy.y, Gz.x, Gz.y,
+ * oz, Gx.z, Gy.z, Gz.z, 0, 0, 0, 0} (x,y parts in one aligned 32 B half). */
 
 /* grid sampler bounds handling: fields/structured.py:89 */
 #define JT_GRID_CLAMP 0
@@ -141,6 +165,19 @@ typedef struct {
     int32_t n_pairs;       /* number of snapshot pairs (>= 1)                  */
     int64_t pair_stride;   /* records per pair (= nx*ny*nz)                    */
     const void* pairs;     /* device                                          */
+    /* affine-tile storages (JT_STORE_TILE_*, JT_STORE_STAGE_TILE) only:
+     *   TILE_*      pairs: residual nodes of n_pairs+1 snapshots, pair_stride
+     *               = tiles*JT_TILE_NODES records (8 B) per snapshot;
+     *               tile_base: (n_pairs+1) x tiles base records
+     *   STAGE_TILE  pairs: residual quads of n_pairs slots, pair_stride =
+     *               tiles*JT_TILE_QUADS quads (32 B) per slot;
+     *               tile_base: n_pairs x tiles base records
+     * where tiles = tiles[0]*tiles[1]*tiles[2], tiles[a] = (n_a + JT_TILE - 1)
+     * / JT_TILE, tile (tx,ty,tz) at (tx*tiles[1] + ty)*tiles[2] + tz.  Unused
+     * (NULL, 0) by the other storages. */
+    const float* tile_base; /* device                                         */
+    int32_t tiles[3];
+    int32_t pad_tiles;
 } jt_grid_field;
 
 /* Tetrahedral mesh field with the octree point location of
@@ -351,6 +388,17 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
 int jt_stage_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
                     int32_t out_storage, void* out, void* stream);
 
+/* The same for affine-tile snapshots (JT_STORE_TILE_BF16 / _F16): blends the
+ * tile bases and the residuals of each entry's pair (the blend is linear, so
+ * the blended field is the blended base plus the blended residual) into n
+ * JT_STORE_STAGE_TILE slots: out_quads + j * tiles * JT_TILE_QUADS * 32 B and
+ * out_base + j * tiles * 16 floats, both device.  The entries carry plain
+ * blend weights (sa = sb = 1).  The tracking launch then takes a
+ * jt_grid_field with storage = JT_STORE_STAGE_TILE, pairs = out_quads,
+ * tile_base = out_base, n_pairs = n, pair_stride = tiles * JT_TILE_QUADS. */
+int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, int32_t n, void* out_quads,
+                         float* out_base, void* stream);
+
 /* ---- adjoint ------------------------------------------------------------- */
 /* No reference counterpart: JAXTrace has no gradients (no jax.grad on this
  * path).  Reverse-mode RK4 for loss gradients with respect to the initial
@@ -429,7 +477,10 @@ int jt_cell_sort(const jt_sort_grid* g, int32_t n, const float* pos_in, const fl
  *           held on every GPU that loads the library until the process exits.
  *   set-up: the first call on a device looks up the array's device address
  *           (cudaGetSymbolAddress) with that device current; make that first
- *           call before any stream capture.
+ *           call before any stream capture.  A device reset (cudaDeviceReset)
+ *           ends the context the address belongs to: the next call notices
+ *           the new context and looks the address up again, so the first
+ *           call after a reset must also come before any stream capture.
  *   sharing: every call uses the same array, which keeps the last call's
  *           contents (the call clears what it accumulates into); calls whose
  *           work overlaps on the GPU race -- serialise them on one stream.

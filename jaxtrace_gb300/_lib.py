@@ -16,10 +16,13 @@ from . import _build
 i32, i64, f32, vp = C.c_int32, C.c_int64, C.c_float, C.c_void_p
 
 # ---- constants (mirror of the header) ------------------------------------
+ABI_VERSION = 2
 JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STATUS = 0, -1, -2, -3, -4, -5
 JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
 JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2
 JT_STORE_STAGE_F32, JT_STORE_STAGE_F16 = 3, 4
+JT_STORE_TILE_BF16, JT_STORE_TILE_F16, JT_STORE_STAGE_TILE = 5, 6, 7
+JT_TILE, JT_TILE_NODES, JT_TILE_QUADS = 4, 125, 80
 JT_GRID_CLAMP, JT_GRID_ZERO, JT_GRID_NAN, JT_GRID_PERIODIC = 0, 1, 2, 3
 JT_BLEND_WEIGHTED, JT_BLEND_LERP_FWD, JT_BLEND_LERP_BWD, JT_BLEND_SAME_A, JT_BLEND_SAME_B = 0, 1, 2, 3, 4
 JT_EULER, JT_RK2, JT_RK4 = 0, 1, 2
@@ -45,7 +48,8 @@ BLEND_DTYPE = np.dtype([("pair", "<i4"), ("form", "<i4"), ("wa", "<f4"), ("wb", 
 class GridField(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("bounds_mode", i32),
                 ("origin", f32 * 3), ("spacing", f32 * 3), ("inv_spacing", f32 * 3), ("valid_hi", f32 * 3),
-                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64), ("pairs", vp)]
+                ("storage", i32), ("n_pairs", i32), ("pair_stride", i64), ("pairs", vp),
+                ("tile_base", vp), ("tiles", i32 * 3), ("pad_tiles", i32)]
 
 
 class OctreeNode(C.Structure):
@@ -195,12 +199,13 @@ def load(build_if_missing: bool = True):
         "jt_adjoint_rk4": (i32, [P(Field), P(Boundary), P(AdjointParams), vp]),
         "jt_adjoint_workspace_bytes": (C.c_size_t, [i64, i32]),
         "jt_stage_fields": (i32, [P(Field), vp, vp, i32, i32, vp, vp]),
+        "jt_stage_tile_fields": (i32, [P(Field), vp, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.jt_abi_version() != 1:
+    if lib.jt_abi_version() != ABI_VERSION:
         raise ImportError("jaxtrace_gb300 native library ABI mismatch")
     _lib = lib
     return lib

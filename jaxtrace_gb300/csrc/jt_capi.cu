@@ -66,6 +66,16 @@ int check_grid_shape(const jt_grid_field& g) {
     return JT_OK;
 }
 
+int check_tiles(const jt_grid_field& g) {
+    const int32_t n[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a)
+        if (g.tiles[a] != (n[a] + JT_TILE - 1) / JT_TILE)
+            return set_error(JT_ERR_INVALID, "tiles[%d] = %d, expected (n + %d) / %d = %d", a, g.tiles[a], JT_TILE - 1,
+                             JT_TILE, (n[a] + JT_TILE - 1) / JT_TILE);
+    if (g.tile_base == nullptr) return set_error(JT_ERR_INVALID, "affine-tile field without tile_base");
+    return JT_OK;
+}
+
 static int check_field(const jt_field* f) {
     if (f == nullptr) return set_error(JT_ERR_INVALID, "field is NULL");
     switch (f->kind) {
@@ -76,6 +86,14 @@ static int check_field(const jt_field* f) {
             if (g->bounds_mode < JT_GRID_CLAMP || g->bounds_mode > JT_GRID_PERIODIC)
                 return set_error(JT_ERR_INVALID, "unknown bounds_mode %d", g->bounds_mode);
             if (g->n_pairs < 1 || g->pairs == nullptr) return set_error(JT_ERR_INVALID, "grid field has no snapshot pairs");
+            if (g->storage == JT_STORE_STAGE_TILE) {
+                if (int rc = check_tiles(*g)) return rc;
+                if (g->pair_stride != (int64_t)g->tiles[0] * g->tiles[1] * g->tiles[2] * JT_TILE_QUADS)
+                    return set_error(JT_ERR_INVALID, "pair_stride must be tiles * JT_TILE_QUADS");
+                return JT_OK;
+            }
+            if (g->storage == JT_STORE_TILE_BF16 || g->storage == JT_STORE_TILE_F16)
+                return set_error(JT_ERR_UNSUPPORTED, "affine-tile snapshots are read by jt_stage_tile_fields only");
             if (g->pair_stride < (int64_t)g->nx * g->ny * g->nz)
                 return set_error(JT_ERR_INVALID, "pair_stride smaller than the node count");
             if (g->storage == JT_STORE_STAGE_F32 || g->storage == JT_STORE_STAGE_F16) return JT_OK;

@@ -99,6 +99,100 @@ __global__ void __launch_bounds__(kStageBlock16, 16) k_stage_f16(jt_grid_field F
     }
 }
 
+// ---------------------------------------------------------------------------
+// Affine-tile stage fields.  One thread per residual quad of a tile (80 per
+// tile: local x plane 0..4, y and z cell 0..3) walks the chunk's entries; a
+// quad's four nodes of snapshots A and B are reloaded only when the pair
+// changes.  The blend is linear, so the stage residual is the blend of the
+// snapshot residuals and the stage base the blend of the snapshot bases; the
+// first thread of each tile blends its base record.  Blocks of 64 threads so
+// that the side-stream launch fits beside the tracking blocks.
+// ---------------------------------------------------------------------------
+
+// Residual node {x, y, z, 0} of 16-bit storage STORE, decoded to float32.
+template <int STORE>
+__device__ __forceinline__ void tile_node(const uint2* __restrict__ r, float2& xy, float& z) {
+    const uint2 w = __ldg(r);
+    if (STORE == JT_STORE_TILE_BF16) {
+        xy = make_float2(bf16_lo(w.x), bf16_hi(w.x));
+        z = bf16_lo(w.y);
+    } else {
+        xy = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
+        z = __low2float(*reinterpret_cast<const __half2*>(&w.y));
+    }
+}
+
+template <int STORE>
+__global__ void __launch_bounds__(kStageBlock16, 16) k_stage_tile(jt_grid_field F, const jt_blend* __restrict__ ent,
+                                                                int n, uint4* __restrict__ out_q,
+                                                                float* __restrict__ out_b) {
+    const int64_t tiles = (int64_t)F.tiles[0] * F.tiles[1] * F.tiles[2];
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t Q = tiles * JT_TILE_QUADS;
+    if (q >= Q) return;
+    const int64_t tile = q / JT_TILE_QUADS;
+    const int lq = (int)(q - tile * JT_TILE_QUADS);
+    const int lx = lq >> 4, ly = (lq >> 2) & 3, lz = lq & 3;
+    // local nodes (lx,ly,lz), (lx,ly,lz+1), (lx,ly+1,lz), (lx,ly+1,lz+1)
+    const int l0 = (lx * (JT_TILE + 1) + ly) * (JT_TILE + 1) + lz;
+    const int lofs[4] = {l0, l0 + 1, l0 + (JT_TILE + 1), l0 + (JT_TILE + 1) + 1};
+    const bool head = lq == 0;
+    const uint2* res = reinterpret_cast<const uint2*>(F.pairs);
+    int cur = -1;
+    PairVal pv[4];
+    PairVal pb[4];  // the tile base's four triples (o, Gx, Gy, Gz) of A and B
+    for (int j = 0; j < n; ++j) {
+        const jt_blend e = ent[j];
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        if (pr != cur) {
+            const uint2* ra = res + ((int64_t)pr * tiles + tile) * JT_TILE_NODES;
+            const uint2* rb = ra + tiles * JT_TILE_NODES;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                tile_node<STORE>(ra + lofs[c], pv[c].axy, pv[c].az);
+                tile_node<STORE>(rb + lofs[c], pv[c].bxy, pv[c].bz);
+            }
+            if (head) {
+                const float* ba = F.tile_base + ((int64_t)pr * tiles + tile) * 16;
+                const float* bb = ba + tiles * 16;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    pb[c].axy = make_float2(__ldg(ba + 2 * c), __ldg(ba + 2 * c + 1));
+                    pb[c].az = __ldg(ba + 8 + c);
+                    pb[c].bxy = make_float2(__ldg(bb + 2 * c), __ldg(bb + 2 * c + 1));
+                    pb[c].bz = __ldg(bb + 8 + c);
+                }
+            }
+            cur = pr;
+        }
+        V3 v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = blend<false, JT_STORE_F32>(pv[c], e);
+        uint4 a, b;
+        a.x = pack_h2(v[0].x, v[0].y);
+        a.y = pack_h2(v[1].x, v[1].y);
+        a.z = pack_h2(v[2].x, v[2].y);
+        a.w = pack_h2(v[3].x, v[3].y);
+        b.x = pack_h2(v[0].z, v[1].z);
+        b.y = pack_h2(v[2].z, v[3].z);
+        b.z = 0u;
+        b.w = 0u;
+        uint4* o = out_q + 2 * ((int64_t)j * Q + q);
+        o[0] = a;
+        o[1] = b;
+        if (head) {
+            float4* ob = reinterpret_cast<float4*>(out_b + ((int64_t)j * tiles + tile) * 16);
+            V3 t[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) t[c] = blend<false, JT_STORE_F32>(pb[c], e);
+            ob[0] = make_float4(t[0].x, t[0].y, t[1].x, t[1].y);
+            ob[1] = make_float4(t[2].x, t[2].y, t[3].x, t[3].y);
+            ob[2] = make_float4(t[0].z, t[1].z, t[2].z, t[3].z);
+            ob[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
 // The bounds mode as a template argument: clamp and periodic get their own
 // kernels, zero and nan share the run-time one.
 template <bool E, int O>
@@ -107,6 +201,18 @@ template <bool E, int O>
 using StagePeriodic = StageGridField<E, O, JT_GRID_PERIODIC>;
 template <bool E, int O>
 using StageAnyMode = StageGridField<E, O, -1>;
+
+template <int MODE>
+static cudaError_t tile_launch(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p,
+                               cudaStream_t s) {
+    const StageTileField<MODE, true> fld = StageTileField<MODE, true>::create(f, 0);
+    const int bs = p.block_size > 0 ? p.block_size : kBlock;
+    const unsigned g = (unsigned)((p.n_particles + bs - 1) / bs);
+    const InletFrame I = inlet_frame(b);
+    typedef Launcher<GridField, jt_grid_field, int> L;
+    if (p.path != nullptr) return L::template launch_track<false, true>(fld, b, I, p, g, bs, s);
+    return L::template launch_track<false, false>(fld, b, I, p, g, bs, s);
+}
 
 template <template <bool, int> class FT>
 static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p,
@@ -120,6 +226,16 @@ static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, co
 
 int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
     const bool exact = p.arith == JT_ARITH_EXACT;
+    if (f.storage == JT_STORE_STAGE_TILE) {
+        if (exact) return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
+        cudaError_t err;
+        switch (f.bounds_mode) {
+            case JT_GRID_CLAMP: err = tile_launch<JT_GRID_CLAMP>(f, b, p, s); break;
+            case JT_GRID_PERIODIC: err = tile_launch<JT_GRID_PERIODIC>(f, b, p, s); break;
+            default: err = tile_launch<-1>(f, b, p, s); break;
+        }
+        return cuda_status(err, "tracking kernel launch");
+    }
     if (f.storage != JT_STORE_STAGE_F32 && exact)
         return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
     cudaError_t err;
@@ -167,5 +283,34 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     } else {
         return set_error(JT_ERR_INVALID, "out_storage must be JT_STORE_STAGE_F32 or JT_STORE_STAGE_F16");
     }
+    return cuda_status(cudaGetLastError(), "stage field launch");
+}
+
+extern "C" int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, int32_t n, void* out_quads,
+                                    float* out_base, void* stream) {
+    if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
+        return set_error(JT_ERR_INVALID, "stage fields need a regular-grid field");
+    const jt_grid_field& F = *field->grid;
+    if (int rc = check_grid_shape(F)) return rc;
+    if (F.storage != JT_STORE_TILE_BF16 && F.storage != JT_STORE_TILE_F16)
+        return set_error(JT_ERR_INVALID, "affine-tile stage fields come from JT_STORE_TILE_* snapshots");
+    if (int rc = check_tiles(F)) return rc;
+    if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
+    if (n == 0) return JT_OK;
+    if (entries == nullptr || out_quads == nullptr || out_base == nullptr)
+        return set_error(JT_ERR_INVALID, "entries, out_quads and out_base are required");
+    if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshots");
+    const int64_t tiles = (int64_t)F.tiles[0] * F.tiles[1] * F.tiles[2];
+    if (F.pair_stride != tiles * JT_TILE_NODES)
+        return set_error(JT_ERR_INVALID, "pair_stride must be tiles * JT_TILE_NODES");
+    const int64_t Q = tiles * JT_TILE_QUADS;
+    const unsigned g = (unsigned)((Q + kStageBlock16 - 1) / kStageBlock16);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (F.storage == JT_STORE_TILE_BF16)
+        k_stage_tile<JT_STORE_TILE_BF16><<<g, kStageBlock16, 0, s>>>(F, entries, n, reinterpret_cast<uint4*>(out_quads),
+                                                                      out_base);
+    else
+        k_stage_tile<JT_STORE_TILE_F16><<<g, kStageBlock16, 0, s>>>(F, entries, n, reinterpret_cast<uint4*>(out_quads),
+                                                                     out_base);
     return cuda_status(cudaGetLastError(), "stage field launch");
 }

@@ -15,6 +15,8 @@ int cuda_status(cudaError_t e, const char* what);
 // index is exact in float32, so a clipped coordinate floors to a valid cell)
 // and fewer than 2^31 nodes (32-bit node offsets within a snapshot).
 int check_grid_shape(const jt_grid_field& g);
+// tiles[] of an affine-tile storage against the grid shape, and its base array
+int check_tiles(const jt_grid_field& g);
 
 // Exclusive scan of n uint32 values in place (n <= scan_capacity()); sums
 // holds scan_partials(n) values, sums2 one.

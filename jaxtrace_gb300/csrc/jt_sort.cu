@@ -219,21 +219,59 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
 static void* g_noalloc_addr[kMaxDevices];
+static unsigned long long g_noalloc_ctx[kMaxDevices];  // context id the address belongs to
 static std::mutex g_noalloc_mu;
 
-// Device address of the scratch on the current device, looked up once per
-// device (with that device current) and cached.
+// The driver's context queries, fetched through the runtime (the library
+// does not link the driver library itself).
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+static CtxGetCurrentFn g_ctx_current = nullptr;
+static CtxGetIdFn g_ctx_id = nullptr;
+static std::once_flag g_ctx_once;
+
+// Process-unique id of the calling thread's current context, 0 when there is
+// none yet or the driver does not answer.  A device reset destroys the
+// context; the next one gets a new id, and the scratch's module a possibly
+// different address.
+unsigned long long current_ctx_id() {
+    std::call_once(g_ctx_once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (g_ctx_current == nullptr || g_ctx_id == nullptr) return 0;
+    void* ctx = nullptr;
+    if (g_ctx_current(&ctx) != 0 || ctx == nullptr) return 0;
+    unsigned long long id = 0;
+    return g_ctx_id(ctx, &id) == 0 ? id : 0;
+}
+
+// Device address of the scratch on the current device, looked up with that
+// device current and cached per device together with the id of the context
+// it was looked up in: a call in another context (after a device reset) looks
+// it up again.  Without a context id (no context yet, or a driver without
+// the query) the lookup runs on every call.
 int noalloc_scratch(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return jt::cuda_status(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return jt::set_error(JT_ERR_UNSUPPORTED, "device ordinal %d >= %d", dev, kMaxDevices);
+    unsigned long long ctx = current_ctx_id();
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (g_noalloc_addr[dev] == nullptr) {
+    if (g_noalloc_addr[dev] == nullptr || ctx == 0 || g_noalloc_ctx[dev] != ctx) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the device's context current if none was
         if (e != cudaSuccess) return jt::cuda_status(e, "cudaGetSymbolAddress of the no-alloc sort scratch");
+        if (ctx == 0) ctx = current_ctx_id();
         g_noalloc_addr[dev] = p;
+        g_noalloc_ctx[dev] = ctx;
     }
     *out = g_noalloc_addr[dev];
     return JT_OK;

@@ -55,15 +55,28 @@ def shard_ensembles(sizes: Sequence[int], world: int) -> List[List[int]]:
     return [sorted(v) for v in out]
 
 
+def collective_device():
+    """Where the process group's collectives take their tensors: this rank's
+    current CUDA device under NCCL (which rejects host tensors), the host
+    under gloo."""
+    import torch
+    dist = _dist()
+    if dist.is_available() and dist.is_initialized() and str(dist.get_backend()).lower() == "nccl":
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device("cpu")
+
+
 def gather_rows(local, n_total: int, to_all: bool = False):
     """Concatenate every rank's (n_r, k) rows in rank order (the layout
     ``shard_bounds`` produced) on rank 0, or on every rank with ``to_all``.
-    Other ranks get None unless ``to_all``."""
+    Other ranks get None unless ``to_all``.  The rows travel on the process
+    group's device (``collective_device``) and come back there."""
     import torch
     dist = _dist()
     world, rank = world_and_rank()
     if world == 1:
         return local
+    local = torch.as_tensor(local).to(collective_device())
     counts = [shard_bounds(n_total, r, world) for r in range(world)]
     width = max(hi - lo for lo, hi in counts)
     pad = torch.zeros((width,) + tuple(local.shape[1:]), dtype=local.dtype, device=local.device)
@@ -82,9 +95,9 @@ def allreduce_sum(t):
     world, _ = world_and_rank()
     if world == 1:
         return t
-    acc = t.to(torch.float64)
+    acc = t.to(device=collective_device(), dtype=torch.float64)
     dist.all_reduce(acc, op=dist.ReduceOp.SUM)
-    t.copy_(acc.to(t.dtype))
+    t.copy_(acc.to(device=t.device, dtype=t.dtype))
     return t
 
 
@@ -98,7 +111,8 @@ def track_sharded(run: Callable, x0: np.ndarray, to_all: bool = False):
     lo, hi = shard_bounds(len(x0), rank, world)
     local = torch.as_tensor(np.ascontiguousarray(run(x0[lo:hi])))
     out = gather_rows(local, len(x0), to_all=to_all)
-    return None if out is None else out.numpy() if out.device.type == "cpu" else out
+    return None if out is None else out.cpu().numpy()
 
 
-__all__ = ["world_and_rank", "shard_bounds", "shard_ensembles", "gather_rows", "allreduce_sum", "track_sharded"]
+__all__ = ["world_and_rank", "shard_bounds", "shard_ensembles", "collective_device", "gather_rows", "allreduce_sum",
+           "track_sharded"]

@@ -143,6 +143,85 @@ def build_pairs_device(data: np.ndarray, storage: int, device="cuda", quad: tupl
     return buf, scales
 
 
+def tile_axis_maps(n: int, periodic: bool):
+    """Grid node and continuous index coordinate of every tile's local nodes
+    along one axis of n nodes: two (tiles, JT_TILE + 1) arrays.  Local node l
+    of tile t is grid node JT_TILE*t + l, clipped to n - 1 (the sampler's
+    clamp, zero and nan modes) or wrapped mod n (periodic, where the
+    coordinate keeps counting past n so that the tile stays one affine piece)."""
+    T = (n + L.JT_TILE - 1) // L.JT_TILE
+    loc = L.JT_TILE * np.arange(T)[:, None] + np.arange(L.JT_TILE + 1)[None, :]
+    if periodic:
+        return loc % max(n, 1), loc.astype(np.float64)
+    c = np.minimum(loc, max(n - 1, 0))
+    return c, c.astype(np.float64)
+
+
+def build_tile_snapshots(data: np.ndarray, dims, periodic: bool, storage: int, device="cuda"):
+    """Affine-tile snapshots (JT_STORE_TILE_BF16 / _F16) of (T, nx*ny*nz, 3)
+    float32 data on a regular grid.
+
+    Each tile of JT_TILE^3 cells gets, per snapshot and component, the least-
+    squares affine function b(f) = o + Gx fx + Gy fy + Gz fz of the continuous
+    index coordinates over its (JT_TILE+1)^3 nodes (a tensor-product design,
+    so the centred columns are orthogonal and the fit is three projections),
+    rounded to float32; each node then stores the 16-bit rounding of the
+    residual v - b(f_node), computed in float64 from the float32 coefficients.
+    Returns (residuals (S, tiles, JT_TILE_NODES, 4) 16-bit with {x, y, z, 0}
+    per node, bases (S, tiles, 16) float32 records) for S = max(T, 2)
+    snapshots (a single snapshot is stored twice, the pair it forms with
+    itself).  ``device`` is where the arithmetic runs (CUDA for a field;
+    the host suite checks the encoding on the CPU)."""
+    import torch
+    if str(device).startswith("cuda"):
+        _torch_cuda()
+    T = data.shape[0]
+    nx, ny, nz = (int(v) for v in dims)
+    maps = [tile_axis_maps(n, periodic) for n in (nx, ny, nz)]
+    TX, TY, TZ = (m[0].shape[0] for m in maps)
+    tiles = TX * TY * TZ
+    K = L.JT_TILE + 1
+    S = max(T, 2)
+    dt16 = torch.bfloat16 if storage in (L.JT_STORE_BF16, L.JT_STORE_TILE_BF16) else torch.float16
+    res = torch.zeros((S, tiles, K ** 3, 4), dtype=dt16, device=device)
+    base = torch.zeros((S, tiles, 16), dtype=torch.float32, device=device)
+    t64 = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device)  # noqa: E731
+    IX, IY, IZ = (torch.as_tensor(m[0], dtype=torch.int64, device=device) for m in maps)
+    node = ((IX[:, None, None, :, None, None] * ny + IY[None, :, None, None, :, None]) * nz
+            + IZ[None, None, :, None, None, :])                                   # (TX,TY,TZ,K,K,K)
+    CX, CY, CZ = (t64(m[1]) for m in maps)                                        # (T_a, K)
+    means = [c.mean(dim=1) for c in (CX, CY, CZ)]
+    dev = [c - m[:, None] for c, m in zip((CX, CY, CZ), means)]
+    # sum over the tile's K^3 nodes of the centred coordinate squared
+    ss = [K * K * (d * d).sum(dim=1) for d in dev]
+    shape = [(TX, 1, 1, K, 1, 1), (1, TY, 1, 1, K, 1), (1, 1, TZ, 1, 1, K)]
+    tshape = [(TX, 1, 1), (1, TY, 1), (1, 1, TZ)]
+    for t in range(S):
+        V = torch.from_numpy(np.ascontiguousarray(data[min(t, T - 1)])).to(device=device, dtype=torch.float64)
+        Vt = V[node]                                                               # (TX,TY,TZ,K,K,K,3)
+        o = Vt.mean(dim=(3, 4, 5))                                                 # (TX,TY,TZ,3)
+        G = []
+        for a in range(3):
+            num = (Vt * dev[a].reshape(shape[a] + (1,))).sum(dim=(3, 4, 5))
+            den = ss[a].reshape(tshape[a] + (1,))
+            G.append(torch.where(den > 0, num / torch.where(den > 0, den, 1.0), 0.0))
+        off = o - sum(G[a] * means[a].reshape(tshape[a] + (1,)) for a in range(3))
+        off32 = off.float().double()
+        G32 = [g.float().double() for g in G]
+        b = off32[:, :, :, None, None, None, :] + sum(
+            G32[a][:, :, :, None, None, None, :] * (CX, CY, CZ)[a].reshape(shape[a] + (1,)) for a in range(3))
+        r = (Vt - b).reshape(tiles, K ** 3, 3)
+        res[t, :, :, :3] = r.float().to(dt16)
+        rec = base[t]
+        off32f, Gf = off32.reshape(tiles, 3).float(), [g.reshape(tiles, 3).float() for g in G32]
+        rec[:, 0], rec[:, 1] = off32f[:, 0], off32f[:, 1]
+        for a in range(3):
+            rec[:, 2 + 2 * a], rec[:, 3 + 2 * a] = Gf[a][:, 0], Gf[a][:, 1]
+            rec[:, 9 + a] = Gf[a][:, 2]
+        rec[:, 8] = off32f[:, 2]
+    return res, base, (TX, TY, TZ)
+
+
 class _DeviceField:
     """Shared plumbing: snapshot times, blend semantics and the jt_field struct."""
 
@@ -172,6 +251,9 @@ class _DeviceField:
                     extrapolation=self.extrapolation, scales=self._scales_or_none())
 
     def _scales_or_none(self):
+        if getattr(self, "encoding", "snapshot") == "tile":
+            # affine tiles are unscaled; their gathering pairs are float32
+            return None
         self._device()
         return None if self._storage == L.JT_STORE_F32 else self._scales
 
@@ -204,10 +286,13 @@ class _DeviceField:
         self._device()
         return self._cfield
 
-    def sample_at_positions(self, query_positions, t):
+    def sample_at_positions(self, query_positions, t, *, arith=None):
         """Velocities at (M,3) positions and time t (fields/base.py:106-122).
 
         Accepts numpy (returns numpy) or CUDA torch tensors (returns a tensor).
+        ``arith`` (JT_ARITH_*): the arithmetic of a tracker that records
+        velocities, so that its row 0 matches the rows its kernel records;
+        the field's own default otherwise.
         """
         torch = _torch_cuda()
         self._device()
@@ -225,7 +310,8 @@ class _DeviceField:
         e = self.blend_at(t)
         blend = L.Blend.from_buffer_copy(e.tobytes())
         status = torch.zeros(1, dtype=torch.int32, device="cuda")
-        L.check(L.load().jt_field_sample(C.byref(self._cfield), C.byref(blend), self._default_arith(),
+        L.check(L.load().jt_field_sample(C.byref(self._cfield), C.byref(blend),
+                                         self._default_arith() if arith is None else int(arith),
                                          L.ptr(q), L.ptr(out), q.shape[0], L.ptr(status), L.stream_ptr()))
         return out if is_tensor else out.cpu().numpy()
 
@@ -298,7 +384,7 @@ class StructuredTimeSeriesField(_DeviceField):
 
     def __init__(self, data, times, grid_x, grid_y, grid_z, bounds_handling: str = "clamp",
                  interpolation: str = "linear", extrapolation: str = "constant", *,
-                 storage: str = "f32", time_semantics: str = "numpy"):
+                 storage: str = "f32", time_semantics: str = "numpy", encoding: str = "snapshot"):
         gx, gy, gz = _as_f32(grid_x), _as_f32(grid_y), _as_f32(grid_z)
         if gx.ndim != 1 or gy.ndim != 1 or gz.ndim != 1:
             raise ValueError("grid axes must be 1-D")
@@ -331,6 +417,18 @@ class StructuredTimeSeriesField(_DeviceField):
         self.y_min, self.y_max = float(gy[0]), float(gy[-1])
         self.z_min, self.z_max = float(gz[0]), float(gz[-1])
         self._mode = codes[mode]
+        # 16-bit encodings of the snapshots: "snapshot" -- every value over a
+        # per-snapshot power-of-two scale, read by every path; "tile" -- per
+        # tile of JT_TILE^3 cells a float32 affine base and 16-bit residuals,
+        # read by the pre-blended stage fields of track_particles (the other
+        # paths, which gather snapshot pairs, read float32 pairs then)
+        enc = str(encoding).lower()
+        if enc not in ("snapshot", "tile"):
+            raise ValueError(f"encoding must be 'snapshot' or 'tile', got {encoding!r}")
+        if enc == "tile" and self._storage == L.JT_STORE_F32:
+            raise ValueError("the tile encoding is a 16-bit storage (storage='bf16' or 'f16')")
+        self.encoding = enc
+        self._tiles = None
 
     def _successors(self):
         """Node indices of (i, j, k1) and (i, j1, k) for every node (i, j, k),
@@ -347,15 +445,11 @@ class StructuredTimeSeriesField(_DeviceField):
         ys = (i * ny + nxt(ny)[j]) * nz + k
         return zs.reshape(-1).astype(np.int64), ys.reshape(-1).astype(np.int64)
 
-    def _device(self):
-        if self._dev is not None:
-            return
-        pairs, scales = build_pairs_device(self.data, self._storage, quad=self._successors())
-        self._scales = scales
-        P = max(self.data.shape[0] - 1, 1)
-        # node n's own six values sit in slots 0-5 of both record layouts
-        view = pairs if self._storage == L.JT_STORE_F32 else pairs[: P * self.N * 16].view(P, self.N, 16)
-        self._dev = {"pairs": view, "buffer": pairs}
+    def _pair_storage(self) -> int:
+        """Storage of the snapshot pairs the gathering paths read."""
+        return L.JT_STORE_F32 if self.encoding == "tile" else self._storage
+
+    def _grid_desc(self) -> "L.GridField":
         g = L.GridField()
         g.nx, g.ny, g.nz = self.Nx, self.Ny, self.Nz
         g.bounds_mode = self._mode
@@ -365,7 +459,40 @@ class StructuredTimeSeriesField(_DeviceField):
         # structured.py:299-301: x <= x_min + (Nx-1)*dx, the Python float rounded to float32
         g.valid_hi[:] = [F32(self.x_min + (self.Nx - 1) * self.dx), F32(self.y_min + (self.Ny - 1) * self.dy),
                          F32(self.z_min + (self.Nz - 1) * self.dz)]
-        g.storage = self._storage
+        return g
+
+    def tile_field(self):
+        """The ctypes ``jt_field`` of the affine-tile snapshots (storage
+        JT_STORE_TILE_*), built on first use; the input of
+        jt_stage_tile_fields."""
+        if self.encoding != "tile":
+            raise ValueError("tile_field() needs encoding='tile'")
+        if self._tiles is None:
+            res, base, tiles = build_tile_snapshots(self.data, (self.Nx, self.Ny, self.Nz),
+                                                    self._mode == L.JT_GRID_PERIODIC, self._storage)
+            g = self._grid_desc()
+            g.storage = L.JT_STORE_TILE_BF16 if self._storage == L.JT_STORE_BF16 else L.JT_STORE_TILE_F16
+            g.n_pairs = res.shape[0] - 1
+            g.pair_stride = res.shape[1] * res.shape[2]
+            g.pairs = res.data_ptr()
+            g.tile_base = base.data_ptr()
+            g.tiles[:] = list(tiles)
+            self._tiles = {"res": res, "base": base, "tiles": tiles, "grid": g,
+                           "field": L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))}
+        return self._tiles["field"]
+
+    def _device(self):
+        if self._dev is not None:
+            return
+        ps = self._pair_storage()
+        pairs, scales = build_pairs_device(self.data, ps, quad=self._successors())
+        self._scales = scales
+        P = max(self.data.shape[0] - 1, 1)
+        # node n's own six values sit in slots 0-5 of both record layouts
+        view = pairs if ps == L.JT_STORE_F32 else pairs[: P * self.N * 16].view(P, self.N, 16)
+        self._dev = {"pairs": view, "buffer": pairs}
+        g = self._grid_desc()
+        g.storage = ps
         g.n_pairs = P
         g.pair_stride = self.N
         g.pairs = pairs.data_ptr()

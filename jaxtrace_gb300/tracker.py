@@ -227,7 +227,7 @@ class ParticleTracker:
         host0 = src if src is not None else torch.from_numpy(x0)
         pos = host0.to("cuda", non_blocking=src is not None)
         if velocities is not None:
-            torch.from_numpy(velocities[0]).copy_(self._field.sample_at_positions(pos, times[0]))
+            torch.from_numpy(velocities[0]).copy_(self._field.sample_at_positions(pos, times[0], arith=self._arith()))
         # row 0 is a host copy of the input: made on a helper thread while
         # the device tracks (torch releases the GIL inside copy_)
         import threading
@@ -258,7 +258,7 @@ class ParticleTracker:
         if compact and self.options.record_final_only and T > 1:
             torch.from_numpy(positions[-1]).copy_(pos)        # device -> final row, no staging array
             if velocities is not None:
-                torch.from_numpy(velocities[-1]).copy_(self._field.sample_at_positions(pos, times[-1]))
+                torch.from_numpy(velocities[-1]).copy_(self._field.sample_at_positions(pos, times[-1], arith=self._arith()))
             if rows_out is not None:
                 rows_out.put(n_rows - 1, 1)
         if rows_out is not None:
@@ -407,7 +407,13 @@ class ParticleTracker:
         eng.timers = timers
         eng.advance(0, len(times) - 1, None)
         eng.finish()
-        return {"track_launches": eng.launches, "kernels": eng.kernels}
+        out = {"track_launches": eng.launches, "kernels": eng.kernels}
+        if eng.stage is not None:
+            # distinct pre-blended fields of the run and the bytes of one
+            # (what a tracking launch must read at least once)
+            out["stage_fields"] = eng.stage.n_fields
+            out["stage_field_bytes"] = eng.stage.field_bytes
+        return out
 
     def ensemble_batch(self, ensembles, release_times, n_timesteps: int, dt: Optional[float] = None,
                        duration: Optional[float] = None) -> "EnsembleBatch":
@@ -579,7 +585,8 @@ class _Engine:
         self.launches = 0      # tracking-kernel launches
         self.kernels = 0       # every kernel of this library
         self.timers = None
-        self.field_c = tracker._field.jt_field()
+        self.field = tracker._field
+        self.field_c = None    # the gathering descriptor, built when a launch needs it
         self.bc_c = tracker._bc.jt_boundary()
         self.lib = L.load()
         self.stream = L.stream_ptr()
@@ -609,7 +616,7 @@ class _Engine:
             if isinstance(tracker._field, StructuredTimeSeriesField):
                 f = tracker._field
                 overlap = bool(tracker.options.stage_overlap)
-                rec_bytes = (16 if f._storage == L.JT_STORE_F32 else 32) * (2 if overlap else 1)
+                rec_bytes = _stage_node_bytes(f) * (2 if overlap else 1)
                 free = torch.cuda.mem_get_info(pos.device)[0]
                 chunk = _stage_chunk(int(tracker.options.stage_chunk), n_steps, len(f.grid_x) * len(f.grid_y) * len(f.grid_z),
                                      rec_bytes, free)
@@ -657,6 +664,8 @@ class _Engine:
                 field_c = self.stage.field_c
                 p.schedule = self.stage.sched.data_ptr()
             else:
+                if self.field_c is None:
+                    self.field_c = self.field.jt_field()
                 field_c = self.field_c
                 p.schedule = self.sched.data_ptr()
             p.pos = self.pos.data_ptr()
@@ -834,10 +843,14 @@ class _StageFields:
         src = every[first]                                                  # one entry per number
         self.slots = (6 if self.overlap else 3) * self.chunk
         self.ready = -1                                                     # last number blended
+        self.tile = getattr(field, "encoding", "snapshot") == "tile"
         self.f32 = field._storage == L.JT_STORE_F32
-        self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
+        if self.tile:
+            self.out_storage = L.JT_STORE_STAGE_TILE
+        else:
+            self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
         scales = np.ones(len(src), dtype=F32)
-        if not self.f32:
+        if not self.f32 and not self.tile:
             scales = _stage_scales(src)
         # the tracking schedule: pair -> slot, weights -> the slot's scale
         stage = host.copy().reshape(n_steps, 4)
@@ -851,25 +864,42 @@ class _StageFields:
         self.sched = torch.from_numpy(stage.reshape(-1).view(np.int32).reshape(-1, 8).copy()).to(dev)
         self.src = torch.from_numpy(src.view(np.int32).reshape(-1, 8).copy()).to(dev)
         self.scales = torch.from_numpy(scales).to(dev)
-        field._device()
-        g0 = field._cgrid
-        nodes = int(g0.pair_stride)
-        rec = 4 if self.f32 else 8                                           # float32 words per node
+        self.bbuf = None
+        if self.tile:
+            self.src_field = field.tile_field()
+            g0 = field._tiles["grid"]
+            tiles = int(g0.tiles[0]) * int(g0.tiles[1]) * int(g0.tiles[2])
+            nodes = tiles * L.JT_TILE_QUADS                                  # residual quads per slot
+            rec = 8                                                          # float32 words per quad
+            self.bbuf = torch.empty(self.slots * tiles * 16, dtype=torch.float32, device=dev)
+            self.tiles = tiles
+        else:
+            field._device()
+            g0 = field._cgrid
+            nodes = int(g0.pair_stride)
+            rec = 4 if self.f32 else 8                                       # float32 words per node
+            self.tiles = 0
+            self.src_field = field.jt_field()
         self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
         self.nodes, self.rec = nodes, rec
+        self.n_fields = int(self.uid[-1]) + 1 if len(self.uid) else 0
+        self.field_bytes = nodes * rec * 4 + self.tiles * 64
         self.side = self.before = self.pending = None
         if self.overlap:
             self.side = torch.cuda.Stream(device=dev, priority=-1)
             self.buf.record_stream(self.side)
+            if self.bbuf is not None:
+                self.bbuf.record_stream(self.side)
         g = L.GridField()
         C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
         g.storage = self.out_storage
         g.n_pairs = self.slots
         g.pair_stride = nodes
         g.pairs = self.buf.data_ptr()
+        if self.bbuf is not None:
+            g.tile_base = self.bbuf.data_ptr()
         self.grid = g
         self.field_c = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
-        self.src_field = field.jt_field()
 
     def prepare(self, s: int, stop: int) -> int:
         """Put the fields of steps [s, stop) in their slots before the launch
@@ -904,6 +934,11 @@ class _StageFields:
             ent = self.src.data_ptr() + lo * 32
             sc = self.scales.data_ptr() + lo * 4
             out = self.buf.data_ptr() + (lo % self.slots) * self.nodes * self.rec * 4
+            if self.tile:
+                ob = self.bbuf.data_ptr() + (lo % self.slots) * self.tiles * 64
+                L.check(self.lib.jt_stage_tile_fields(C.byref(self.src_field), C.c_void_p(ent), run,
+                                                      C.c_void_p(out), C.c_void_p(ob), stream))
+                continue
             L.check(self.lib.jt_stage_fields(C.byref(self.src_field), C.c_void_p(ent),
                                              C.c_void_p(None if self.f32 else sc), run, self.out_storage,
                                              C.c_void_p(out), stream))
@@ -919,6 +954,19 @@ def _stage_numbers(entries) -> np.ndarray:
         new[1:] = np.any(raw[1:] != raw[:-1], axis=1)
     new[0] = 0
     return np.cumsum(new)
+
+
+def _stage_node_bytes(field) -> int:
+    """Device bytes per grid node of one pre-blended stage field: float32
+    node records (16 B), float16 yz-quads (32 B), or affine tiles (80 residual
+    quads of 32 B and a 64 B base per 64 cells, about 41 B per node)."""
+    if getattr(field, "encoding", "snapshot") == "tile":
+        nodes = len(field.grid_x) * len(field.grid_y) * len(field.grid_z)
+        tiles = 1
+        for n in (len(field.grid_x), len(field.grid_y), len(field.grid_z)):
+            tiles *= (n + L.JT_TILE - 1) // L.JT_TILE
+        return -(-tiles * (L.JT_TILE_QUADS * 32 + 64) // nodes)
+    return 16 if field._storage == L.JT_STORE_F32 else 32
 
 
 def _stage_chunk(chunk: int, n_steps: int, nodes: int, rec_bytes: int, free_bytes: int) -> int:

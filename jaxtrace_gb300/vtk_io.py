@@ -393,7 +393,9 @@ class VTKUnstructuredTimeSeriesReader:
             files = glob.glob(os.path.expanduser(self.file_pattern))
         pvtu = [f for f in files if f.lower().endswith(".pvtu")]
         vtu = [f for f in files if f.lower().endswith(".vtu")]
-        chosen = pvtu if pvtu else vtu
+        # legacy .vtk files (read by read_vtk_xml) when there is no XML file
+        vtk = [f for f in files if f.lower().endswith(".vtk")]
+        chosen = pvtu if pvtu else (vtu if vtu else vtk)
         chosen.sort(key=_natural_key)
         if self.max_time_steps is not None and len(chosen) > self.max_time_steps:
             chosen = chosen[-self.max_time_steps:]
@@ -763,7 +765,10 @@ def create_field_from_vtk(file_pattern: str, field_type: str = "auto", **kwargs)
     if os.path.isdir(file_pattern):
         files = sorted(f for ext in ("*.vtu", "*.pvtu", "*.vtk", "*.vti", "*.vts", "*.vtr")
                        for f in glob.glob(os.path.join(file_pattern, ext)))
-        pattern = os.path.join(file_pattern, "*.pvtu" if any(f.endswith(".pvtu") for f in files) else "*.vtu")
+        # the pattern of the extension the reader will take: .pvtu, else .vtu, else legacy .vtk
+        exts = {os.path.splitext(f)[1].lower() for f in files}
+        ext = next((e for e in (".pvtu", ".vtu", ".vtk") if e in exts), ".vtu")
+        pattern = os.path.join(file_pattern, "*" + ext)
     else:
         files = sorted(glob.glob(os.path.expanduser(file_pattern)))
         pattern = file_pattern

@@ -59,7 +59,7 @@ class OrcBoundary(C.Structure):
 
 class OrcRun(C.Structure):
     _fields_ = [("precision", i32), ("integrator", i32), ("step_times", vp), ("n_times", i32), ("dt", f64),
-                ("n_threads", i32), ("fallback_count", i64), ("wrapped_count", i64)]
+                ("n_threads", i32), ("fallback_count", i64), ("wrapped_count", i64), ("reseed", vp)]
 
 
 def build(force: bool = False) -> Path:
@@ -233,9 +233,12 @@ class FemSpec:
 
 
 def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F32, n_threads=0,
-          record=False):
+          record=False, reseed=False):
     """Run the oracle; returns (final positions, trajectory or None, run info).
-    In float64 mode a float64 ``x0`` is used as given (no float32 rounding)."""
+    In float64 mode a float64 ``x0`` is used as given (no float32 rounding).
+    With ``reseed`` the info holds ``"reseed"``: (n,3) int32, each particle's
+    last continuous-inlet replacement (step, lattice index 0, lattice index 1),
+    -1 where the inlet never replaced it."""
     lib = load()
     x64 = None
     if precision == ORC_F64 and np.asarray(x0).dtype == np.float64:
@@ -248,12 +251,17 @@ def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F
     out32 = np.zeros((n, 3), np.float32) if precision == ORC_F32 else None
     out64 = np.zeros((n, 3), np.float64) if precision == ORC_F64 else None
     traj = np.zeros((len(st), n, 3), np.float32) if (record and precision == ORC_F32) else None
+    ev = np.full((n, 3), -1, np.int32) if reseed else None
+    r.reseed = _p(ev)
     rc = lib.orc_track(C.byref(field.c), C.byref(boundary.c), C.byref(r), n, x0.ctypes.data, _p(out32), _p(out64),
                        _p(traj), _p(x64))
     if rc != 0:
         raise RuntimeError("oracle rejected its arguments")
     out = out32 if precision == ORC_F32 else out64
-    return out, traj, {"fallback_count": int(r.fallback_count), "wrapped_count": int(r.wrapped_count)}
+    info = {"fallback_count": int(r.fallback_count), "wrapped_count": int(r.wrapped_count)}
+    if reseed:
+        info["reseed"] = ev
+    return out, traj, info
 
 
 def sample(field, pos, t, t_is_f32=True, precision=ORC_F32):

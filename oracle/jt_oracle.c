@@ -87,6 +87,9 @@ typedef struct {
     int n_threads;
     int64_t fallback_count;  /* out: octree fallback lookups */
     int64_t wrapped_count;   /* out: periodic index == N events */
+    int32_t* reseed;         /* optional out (n,3): the last continuous-inlet
+                                replacement of each particle -- its step and
+                                the lattice indices it snapped to; -1 if none */
 } orc_run;
 
 /* ------------------------------------------------------------------------ */
@@ -599,26 +602,29 @@ static double bc_axis_d(int kind, double x, double lo, double hi, double outside
 }
 
 /* argmin |coords - c| over the float32 lattice, first index on ties (boundary.py:1309) */
-static float lattice_f(int res, float c, const float* lat) {
+static int lattice_index_f(int res, float c, const float* lat) {
     int best = 0;
     float bd = fabsf(lat[0] - c);
     for (int j = 1; j < res; ++j) {
         const float d = fabsf(lat[j] - c);
         if (d < bd) { bd = d; best = j; }
     }
-    return lat[best];
+    return best;
 }
 
-static void boundary_f(const orc_boundary* B, const float* lat0, const float* lat1, float* r) {
+/* ev (may be NULL): set to the snapped lattice indices when the inlet
+ * replaced the particle in this call */
+static void boundary_f(const orc_boundary* B, const float* lat0, const float* lat1, float* r, int* ev) {
     if (B->inlet_axis >= 0) {
         const int a = B->inlet_axis, o0 = a == 0 ? 1 : 0, o1 = a == 2 ? 1 : 2;
         const float amin = B->lo[a], amax = B->hi[a];
         const int exited = B->inlet_positive ? r[a] > amax : r[a] < amin;
         if (exited) {
-            const float g0 = lattice_f(B->inlet_res[0], r[o0], lat0);
-            const float g1 = lattice_f(B->inlet_res[1], r[o1], lat1);
+            const int j0 = lattice_index_f(B->inlet_res[0], r[o0], lat0);
+            const int j1 = lattice_index_f(B->inlet_res[1], r[o1], lat1);
             r[a] = B->inlet_positive ? amin : amax;
-            r[o0] = g0; r[o1] = g1;
+            r[o0] = lat0[j0]; r[o1] = lat1[j1];
+            if (ev) { ev[0] = j0; ev[1] = j1; }
         }
         if (B->inlet_positive) {
             if (r[a] < amin) { float w = amax - amin; float s = 0.001f * w; r[a] = amin + s; }
@@ -642,7 +648,7 @@ static void boundary_f(const orc_boundary* B, const float* lat0, const float* la
     for (int a = 0; a < 3; ++a) r[a] = bc_axis_f(B->axis_kind[a], r[a], B->lo[a], B->hi[a], B->outside_value);
 }
 
-static void boundary_d(const orc_boundary* B, const float* lat0, const float* lat1, double* r) {
+static void boundary_d(const orc_boundary* B, const float* lat0, const float* lat1, double* r, int* ev) {
     if (B->inlet_axis >= 0) {
         const int a = B->inlet_axis, o0 = a == 0 ? 1 : 0, o1 = a == 2 ? 1 : 2;
         const double amin = B->lo[a], amax = B->hi[a];
@@ -660,6 +666,7 @@ static void boundary_d(const orc_boundary* B, const float* lat0, const float* la
                     if (d < bd) { bd = d; best = j; }
                 }
                 g[q] = lats[q][best];
+                if (ev) ev[q] = best;
             }
             r[a] = B->inlet_positive ? amin : amax;
             r[o0] = g[0]; r[o1] = g[1];
@@ -818,12 +825,15 @@ int orc_track(const orc_field* F, const orc_boundary* B, orc_run* R, int n, cons
 #endif
 #pragma omp parallel for schedule(static) reduction(+ : fb, wr)
     for (int i = 0; i < n; ++i) {
+        int32_t last[3] = {-1, -1, -1};
         if (R->precision == ORC_F32) {
             float x[3] = {x0[3 * (size_t)i], x0[3 * (size_t)i + 1], x0[3 * (size_t)i + 2]};
             if (traj) memcpy(traj + 3 * (size_t)i, x, sizeof x);
             for (int s = 0; s + 1 < T; ++s) {
+                int ev[2] = {-1, -1};
                 step_f(F, R, s, x, &fb, &wr);
-                boundary_f(B, lat[0], lat[1], x);
+                boundary_f(B, lat[0], lat[1], x, ev);
+                if (ev[0] >= 0) { last[0] = s; last[1] = ev[0]; last[2] = ev[1]; }
                 if (traj) memcpy(traj + ((size_t)(s + 1) * n + i) * 3, x, sizeof x);
             }
             memcpy(out_f32 + 3 * (size_t)i, x, sizeof x);
@@ -831,11 +841,14 @@ int orc_track(const orc_field* F, const orc_boundary* B, orc_run* R, int n, cons
             double x[3];
             for (int a = 0; a < 3; ++a) x[a] = x0_f64 ? x0_f64[3 * (size_t)i + a] : (double)x0[3 * (size_t)i + a];
             for (int s = 0; s + 1 < T; ++s) {
+                int ev[2] = {-1, -1};
                 step_d(F, R, s, x, &fb);
-                boundary_d(B, lat[0], lat[1], x);
+                boundary_d(B, lat[0], lat[1], x, ev);
+                if (ev[0] >= 0) { last[0] = s; last[1] = ev[0]; last[2] = ev[1]; }
             }
             out_f64[3 * (size_t)i] = x[0]; out_f64[3 * (size_t)i + 1] = x[1]; out_f64[3 * (size_t)i + 2] = x[2];
         }
+        if (R->reseed) memcpy(R->reseed + 3 * (size_t)i, last, sizeof last);
     }
     R->fallback_count = fb;
     R->wrapped_count = wr;
@@ -861,7 +874,7 @@ int orc_sample(const orc_field* F, double t, int t_is_f32, int precision, int m,
 /* Apply a boundary to m float32 points in place. */
 int orc_boundary_apply(const orc_boundary* B, int m, float* pos) {
     if (B->inlet_axis >= 0 && (B->lattice[0] == NULL || B->lattice[1] == NULL)) return -1;
-    for (int i = 0; i < m; ++i) boundary_f(B, B->lattice[0], B->lattice[1], pos + 3 * (size_t)i);
+    for (int i = 0; i < m; ++i) boundary_f(B, B->lattice[0], B->lattice[1], pos + 3 * (size_t)i, NULL);
     return 0;
 }
 

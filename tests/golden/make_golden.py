@@ -2,6 +2,7 @@
 
 Run from the repository root in a checkout that has the reference sources:
     python tests/golden/make_golden.py /path/to/JAXTrace
+(or with the path in the JAXTRACE_REFERENCE environment variable).
 Phase ``numpy`` imports the reference as-is (no jax installed, so every
 module takes its NumPy path).  Phase ``octree`` puts the NumPy stand-in for
 jax (oracle/jaxshim) first on sys.path so the octree modules, which import
@@ -355,7 +356,9 @@ if __name__ == "__main__":
     if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
         PHASES[sys.argv[1]](sys.argv[2])
         sys.exit(0)
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("JAXTRACE_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py /path/to/JAXTrace   (or set JAXTRACE_REFERENCE)")
     env = dict(os.environ, PYTHONDONTWRITEBYTECODE="1")
     for phase in PHASES:
         subprocess.run([sys.executable, __file__, phase, ref], check=True, env=env)

@@ -90,3 +90,37 @@ def test_sharded_tracking_and_grid_reduction_on_two_gloo_ranks():
     assert res[0]["local"] == [501, 501] and res[1]["local"] == [500, 500]
     for r in res:
         assert np.all(r["grid"] == 3.0)
+
+
+def test_nccl_collectives_take_device_tensors(monkeypatch):
+    """Under NCCL the helpers hand the collectives tensors on the rank's
+    CUDA device (NCCL rejects host tensors); the backend, the device and the
+    collective are stand-ins here, so this runs without a GPU."""
+    import torch
+    import torch.distributed as dist
+    monkeypatch.setattr(dist, "is_initialized", lambda: True)
+    monkeypatch.setattr(dist, "get_world_size", lambda *a: 2)
+    monkeypatch.setattr(dist, "get_rank", lambda *a: 0)
+    monkeypatch.setattr(dist, "get_backend", lambda *a: "nccl")
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 3)
+    assert D.collective_device() == torch.device("cuda", 3)
+    # route "the device" to the meta device to watch what the collectives get
+    monkeypatch.setattr(D, "collective_device", lambda: torch.device("meta"))
+    seen = []
+
+    def fake_all_gather(parts, t):
+        seen.append(t.device.type)
+        for p in parts:
+            p.copy_(t)
+
+    def fake_all_reduce(t, op=None):
+        seen.append(t.device.type)
+
+    monkeypatch.setattr(dist, "all_gather", fake_all_gather)
+    monkeypatch.setattr(dist, "all_reduce", fake_all_reduce)
+    out = D.gather_rows(torch.zeros((3, 3)), 5)
+    assert out.device.type == "meta" and out.shape == (5, 3)
+    D.allreduce_sum(torch.ones((2, 2), device="meta"))
+    assert seen == ["meta", "meta"]
+    monkeypatch.undo()
+    assert D.collective_device() == torch.device("cpu")

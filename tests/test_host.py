@@ -27,7 +27,7 @@ def test_library_exports_every_header_symbol():
     assert len(names) >= 8
     for n in names:
         assert hasattr(lib, n), n
-    assert lib.jt_abi_version() == 1
+    assert lib.jt_abi_version() == L.ABI_VERSION == 2
 
 
 def test_struct_layouts_match():

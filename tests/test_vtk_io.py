@@ -207,3 +207,21 @@ def test_fields_from_vtk_files(tmp_path):
     assert jt.TimeVaryingField is jt.TimeSeriesField
     with pytest.raises(FileNotFoundError):
         jt.create_field_from_vtk(str(tmp_path / "nothing_*.vtu"))
+
+
+def test_legacy_vtk_time_series(tmp_path):
+    """A directory or a pattern of legacy .vtk files reads as a time series
+    (the reader falls back to .vtk when there is no .pvtu/.vtu file)."""
+    import jaxtrace_gb300 as jt
+    rng = np.random.default_rng(8)
+    P = rng.random((15, 3)).astype(F32)
+    T4 = rng.integers(0, 15, size=(6, 4))
+    U = rng.normal(size=(3, 15, 3)).astype(F32)
+    d = tmp_path / "legacy"
+    d.mkdir()
+    for k in range(3):
+        V.write_vtk_legacy(str(d / f"step_{k}.vtk"), P, T4, {"velocity": U[k]}, binary=bool(k % 2))
+    for spec in (str(d), str(d / "step_*.vtk")):
+        f = jt.create_field_from_vtk(spec)
+        assert isinstance(f, jt.TimeSeriesField) and np.array_equal(f.data, U)
+        assert np.array_equal(f.positions, P)
