@@ -266,12 +266,15 @@ def adjoint_leg(a, profile=False):
             fwd_ms.append(e[0].elapsed_time(e[1]))
             bwd_ms.append(e[1].elapsed_time(e[2]))
     gx = x0_t.grad.cpu().numpy().astype(np.float64)
-    # float64 central differences of single particles (each particle's loss term is its own)
+    # float64 central differences (oracle.fd), each split by whether its two
+    # runs kept every field evaluation in the unperturbed run's cells
+    import oracle.fd as FD
     spec = oracle.GridSpec(c["data"], c["times"], g, g, g, "periodic")
     obc = oracle.BoundarySpec(kinds=("periodic",) * 3)
     rng = np.random.default_rng(17)
     fd_stats = {}
-    for horizon in sorted({min(50, n_steps), n_steps}):
+    horizons = sorted({min(50, n_steps), n_steps})
+    for horizon in horizons:
         if horizon != n_steps:
             # a shorter horizon needs its own adjoint
             xs = torch.tensor(x0[:4096], device="cuda", requires_grad=True)
@@ -282,55 +285,33 @@ def adjoint_leg(a, profile=False):
         else:
             gref, pool = gx, n
         times = np.linspace(0.0, horizon * dt, horizon + 1, dtype=np.float32)
-        picks = list(zip(rng.integers(0, pool, 96), rng.integers(0, 3, 96)))
+        # 1,024 particles x 3 components
+        parts = rng.choice(pool, size=min(1024, pool), replace=False)
+        picks = [(int(i), a) for i in parts for a in range(3)]
+        ad = np.array([gref[i, a] for i, a in picks])
         for h in (1e-3, 1e-5, 1e-7):
-            ad, fd = [], []
-            for i, ax in picks:
-                if h < 1e-6:
-                    # below float32 resolution: float64 start points straddle fewer cell faces
-                    pair = np.repeat(x0[i:i + 1].astype(np.float64), 2, axis=0)
-                    xp, xm = float(x0[i, ax]) + h, float(x0[i, ax]) - h
-                else:
-                    pair = np.repeat(x0[i:i + 1], 2, axis=0)
-                    xp, xm = np.float32(float(x0[i, ax]) + h), np.float32(float(x0[i, ax]) - h)
-                pair[0, ax], pair[1, ax] = xp, xm
-                out, _, _ = oracle.track(spec, obc, pair, times, dt, precision=oracle.ORC_F64)
-                fd.append((np.sum((out[0] - y[i]) ** 2) - np.sum((out[1] - y[i]) ** 2)) / (float(xp) - float(xm)))
-                ad.append(gref[i, ax])
-            ad, fd = np.array(ad), np.array(fd)
-            rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
-            fd_stats[f"{horizon}_steps_h{h:g}"] = {"frac_within_1e-3": float(np.mean(rel < 1e-3)),
-                                                  "median_rel": float(np.median(rel)), "samples": int(len(rel))}
-    # dL/dU of a 2048-particle subset's loss against float64 central differences
-    # (h = 1e-3 on one snapshot value; each difference reruns the subset in the oracle)
-    m = 2048
+            # below float32 resolution float64 start points are needed
+            fd, same = FD.dx0_differences(spec, obc, x0, y, picks, times, dt, h, f64_start=h < 1e-6)
+            fd_stats[f"{horizon}_steps_h{h:g}"] = FD.agreement(ad, fd, same)
+    # dL/dU of a 128-particle subset's loss against float64 central
+    # differences at h = 1e-3 on 1,024 snapshot entries the subset samples
+    m = 128
     fd_U = {}
-    for horizon in sorted({min(50, n_steps), n_steps}):
+    for horizon in horizons:
         xs = torch.tensor(x0[:m], device="cuda")
         Us = U_t.detach().clone().requires_grad_(True)
         xh = solver(xs, Us, (0.0, horizon * dt), horizon + 1, dt=dt)
         ((xh - y_t[:m]) ** 2).sum().backward()
         gU = Us.grad.cpu().numpy().reshape(16, -1, 3).astype(np.float64)
         nz = np.argwhere(gU != 0.0)
+        sel = nz[rng.choice(len(nz), size=min(1024, len(nz)), replace=False)]
         times = np.linspace(0.0, horizon * dt, horizon + 1, dtype=np.float32)
-
-        def sub_loss(d):
-            s = oracle.GridSpec(d, c["times"], g, g, g, "periodic")
-            o, _, _ = oracle.track(s, obc, x0[:m], times, dt, precision=oracle.ORC_F64)
-            return float(np.sum((o - y[:m]) ** 2))
-
-        ad, fd = [], []
-        for t, nd, cc in nz[rng.choice(len(nz), size=min(24, len(nz)), replace=False)]:
-            dp, dm = c["data"].copy(), c["data"].copy()
-            dp[t, nd, cc] += np.float32(1e-3)
-            dm[t, nd, cc] -= np.float32(1e-3)
-            fd.append((sub_loss(dp) - sub_loss(dm)) / (float(dp[t, nd, cc]) - float(dm[t, nd, cc])))
-            ad.append(gU[t, nd, cc])
-        ad, fd = np.array(ad), np.array(fd)
-        rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-3 * np.abs(fd).max())
-        fd_U[f"{horizon}_steps_h0.001"] = {"frac_within_1e-3": float(np.mean(rel < 1e-3)),
-                                           "median_rel": float(np.median(rel)), "samples": int(len(rel)),
-                                           "subset_particles": m}
+        spec_u = oracle.GridSpec(c["data"].copy(), c["times"], g, g, g, "periodic")
+        fd, same = FD.du_differences(spec_u, obc, x0[:m], y[:m], [tuple(int(v) for v in q) for q in sel], times,
+                                     dt, h=1e-3)
+        r = FD.agreement(np.array([gU[t, nd, cc] for t, nd, cc in sel]), fd, same)
+        r["subset_particles"] = m
+        fd_U[f"{horizon}_steps_h0.001"] = r
     f, b = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
     return {"fd_check_dL_dU": fd_U,
             "workload": f"differentiation: 64^3 periodic ABC, 16 snapshots, {n:,} lattice seeds, RK4 dt=0.01, "
@@ -339,10 +320,11 @@ def adjoint_leg(a, profile=False):
             "forward_particle_steps_per_s": n * n_steps / (f / 1e3),
             "adjoint_particle_steps_per_s": n * n_steps / (b / 1e3),
             "fd_check_dL_dx0": fd_stats,
-            "fd_note": "float64 central differences of single particles at h=1e-3, 1e-5 (float32 start points) "
-                       "and 1e-7 (float64 start points) on x0; trilinear cell faces make the exact derivative "
-                       "jump, so the wider steps and the longer horizon have more samples whose difference "
-                       "straddles a face"}
+            "fd_note": "float64 central differences (oracle/fd.py) of 1,024 particles x 3 components at h=1e-3, "
+                       "1e-5 (float32 start points) and 1e-7 (float64 start points), and of 1,024 snapshot "
+                       "entries of a 128-particle loss at h=1e-3; 'same_cells' are the differences whose two "
+                       "runs evaluated the field in exactly the unperturbed run's cells, 'crossing_a_face' the "
+                       "rest, where the trilinear field's derivative jumps and the difference is a chord"}
 
 
 def _mesh_oracle_spec(c, f):
@@ -985,10 +967,12 @@ def main():
                    "sample": f"{len(sub)} particles (every 256th) x {a.n_steps} RK4 steps, float32 C restatement "
                              f"of the reference NumPy path (oracle/jt_oracle.c), OpenMP on {cores} threads"}
 
-    # headline: the fastest 16-bit variant whose error meets the budget
+    # headline: the fastest BF16-storage variant whose error meets the budget
+    # (the storage the metric names), else the fastest 16-bit one that does
     sixteen = [v for v in results if VARIANTS[v][0] != "f32"]
     ok = [v for v in sixteen if accuracy.get(v, {}).get("budget_met")]
-    pool = ok or sixteen or list(results)
+    ok_bf16 = [v for v in ok if VARIANTS[v][0] == "bf16"]
+    pool = ok_bf16 or ok or sixteen or list(results)
     head = max(pool, key=lambda v: results[v]["value"])
     fp32 = {k: results[k]["value"] for k in ("f32", "f32c") if k in results}
     line = {"metric": METRIC, "value": results[head]["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -1002,8 +986,9 @@ def main():
                          "error_p99_not_reseed_differs": accuracy.get(head, {}).get("not_reseed_differs", {}).get("p99"),
                          "over_f32_exact": results[head]["value"] / fp32["f32"] if "f32" in fp32 else None,
                          "over_f32_compensated": results[head]["value"] / fp32["f32c"] if "f32c" in fp32 else None,
-                         "choice": "fastest 16-bit variant whose p99 error over the particles with the float64 run's "
-                                   "last inlet replacement is <= 1e-4" if ok else "no 16-bit variant met the budget"},
+                         "choice": ("fastest BF16-storage variant (else 16-bit) whose p99 error over the particles with "
+                                    "the float64 run's last inlet replacement is <= 1e-4") if ok else
+                                   "no 16-bit variant met the budget"},
             "roofline": results[head]["roofline"], "gpu_launches": results[head]["gpu_launches"]}
     if parity is not None:
         line["parity_f32_oracle"] = parity
@@ -1042,7 +1027,9 @@ def main():
         if not a.no_batch:
             line["batching"] = batch_leg(a)
     # the per-variant table and the error split last, so that the end of the line carries them
-    line["variants"] = {v: {"value": r["value"], "ms_per_step": r["ms_per_step"], "storage": r["storage"],
+    line["variants"] = {v: {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                            "track_kernel_ms_per_step": r["track_kernel_ms_per_step"],
+                            "launch_ms": r["launch_ms"], "storage": r["storage"],
                             "arithmetic": r["arithmetic"], "encoding": r["encoding"], "status": r["status"],
                             "roofline_frac": r["roofline"]["frac"],
                             "issue_frac": r["roofline"].get("issue", {}).get("frac"),

@@ -57,8 +57,15 @@ extern "C" {
 /* Pre-blended stage fields of a regular grid (jt_stage_fields), tracking only:
  * one time level per schedule entry, entry.pair = the field slot. */
 #define JT_STORE_STAGE_F32 3 /* float32 {x,y,z,0} per node (16 B)               */
-#define JT_STORE_STAGE_F16 4 /* float16 yz-quads per node (32 B); entry.wa holds
-                                the field's power-of-two scale                 */
+#define JT_STORE_STAGE_F16 4 /* offset float16 yz-quads per node (32 B) of the
+                                values divided by the power-of-two scale held
+                                in entry.wa: the values of nodes (j,k),
+                                (j,k1), (j1,k), (j1,k1) are o + r with float16
+                                residuals r -- words 0-3 their (rx,ry), words
+                                4-5 their rz in pairs -- and a per-quad offset
+                                o: word 6 ox as float32, word 7 a float32
+                                whose value is oy and whose low 16 bits are oz
+                                as float16                                  */
 /* Affine-tile snapshots of a regular grid (input of jt_stage_tile_fields).
  * The grid's cells are cut into tiles of JT_TILE^3 cells; tile (tx,ty,tz)
  * covers cells [JT_TILE*t, JT_TILE*t + JT_TILE) per axis and its
@@ -67,22 +74,14 @@ extern "C" {
  * (periodic), at continuous index coordinate min(JT_TILE*t + l, n-1) or
  * JT_TILE*t + l.  Per snapshot and tile a float32 affine base
  * b(f) = o + Gx*fx + Gy*fy + Gz*fz in the continuous index coordinates f is
- * stored (jt_tile_base layout below), and every tile node holds the 16-bit
- * residual v - b at its coordinate: 4 halves {x, y, z, 0} (8 B), nodes in
- * order (lx*(JT_TILE+1) + ly)*(JT_TILE+1) + lz. */
+ * stored as 16 floats {ox, oy, Gx.x, Gx.y, Gy.x, Gy.y, Gz.x, Gz.y, oz, Gx.z,
+ * Gy.z, Gz.z, 0, 0, 0, 0}, and every tile node holds the 16-bit residual
+ * v - b at its coordinate: 4 halves {x, y, z, 0} (8 B), nodes in order
+ * (lx*(JT_TILE+1) + ly)*(JT_TILE+1) + lz. */
 #define JT_STORE_TILE_BF16 5 /* bfloat16 residuals                            */
 #define JT_STORE_TILE_F16 6  /* float16 residuals                             */
-/* Pre-blended affine-tile stage field (tracking only): per slot and tile the
- * blended float32 base, and (JT_TILE+1)*JT_TILE*JT_TILE float16 residual
- * yz-quads of 32 B: quad (lx*JT_TILE + ly)*JT_TILE + lz holds local nodes
- * (lx,ly,lz), (lx,ly,lz+1), (lx,ly+1,lz), (lx,ly+1,lz+1); words 0-3 their
- * (x,y) half pairs, words 4-5 their z in pairs, words 6-7 zero. */
-#define JT_STORE_STAGE_TILE 7
 #define JT_TILE 4
 #define JT_TILE_NODES 125 /* (JT_TILE+1)^3 residual nodes per snapshot tile   */
-#define JT_TILE_QUADS 80  /* (JT_TILE+1)*JT_TILE^2 residual quads per stage tile */
-/* Tile base record, 16 floats: {ox, oy, Gx.x, Gx.y, Gy.x, Gy.y, Gz.x, Gz.y,
- * oz, Gx.z, Gy.z, Gz.z, 0, 0, 0, 0} (x,y parts in one aligned 32 B half). */
 
 /* grid sampler bounds handling: fields/structured.py:89 */
 #define JT_GRID_CLAMP 0
@@ -165,13 +164,9 @@ typedef struct {
     int32_t n_pairs;       /* number of snapshot pairs (>= 1)                  */
     int64_t pair_stride;   /* records per pair (= nx*ny*nz)                    */
     const void* pairs;     /* device                                          */
-    /* affine-tile storages (JT_STORE_TILE_*, JT_STORE_STAGE_TILE) only:
-     *   TILE_*      pairs: residual nodes of n_pairs+1 snapshots, pair_stride
-     *               = tiles*JT_TILE_NODES records (8 B) per snapshot;
-     *               tile_base: (n_pairs+1) x tiles base records
-     *   STAGE_TILE  pairs: residual quads of n_pairs slots, pair_stride =
-     *               tiles*JT_TILE_QUADS quads (32 B) per slot;
-     *               tile_base: n_pairs x tiles base records
+    /* affine-tile snapshots (JT_STORE_TILE_*) only: pairs holds the residual
+     * nodes of n_pairs+1 snapshots, pair_stride = tiles*JT_TILE_NODES records
+     * (8 B) per snapshot, and tile_base the (n_pairs+1) x tiles base records,
      * where tiles = tiles[0]*tiles[1]*tiles[2], tiles[a] = (n_a + JT_TILE - 1)
      * / JT_TILE, tile (tx,ty,tz) at (tx*tiles[1] + ty)*tiles[2] + tz.  Unused
      * (NULL, 0) by the other storages. */
@@ -388,16 +383,14 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
 int jt_stage_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
                     int32_t out_storage, void* out, void* stream);
 
-/* The same for affine-tile snapshots (JT_STORE_TILE_BF16 / _F16): blends the
- * tile bases and the residuals of each entry's pair (the blend is linear, so
- * the blended field is the blended base plus the blended residual) into n
- * JT_STORE_STAGE_TILE slots: out_quads + j * tiles * JT_TILE_QUADS * 32 B and
- * out_base + j * tiles * 16 floats, both device.  The entries carry plain
- * blend weights (sa = sb = 1).  The tracking launch then takes a
- * jt_grid_field with storage = JT_STORE_STAGE_TILE, pairs = out_quads,
- * tile_base = out_base, n_pairs = n, pair_stride = tiles * JT_TILE_QUADS. */
-int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, int32_t n, void* out_quads,
-                         float* out_base, void* stream);
+/* The same for affine-tile snapshots (JT_STORE_TILE_BF16 / _F16), always
+ * into JT_STORE_STAGE_F16 fields: each node's quad values are the tile base
+ * at the nodes' coordinates plus their residuals, blended per the entry
+ * (sa = sb = 1: tile snapshots carry no per-snapshot scale).  out_scales:
+ * device (n) power-of-two bounds of the blended values (the entries' wa in
+ * the tracking launch); out: device, field j at out + j * nodes * 32 B. */
+int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
+                         void* out, void* stream);
 
 /* ---- adjoint ------------------------------------------------------------- */
 /* No reference counterpart: JAXTrace has no gradients (no jax.grad on this

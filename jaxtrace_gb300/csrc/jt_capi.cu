@@ -86,12 +86,6 @@ static int check_field(const jt_field* f) {
             if (g->bounds_mode < JT_GRID_CLAMP || g->bounds_mode > JT_GRID_PERIODIC)
                 return set_error(JT_ERR_INVALID, "unknown bounds_mode %d", g->bounds_mode);
             if (g->n_pairs < 1 || g->pairs == nullptr) return set_error(JT_ERR_INVALID, "grid field has no snapshot pairs");
-            if (g->storage == JT_STORE_STAGE_TILE) {
-                if (int rc = check_tiles(*g)) return rc;
-                if (g->pair_stride != (int64_t)g->tiles[0] * g->tiles[1] * g->tiles[2] * JT_TILE_QUADS)
-                    return set_error(JT_ERR_INVALID, "pair_stride must be tiles * JT_TILE_QUADS");
-                return JT_OK;
-            }
             if (g->storage == JT_STORE_TILE_BF16 || g->storage == JT_STORE_TILE_F16)
                 return set_error(JT_ERR_UNSUPPORTED, "affine-tile snapshots are read by jt_stage_tile_fields only");
             if (g->pair_stride < (int64_t)g->nx * g->ny * g->nz)

@@ -43,7 +43,31 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// 16-bit yz-quad pairs -> float16 yz-quads of the blended values divided by
+// Offset yz-quad (quad_yz in jt_grid.cuh) of the four nodes' values u,
+// already divided by the entry's power-of-two scale: ox the float32 mean of
+// the x values; oy the mean of the y values rounded to bfloat16 in the high
+// half of word 7, whose low half holds oz, the mean of the z values rounded
+// to float16; each residual is the value minus the offset as the tracking
+// kernel reads it back (word 7 whole as a float32 for oy), rounded to
+// float16.
+__device__ __forceinline__ void encode_quad(const V3 (&u)[4], uint4& a, uint4& b) {
+    const float ox = 0.25f * ((u[0].x + u[1].x) + (u[2].x + u[3].x));
+    const float my = 0.25f * ((u[0].y + u[1].y) + (u[2].y + u[3].y));
+    const float mz = 0.25f * ((u[0].z + u[1].z) + (u[2].z + u[3].z));
+    const __half hz = __float2half_rn(mz);
+    const uint32_t w7 = ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(my)) << 16) | __half_as_ushort(hz);
+    const float oy = __uint_as_float(w7), oz = __half2float(hz);
+    a.x = pack_h2(u[0].x - ox, u[0].y - oy);
+    a.y = pack_h2(u[1].x - ox, u[1].y - oy);
+    a.z = pack_h2(u[2].x - ox, u[2].y - oy);
+    a.w = pack_h2(u[3].x - ox, u[3].y - oy);
+    b.x = pack_h2(u[0].z - oz, u[1].z - oz);
+    b.y = pack_h2(u[2].z - oz, u[3].z - oz);
+    b.z = __float_as_uint(ox);
+    b.w = w7;
+}
+
+// 16-bit yz-quad pairs -> offset yz-quads of the blended values divided by
 // the entry's power-of-two scale.  Blocks of 64 threads at <= 64 registers
 // (4,096 per block): one fits beside five blocks of the float16 tracking
 // kernel (5 x 256 threads x 48 registers), so the next chunk's fields are
@@ -84,15 +108,10 @@ __global__ void __launch_bounds__(kStageBlock16, 16) k_stage_f16(jt_grid_field F
             c10 = scale_cv(blend_cv<false, STORE>(p10, e, WA, WB, false), inv);
             c11 = scale_cv(blend_cv<false, STORE>(p11, e, WA, WB, false), inv);
         }
+        const V3 u[4] = {V3{c00.xy.x, c00.xy.y, c00.z}, V3{c01.xy.x, c01.xy.y, c01.z},
+                         V3{c10.xy.x, c10.xy.y, c10.z}, V3{c11.xy.x, c11.xy.y, c11.z}};
         uint4 a, b;
-        a.x = pack_h2(c00.xy.x, c00.xy.y);
-        a.y = pack_h2(c01.xy.x, c01.xy.y);
-        a.z = pack_h2(c10.xy.x, c10.xy.y);
-        a.w = pack_h2(c11.xy.x, c11.xy.y);
-        b.x = pack_h2(c00.z, c01.z);
-        b.y = pack_h2(c10.z, c11.z);
-        b.z = 0u;
-        b.w = 0u;
+        encode_quad(u, a, b);
         uint4* o = out + 2 * ((int64_t)j * N + node);
         o[0] = a;
         o[1] = b;
@@ -100,96 +119,98 @@ __global__ void __launch_bounds__(kStageBlock16, 16) k_stage_f16(jt_grid_field F
 }
 
 // ---------------------------------------------------------------------------
-// Affine-tile stage fields.  One thread per residual quad of a tile (80 per
-// tile: local x plane 0..4, y and z cell 0..3) walks the chunk's entries; a
-// quad's four nodes of snapshots A and B are reloaded only when the pair
-// changes.  The blend is linear, so the stage residual is the blend of the
-// snapshot residuals and the stage base the blend of the snapshot bases; the
-// first thread of each tile blends its base record.  Blocks of 64 threads so
-// that the side-stream launch fits beside the tracking blocks.
+// Offset yz-quads from affine-tile snapshots (JT_STORE_TILE_*).  One thread
+// per grid node walks the chunk's entries; when the pair changes it rebuilds
+// its quad's four node values of snapshots A and B from the tile that holds
+// the node's cell (tile base at the nodes' index coordinates plus their
+// residuals) and keeps them in registers.  Blocks of 64 threads, as
+// k_stage_f16, so the side-stream launch fits beside the tracking blocks.
 // ---------------------------------------------------------------------------
 
 // Residual node {x, y, z, 0} of 16-bit storage STORE, decoded to float32.
 template <int STORE>
-__device__ __forceinline__ void tile_node(const uint2* __restrict__ r, float2& xy, float& z) {
+__device__ __forceinline__ V3 tile_residual(const uint2* __restrict__ r) {
     const uint2 w = __ldg(r);
-    if (STORE == JT_STORE_TILE_BF16) {
-        xy = make_float2(bf16_lo(w.x), bf16_hi(w.x));
-        z = bf16_lo(w.y);
-    } else {
-        xy = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
-        z = __low2float(*reinterpret_cast<const __half2*>(&w.y));
+    if (STORE == JT_STORE_TILE_BF16) return V3{bf16_lo(w.x), bf16_hi(w.x), bf16_lo(w.y)};
+    const float2 xy = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
+    return V3{xy.x, xy.y, __low2float(*reinterpret_cast<const __half2*>(&w.y))};
+}
+
+// Index coordinate of a tile's local node l on an axis of n nodes.
+__device__ __forceinline__ float tile_coord(int t, int l, int n, bool periodic) {
+    const int g = JT_TILE * t + l;
+    return (float)(periodic ? g : min(g, n - 1));
+}
+
+// The four quad nodes' values of one snapshot: base o + Gx cx + Gy cy + Gz cz
+// at their coordinates plus their residuals.
+template <int STORE>
+__device__ __forceinline__ void tile_values(const uint2* __restrict__ res, const float* __restrict__ rec,
+                                            const int (&lofs)[4], float cx, const float (&cy)[2],
+                                            const float (&cz)[2], V3 (&v)[4]) {
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(rec));
+    const float4 r1 = __ldg(reinterpret_cast<const float4*>(rec) + 1);
+    const float4 r2 = __ldg(reinterpret_cast<const float4*>(rec) + 2);
+    // {ox, oy, Gx.x, Gx.y}, {Gy.x, Gy.y, Gz.x, Gz.y}, {oz, Gx.z, Gy.z, Gz.z}
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float y = cy[c >> 1], z = cz[c & 1];
+        const V3 r = tile_residual<STORE>(res + lofs[c]);
+        v[c] = V3{fmaf(r1.z, z, fmaf(r1.x, y, fmaf(r0.z, cx, r0.x))) + r.x,
+                  fmaf(r1.w, z, fmaf(r1.y, y, fmaf(r0.w, cx, r0.y))) + r.y,
+                  fmaf(r2.w, z, fmaf(r2.z, y, fmaf(r2.y, cx, r2.x))) + r.z};
     }
 }
 
 template <int STORE>
 __global__ void __launch_bounds__(kStageBlock16, 16) k_stage_tile(jt_grid_field F, const jt_blend* __restrict__ ent,
-                                                                int n, uint4* __restrict__ out_q,
-                                                                float* __restrict__ out_b) {
+                                                                const float* __restrict__ scales, int n,
+                                                                uint4* __restrict__ out) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = (int64_t)F.nx * F.ny * F.nz;
+    if (node >= N) return;
+    const int k = (int)(node % F.nz);
+    const int j = (int)((node / F.nz) % F.ny);
+    const int i = (int)(node / ((int64_t)F.nz * F.ny));
+    const bool per = F.bounds_mode == JT_GRID_PERIODIC;
+    const int tx = i >> 2, ty = j >> 2, tz = k >> 2, li = i & 3, lj = j & 3, lk = k & 3;
     const int64_t tiles = (int64_t)F.tiles[0] * F.tiles[1] * F.tiles[2];
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t Q = tiles * JT_TILE_QUADS;
-    if (q >= Q) return;
-    const int64_t tile = q / JT_TILE_QUADS;
-    const int lq = (int)(q - tile * JT_TILE_QUADS);
-    const int lx = lq >> 4, ly = (lq >> 2) & 3, lz = lq & 3;
-    // local nodes (lx,ly,lz), (lx,ly,lz+1), (lx,ly+1,lz), (lx,ly+1,lz+1)
-    const int l0 = (lx * (JT_TILE + 1) + ly) * (JT_TILE + 1) + lz;
-    const int lofs[4] = {l0, l0 + 1, l0 + (JT_TILE + 1), l0 + (JT_TILE + 1) + 1};
-    const bool head = lq == 0;
+    const int64_t tile = ((int64_t)tx * F.tiles[1] + ty) * F.tiles[2] + tz;
+    constexpr int K = JT_TILE + 1;
+    // quad nodes (j,k), (j,k1), (j1,k), (j1,k1): local (lj,lk), (lj,lk+1), (lj+1,lk), (lj+1,lk+1)
+    const int l0 = (li * K + lj) * K + lk;
+    const int lofs[4] = {l0, l0 + 1, l0 + K, l0 + K + 1};
+    const float cx = tile_coord(tx, li, F.nx, per);
+    const float cy[2] = {tile_coord(ty, lj, F.ny, per), tile_coord(ty, lj + 1, F.ny, per)};
+    const float cz[2] = {tile_coord(tz, lk, F.nz, per), tile_coord(tz, lk + 1, F.nz, per)};
     const uint2* res = reinterpret_cast<const uint2*>(F.pairs);
     int cur = -1;
     PairVal pv[4];
-    PairVal pb[4];  // the tile base's four triples (o, Gx, Gy, Gz) of A and B
-    for (int j = 0; j < n; ++j) {
-        const jt_blend e = ent[j];
+    for (int jj = 0; jj < n; ++jj) {
+        const jt_blend e = ent[jj];
         const int pr = min(max(e.pair, 0), F.n_pairs - 1);
         if (pr != cur) {
-            const uint2* ra = res + ((int64_t)pr * tiles + tile) * JT_TILE_NODES;
-            const uint2* rb = ra + tiles * JT_TILE_NODES;
+            V3 va[4], vb[4];
+            const int64_t sa = (int64_t)pr * tiles + tile, sb = sa + tiles;
+            tile_values<STORE>(res + sa * JT_TILE_NODES, F.tile_base + sa * 16, lofs, cx, cy, cz, va);
+            tile_values<STORE>(res + sb * JT_TILE_NODES, F.tile_base + sb * 16, lofs, cx, cy, cz, vb);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                tile_node<STORE>(ra + lofs[c], pv[c].axy, pv[c].az);
-                tile_node<STORE>(rb + lofs[c], pv[c].bxy, pv[c].bz);
-            }
-            if (head) {
-                const float* ba = F.tile_base + ((int64_t)pr * tiles + tile) * 16;
-                const float* bb = ba + tiles * 16;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    pb[c].axy = make_float2(__ldg(ba + 2 * c), __ldg(ba + 2 * c + 1));
-                    pb[c].az = __ldg(ba + 8 + c);
-                    pb[c].bxy = make_float2(__ldg(bb + 2 * c), __ldg(bb + 2 * c + 1));
-                    pb[c].bz = __ldg(bb + 8 + c);
-                }
-            }
+            for (int c = 0; c < 4; ++c)
+                pv[c] = PairVal{make_float2(va[c].x, va[c].y), make_float2(vb[c].x, vb[c].y), va[c].z, vb[c].z};
             cur = pr;
         }
-        V3 v[4];
+        const float inv = __frcp_rn(__ldg(scales + jj));   // a power of two: exact
+        V3 u[4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = blend<false, JT_STORE_F32>(pv[c], e);
+        for (int c = 0; c < 4; ++c) {
+            const V3 v = blend<false, JT_STORE_F32>(pv[c], e);
+            u[c] = V3{v.x * inv, v.y * inv, v.z * inv};
+        }
         uint4 a, b;
-        a.x = pack_h2(v[0].x, v[0].y);
-        a.y = pack_h2(v[1].x, v[1].y);
-        a.z = pack_h2(v[2].x, v[2].y);
-        a.w = pack_h2(v[3].x, v[3].y);
-        b.x = pack_h2(v[0].z, v[1].z);
-        b.y = pack_h2(v[2].z, v[3].z);
-        b.z = 0u;
-        b.w = 0u;
-        uint4* o = out_q + 2 * ((int64_t)j * Q + q);
+        encode_quad(u, a, b);
+        uint4* o = out + 2 * ((int64_t)jj * N + node);
         o[0] = a;
         o[1] = b;
-        if (head) {
-            float4* ob = reinterpret_cast<float4*>(out_b + ((int64_t)j * tiles + tile) * 16);
-            V3 t[4];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) t[c] = blend<false, JT_STORE_F32>(pb[c], e);
-            ob[0] = make_float4(t[0].x, t[0].y, t[1].x, t[1].y);
-            ob[1] = make_float4(t[2].x, t[2].y, t[3].x, t[3].y);
-            ob[2] = make_float4(t[0].z, t[1].z, t[2].z, t[3].z);
-            ob[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
     }
 }
 
@@ -201,18 +222,6 @@ template <bool E, int O>
 using StagePeriodic = StageGridField<E, O, JT_GRID_PERIODIC>;
 template <bool E, int O>
 using StageAnyMode = StageGridField<E, O, -1>;
-
-template <int MODE>
-static cudaError_t tile_launch(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p,
-                               cudaStream_t s) {
-    const StageTileField<MODE, true> fld = StageTileField<MODE, true>::create(f, 0);
-    const int bs = p.block_size > 0 ? p.block_size : kBlock;
-    const unsigned g = (unsigned)((p.n_particles + bs - 1) / bs);
-    const InletFrame I = inlet_frame(b);
-    typedef Launcher<GridField, jt_grid_field, int> L;
-    if (p.path != nullptr) return L::template launch_track<false, true>(fld, b, I, p, g, bs, s);
-    return L::template launch_track<false, false>(fld, b, I, p, g, bs, s);
-}
 
 template <template <bool, int> class FT>
 static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p,
@@ -226,16 +235,6 @@ static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, co
 
 int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
     const bool exact = p.arith == JT_ARITH_EXACT;
-    if (f.storage == JT_STORE_STAGE_TILE) {
-        if (exact) return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
-        cudaError_t err;
-        switch (f.bounds_mode) {
-            case JT_GRID_CLAMP: err = tile_launch<JT_GRID_CLAMP>(f, b, p, s); break;
-            case JT_GRID_PERIODIC: err = tile_launch<JT_GRID_PERIODIC>(f, b, p, s); break;
-            default: err = tile_launch<-1>(f, b, p, s); break;
-        }
-        return cuda_status(err, "tracking kernel launch");
-    }
     if (f.storage != JT_STORE_STAGE_F32 && exact)
         return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
     cudaError_t err;
@@ -286,31 +285,30 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     return cuda_status(cudaGetLastError(), "stage field launch");
 }
 
-extern "C" int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, int32_t n, void* out_quads,
-                                    float* out_base, void* stream) {
+extern "C" int jt_stage_tile_fields(const jt_field* field, const jt_blend* entries, const float* out_scales,
+                                    int32_t n, void* out, void* stream) {
     if (field == nullptr || field->kind != JT_FIELD_GRID || field->grid == nullptr)
         return set_error(JT_ERR_INVALID, "stage fields need a regular-grid field");
     const jt_grid_field& F = *field->grid;
     if (int rc = check_grid_shape(F)) return rc;
     if (F.storage != JT_STORE_TILE_BF16 && F.storage != JT_STORE_TILE_F16)
-        return set_error(JT_ERR_INVALID, "affine-tile stage fields come from JT_STORE_TILE_* snapshots");
+        return set_error(JT_ERR_INVALID, "jt_stage_tile_fields reads JT_STORE_TILE_* snapshots");
     if (int rc = check_tiles(F)) return rc;
     if (n < 0) return set_error(JT_ERR_INVALID, "n must be >= 0");
     if (n == 0) return JT_OK;
-    if (entries == nullptr || out_quads == nullptr || out_base == nullptr)
-        return set_error(JT_ERR_INVALID, "entries, out_quads and out_base are required");
+    if (entries == nullptr || out == nullptr || out_scales == nullptr)
+        return set_error(JT_ERR_INVALID, "entries, out_scales and out are required");
     if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshots");
     const int64_t tiles = (int64_t)F.tiles[0] * F.tiles[1] * F.tiles[2];
     if (F.pair_stride != tiles * JT_TILE_NODES)
         return set_error(JT_ERR_INVALID, "pair_stride must be tiles * JT_TILE_NODES");
-    const int64_t Q = tiles * JT_TILE_QUADS;
-    const unsigned g = (unsigned)((Q + kStageBlock16 - 1) / kStageBlock16);
+    const int64_t N = (int64_t)F.nx * F.ny * F.nz;
+    const unsigned g = (unsigned)((N + kStageBlock16 - 1) / kStageBlock16);
     cudaStream_t s = (cudaStream_t)stream;
+    uint4* o = reinterpret_cast<uint4*>(out);
     if (F.storage == JT_STORE_TILE_BF16)
-        k_stage_tile<JT_STORE_TILE_BF16><<<g, kStageBlock16, 0, s>>>(F, entries, n, reinterpret_cast<uint4*>(out_quads),
-                                                                      out_base);
+        k_stage_tile<JT_STORE_TILE_BF16><<<g, kStageBlock16, 0, s>>>(F, entries, out_scales, n, o);
     else
-        k_stage_tile<JT_STORE_TILE_F16><<<g, kStageBlock16, 0, s>>>(F, entries, n, reinterpret_cast<uint4*>(out_quads),
-                                                                     out_base);
+        k_stage_tile<JT_STORE_TILE_F16><<<g, kStageBlock16, 0, s>>>(F, entries, out_scales, n, o);
     return cuda_status(cudaGetLastError(), "stage field launch");
 }

@@ -181,17 +181,42 @@ struct GridField {
     }
 };
 
+__device__ __forceinline__ __half2 u2h2(uint32_t w) { return *reinterpret_cast<const __half2*>(&w); }
+
+// a + w (b - a) on half pairs
+__device__ __forceinline__ __half2 hlerp2(__half2 w, __half2 a, __half2 b) { return __hfma2(w, __hsub2(b, a), a); }
+
+// Offset yz-quad of a float16 stage field (32 B): the blended values of the
+// nodes (j,k), (j,k1), (j1,k), (j1,k1) of one x plane, each stored as
+// o + r with a per-quad offset o and float16 residuals r:
+//   words 0-3  (rx, ry) of the four nodes      words 4-5  (rz, rz) pairs
+//   word 6     ox as float32
+//   word 7     a float32 whose value is oy; its low 16 bits are oz as a
+//              float16 (the encoder measures oy with them in place)
+// The residuals are the spread of four neighbouring values, small beside the
+// values, so float16 arithmetic on them rounds far below the values' own
+// float16 rounding.  Returns the bilinear (y, then z) value at (wy, wz).
+__device__ __forceinline__ V3 quad_yz(const uint32_t (&q)[8], __half2 WY, __half2 WZ) {
+    const __half2 ck = hlerp2(WY, u2h2(q[0]), u2h2(q[2]));   // (x, y) at k
+    const __half2 ck1 = hlerp2(WY, u2h2(q[1]), u2h2(q[3]));  // (x, y) at k1
+    const float2 rxy = __half22float2(hlerp2(WZ, ck, ck1));
+    const __half2 zy = hlerp2(WY, u2h2(q[4]), u2h2(q[5]));   // (z at k, z at k1)
+    const __half rz = __hfma(__high2half(WZ), __hsub(__high2half(zy), __low2half(zy)), __low2half(zy));
+    const float oz = __low2float(u2h2(q[7]));
+    const float2 v = __fadd2_rn(make_float2(__uint_as_float(q[6]), __uint_as_float(q[7])), rxy);
+    return V3{v.x, v.y, oz + __half2float(rz)};
+}
+
 // Pre-blended stage field of a time chunk: one time level per schedule entry
 // (slot = e.pair), blended per node ahead of the tracking launch exactly as
 // TimeSeriesField.sample_at_time blends every node (time_series.py:326-367)
 // before StructuredGridSampler interpolates -- the reference's own order, so
 // the exact mode is bit-identical to blending the gathered corners.
 //   JT_STORE_STAGE_F32: float4 {x, y, z, 0} per node (16 B);
-//   JT_STORE_STAGE_F16: float16 yz-quads per node (32 B): words 0-3 the
-//     (x, y) of nodes (j,k), (j,k1), (j1,k), (j1,k1); words 4-5 their z in
-//     pairs; values divided by the power-of-two scale carried in e.wa.  Two
-//     256-bit loads per evaluation measured faster than eight 64-bit loads of
-//     float16 node records, although those fit L2 and the quads do not.
+//   JT_STORE_STAGE_F16: offset yz-quads per node (32 B, quad_yz), values
+//     divided by the power-of-two scale carried in e.wa.  Two 256-bit loads
+//     per evaluation measured faster than eight 64-bit loads of float16 node
+//     records, although those fit L2 and the quads do not.
 #ifndef JT_STAGE16_MIN_BLOCKS
 #define JT_STAGE16_MIN_BLOCKS 5
 #endif
@@ -259,149 +284,16 @@ struct StageGridField {
             const Quad32* bq = reinterpret_cast<const Quad32*>(F.pairs) + base;
             ldg256(bq + n000, q0);
             ldg256(bq + n100, q1);
-            const float2 z0a = h2f2(q0[4]), z0b = h2f2(q0[5]), z1a = h2f2(q1[4]), z1b = h2f2(q1[5]);
-            v000 = CV{h2f2(q0[0]), z0a.x}; v001 = CV{h2f2(q0[1]), z0a.y};
-            v010 = CV{h2f2(q0[2]), z0b.x}; v011 = CV{h2f2(q0[3]), z0b.y};
-            v100 = CV{h2f2(q1[0]), z1a.x}; v101 = CV{h2f2(q1[1]), z1a.y};
-            v110 = CV{h2f2(q1[2]), z1b.x}; v111 = CV{h2f2(q1[3]), z1b.y};
-            r = trilinear_lerp(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
-            r = V3{r.x * e.wa, r.y * e.wa, r.z * e.wa};
+            // y and z in float16 pairs on the small residuals of each x plane,
+            // x in float32 on the planes' values
+            const __half2 WY = __float2half2_rn(wy), WZ = __float2half2_rn(wz);
+            const V3 a = quad_yz(q0, WY, WZ);
+            const V3 b = quad_yz(q1, WY, WZ);
+            const float2 axy = make_float2(a.x, a.y);
+            const float2 rxy = __ffma2_rn(splat(wx), sub2(make_float2(b.x, b.y), axy), axy);
+            const float rz = fmaf(wx, b.z - a.z, a.z);
+            r = V3{rxy.x * e.wa, rxy.y * e.wa, rz * e.wa};
         }
-        if (mode == JT_GRID_ZERO || mode == JT_GRID_NAN) {
-            if (!(vx && vy && vz)) {
-                const float o = mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);
-                r = V3{o, o, o};
-            }
-        }
-        return r;
-    }
-};
-
-// ---------------------------------------------------------------------------
-// Affine-tile stage field (JT_STORE_STAGE_TILE): per tile of JT_TILE^3 cells
-// a float32 affine base b(f) = o + Gx fx + Gy fy + Gz fz in the continuous
-// index coordinates f, and float16 residual yz-quads.  A cell lies in one
-// tile, so its eight corners carry that tile's residuals, and trilinear
-// interpolation reproduces an affine function exactly: the field at f is
-// b(f) plus the trilinear interpolant of the corner residuals.  The residuals
-// are small (the tile's noise and curvature), so float16 arithmetic on them
-// keeps absolute errors far below those of the values themselves.
-// ---------------------------------------------------------------------------
-
-// Continuous index (clipped or wrapped as structured.py:289-322 does), cell
-// and weight of one axis, fast arithmetic.  f is returned for the base.
-template <int MODE>
-__device__ __forceinline__ void tile_axis(float x, float nofs, float inv_d, int n, float vlo, float vhi, float& f,
-                                          int& i0, float& w, bool& valid, int& flags) {
-    float t = fmaf(x, inv_d, nofs);
-    if (MODE == JT_GRID_PERIODIC) {
-        const int nn = n > 1 ? n : 1;
-        t = np_mod(t, (float)nn);
-        const float fl = floorf(t);
-        int i = (int)fl;
-        w = t - fl;
-        if (i >= nn) {  // the remainder rounded up to N: wrap onto node 0
-            i -= nn;
-            t = 0.0f;
-            flags |= JT_STATUS_INDEX_WRAPPED;
-        }
-        if (i < 0) i = 0;
-        i0 = i;
-        valid = true;
-    } else {
-        valid = (x >= vlo) && (x <= vhi);
-        t = fminf(fmaxf(t, 0.0f), (float)(n > 1 ? n - 1 : 0));  // NaN goes to cell 0
-        const float fl = floorf(t);
-        i0 = __float2int_rz(fl);
-        w = t - fl;
-    }
-    f = t;
-}
-
-__device__ __forceinline__ __half2 u2h2(uint32_t w) { return *reinterpret_cast<const __half2*>(&w); }
-
-// a + w (b - a) on half pairs
-__device__ __forceinline__ __half2 hlerp2(__half2 w, __half2 a, __half2 b) { return __hfma2(w, __hsub2(b, a), a); }
-
-// H2: interpolate the residuals in float16 pairs (HFMA2), converting once at
-// the end; otherwise convert every corner to float32 first.
-template <int MODE, bool H2 = true>
-struct StageTileField {
-    static constexpr int kMinBlocks = JT_STAGE16_MIN_BLOCKS;
-    static constexpr bool kUnrollStages = true;
-    jt_grid_field F;
-    float nofs[3];  // -origin * inv_spacing per axis
-    int tyz;        // tiles[1] * tiles[2]
-    int64_t tiles;  // tiles per slot
-
-    __host__ __device__ static StageTileField create(const jt_grid_field& d, int) {
-        StageTileField s{d, {0.0f, 0.0f, 0.0f}, d.tiles[1] * d.tiles[2],
-                         (int64_t)d.tiles[0] * d.tiles[1] * d.tiles[2]};
-        for (int a = 0; a < 3; ++a) s.nofs[a] = -d.origin[a] * d.inv_spacing[a];
-        return s;
-    }
-
-    __device__ __forceinline__ V3 operator()(const V3& p, const jt_blend& e, int& flags) const {
-        const int mode = MODE >= 0 ? MODE : F.bounds_mode;
-        float fx, fy, fz, wx, wy, wz;
-        int i0, j0, k0;
-        bool vx, vy, vz;
-        if (MODE >= 0) {
-            tile_axis<MODE>(p.x, nofs[0], F.inv_spacing[0], F.nx, F.origin[0], F.valid_hi[0], fx, i0, wx, vx, flags);
-            tile_axis<MODE>(p.y, nofs[1], F.inv_spacing[1], F.ny, F.origin[1], F.valid_hi[1], fy, j0, wy, vy, flags);
-            tile_axis<MODE>(p.z, nofs[2], F.inv_spacing[2], F.nz, F.origin[2], F.valid_hi[2], fz, k0, wz, vz, flags);
-        } else if (mode == JT_GRID_PERIODIC) {
-            tile_axis<JT_GRID_PERIODIC>(p.x, nofs[0], F.inv_spacing[0], F.nx, F.origin[0], F.valid_hi[0], fx, i0, wx, vx, flags);
-            tile_axis<JT_GRID_PERIODIC>(p.y, nofs[1], F.inv_spacing[1], F.ny, F.origin[1], F.valid_hi[1], fy, j0, wy, vy, flags);
-            tile_axis<JT_GRID_PERIODIC>(p.z, nofs[2], F.inv_spacing[2], F.nz, F.origin[2], F.valid_hi[2], fz, k0, wz, vz, flags);
-        } else {
-            tile_axis<JT_GRID_CLAMP>(p.x, nofs[0], F.inv_spacing[0], F.nx, F.origin[0], F.valid_hi[0], fx, i0, wx, vx, flags);
-            tile_axis<JT_GRID_CLAMP>(p.y, nofs[1], F.inv_spacing[1], F.ny, F.origin[1], F.valid_hi[1], fy, j0, wy, vy, flags);
-            tile_axis<JT_GRID_CLAMP>(p.z, nofs[2], F.inv_spacing[2], F.nz, F.origin[2], F.valid_hi[2], fz, k0, wz, vz, flags);
-        }
-        const int slot = min(max(e.pair, 0), F.n_pairs - 1);
-        const int tile = ((i0 >> 2) * F.tiles[1] + (j0 >> 2)) * F.tiles[2] + (k0 >> 2);
-        const int q = tile * JT_TILE_QUADS + ((i0 & 3) << 4) + ((j0 & 3) << 2) + (k0 & 3);
-        const Quad32* bq = reinterpret_cast<const Quad32*>(F.pairs) + (int64_t)slot * F.pair_stride;
-        uint32_t q0[8], q1[8], tb[8];
-        ldg256(bq + q, q0);
-        ldg256(bq + q + 16, q1);
-        const float* rec = F.tile_base + ((int64_t)slot * tiles + tile) * 16;
-        ldg256(rec, tb);
-        const float4 tz = __ldg(reinterpret_cast<const float4*>(rec + 8));
-        // the base: o + Gx fx + Gy fy + Gz fz, x and y in packed pairs
-        float2 bxy = make_float2(__uint_as_float(tb[0]), __uint_as_float(tb[1]));
-        bxy = __ffma2_rn(make_float2(__uint_as_float(tb[2]), __uint_as_float(tb[3])), splat(fx), bxy);
-        bxy = __ffma2_rn(make_float2(__uint_as_float(tb[4]), __uint_as_float(tb[5])), splat(fy), bxy);
-        bxy = __ffma2_rn(make_float2(__uint_as_float(tb[6]), __uint_as_float(tb[7])), splat(fz), bxy);
-        const float bz = fmaf(tz.w, fz, fmaf(tz.z, fy, fmaf(tz.y, fx, tz.x)));
-        V3 r;
-        if (H2) {
-            const __half2 WX = __float2half2_rn(wx), WY = __float2half2_rn(wy), WZ = __float2half2_rn(wz);
-            // x: planes lx (q0) and lx+1 (q1); words 0-3 (x,y) of (y,z), (y,z1), (y1,z), (y1,z1)
-            const __half2 c00 = hlerp2(WX, u2h2(q0[0]), u2h2(q1[0]));
-            const __half2 c01 = hlerp2(WX, u2h2(q0[1]), u2h2(q1[1]));
-            const __half2 c10 = hlerp2(WX, u2h2(q0[2]), u2h2(q1[2]));
-            const __half2 c11 = hlerp2(WX, u2h2(q0[3]), u2h2(q1[3]));
-            const __half2 cz0 = hlerp2(WX, u2h2(q0[4]), u2h2(q1[4]));  // z of (y,z), (y,z1)
-            const __half2 cz1 = hlerp2(WX, u2h2(q0[5]), u2h2(q1[5]));  // z of (y1,z), (y1,z1)
-            // y
-            const __half2 c0 = hlerp2(WY, c00, c10);
-            const __half2 c1 = hlerp2(WY, c01, c11);
-            const float2 zz = __half22float2(hlerp2(WY, cz0, cz1));
-            // z
-            const float2 rxy = __half22float2(hlerp2(WZ, c0, c1));
-            r = V3{rxy.x, rxy.y, fmaf(wz, zz.y - zz.x, zz.x)};
-        } else {
-            const float2 z0a = h2f2(q0[4]), z0b = h2f2(q0[5]), z1a = h2f2(q1[4]), z1b = h2f2(q1[5]);
-            const CV v000{h2f2(q0[0]), z0a.x}, v001{h2f2(q0[1]), z0a.y};
-            const CV v010{h2f2(q0[2]), z0b.x}, v011{h2f2(q0[3]), z0b.y};
-            const CV v100{h2f2(q1[0]), z1a.x}, v101{h2f2(q1[1]), z1a.y};
-            const CV v110{h2f2(q1[2]), z1b.x}, v111{h2f2(q1[3]), z1b.y};
-            r = trilinear_lerp(v000, v100, v010, v110, v001, v101, v011, v111, wx, wy, wz);
-        }
-        const float2 vxy = __fadd2_rn(bxy, make_float2(r.x, r.y));
-        r = V3{vxy.x, vxy.y, bz + r.z};
         if (mode == JT_GRID_ZERO || mode == JT_GRID_NAN) {
             if (!(vx && vy && vz)) {
                 const float o = mode == JT_GRID_ZERO ? 0.0f : __int_as_float(0x7fc00000);

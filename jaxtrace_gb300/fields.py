@@ -384,7 +384,7 @@ class StructuredTimeSeriesField(_DeviceField):
 
     def __init__(self, data, times, grid_x, grid_y, grid_z, bounds_handling: str = "clamp",
                  interpolation: str = "linear", extrapolation: str = "constant", *,
-                 storage: str = "f32", time_semantics: str = "numpy", encoding: str = "snapshot"):
+                 storage: str = "f32", time_semantics: str = "numpy", encoding: str = "auto"):
         gx, gy, gz = _as_f32(grid_x), _as_f32(grid_y), _as_f32(grid_z)
         if gx.ndim != 1 or gy.ndim != 1 or gz.ndim != 1:
             raise ValueError("grid axes must be 1-D")
@@ -417,14 +417,17 @@ class StructuredTimeSeriesField(_DeviceField):
         self.y_min, self.y_max = float(gy[0]), float(gy[-1])
         self.z_min, self.z_max = float(gz[0]), float(gz[-1])
         self._mode = codes[mode]
-        # 16-bit encodings of the snapshots: "snapshot" -- every value over a
-        # per-snapshot power-of-two scale, read by every path; "tile" -- per
-        # tile of JT_TILE^3 cells a float32 affine base and 16-bit residuals,
-        # read by the pre-blended stage fields of track_particles (the other
-        # paths, which gather snapshot pairs, read float32 pairs then)
+        # 16-bit encodings of the snapshots: "tile" (the default for 16-bit
+        # storage) -- per tile of JT_TILE^3 cells a float32 affine base and
+        # 16-bit residuals, read by the pre-blended stage fields of
+        # track_particles (the paths that gather snapshot pairs read float32
+        # pairs then); "snapshot" -- every value over a per-snapshot
+        # power-of-two scale, read by every path
         enc = str(encoding).lower()
+        if enc == "auto":
+            enc = "snapshot" if self._storage == L.JT_STORE_F32 else "tile"
         if enc not in ("snapshot", "tile"):
-            raise ValueError(f"encoding must be 'snapshot' or 'tile', got {encoding!r}")
+            raise ValueError(f"encoding must be 'auto', 'snapshot' or 'tile', got {encoding!r}")
         if enc == "tile" and self._storage == L.JT_STORE_F32:
             raise ValueError("the tile encoding is a 16-bit storage (storage='bf16' or 'f16')")
         self.encoding = enc
@@ -477,7 +480,11 @@ class StructuredTimeSeriesField(_DeviceField):
             g.pairs = res.data_ptr()
             g.tile_base = base.data_ptr()
             g.tiles[:] = list(tiles)
-            self._tiles = {"res": res, "base": base, "tiles": tiles, "grid": g,
+            # per-snapshot max |v|: the bound the stage fields' scales come from
+            amax = np.abs(self.data.reshape(self.data.shape[0], -1)).max(axis=1).astype(np.float64)
+            if len(amax) == 1:
+                amax = np.repeat(amax, 2)
+            self._tiles = {"res": res, "base": base, "tiles": tiles, "grid": g, "amax": amax,
                            "field": L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))}
         return self._tiles["field"]
 
@@ -512,7 +519,7 @@ class StructuredGridSampler(StructuredTimeSeriesField):
     """Static trilinear sampler, structured.py:65 (velocity_data (Nx,Ny,Nz,3))."""
 
     def __init__(self, velocity_data, grid_x, grid_y, grid_z, bounds_handling: str = "clamp",
-                 grid_meta=None, *, storage: str = "f32"):
+                 grid_meta=None, *, storage: str = "f32", encoding: str = "auto"):
         v = _as_f32(velocity_data)
         if v.ndim != 4:
             raise ValueError(f"velocity_data must be 4D (Nx,Ny,Nz,3), got {v.shape}")
@@ -522,7 +529,7 @@ class StructuredGridSampler(StructuredTimeSeriesField):
             if _as_f32(g).shape != (n,):
                 raise ValueError(f"{name} shape {_as_f32(g).shape} doesn't match velocity_data")
         super().__init__(v[None], np.zeros(1, dtype=F32), grid_x, grid_y, grid_z, bounds_handling,
-                         storage=storage)
+                         storage=storage, encoding=encoding)
         self.velocity_data = v
         self.grid_meta = grid_meta
 

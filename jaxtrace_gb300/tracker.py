@@ -845,12 +845,12 @@ class _StageFields:
         self.ready = -1                                                     # last number blended
         self.tile = getattr(field, "encoding", "snapshot") == "tile"
         self.f32 = field._storage == L.JT_STORE_F32
-        if self.tile:
-            self.out_storage = L.JT_STORE_STAGE_TILE
-        else:
-            self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
+        self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
         scales = np.ones(len(src), dtype=F32)
-        if not self.f32 and not self.tile:
+        if self.tile:
+            field.tile_field()
+            scales = _tile_stage_scales(src, field._tiles["amax"])
+        elif not self.f32:
             scales = _stage_scales(src)
         # the tracking schedule: pair -> slot, weights -> the slot's scale
         stage = host.copy().reshape(n_steps, 4)
@@ -864,40 +864,31 @@ class _StageFields:
         self.sched = torch.from_numpy(stage.reshape(-1).view(np.int32).reshape(-1, 8).copy()).to(dev)
         self.src = torch.from_numpy(src.view(np.int32).reshape(-1, 8).copy()).to(dev)
         self.scales = torch.from_numpy(scales).to(dev)
-        self.bbuf = None
         if self.tile:
             self.src_field = field.tile_field()
             g0 = field._tiles["grid"]
-            tiles = int(g0.tiles[0]) * int(g0.tiles[1]) * int(g0.tiles[2])
-            nodes = tiles * L.JT_TILE_QUADS                                  # residual quads per slot
-            rec = 8                                                          # float32 words per quad
-            self.bbuf = torch.empty(self.slots * tiles * 16, dtype=torch.float32, device=dev)
-            self.tiles = tiles
         else:
             field._device()
             g0 = field._cgrid
-            nodes = int(g0.pair_stride)
-            rec = 4 if self.f32 else 8                                       # float32 words per node
-            self.tiles = 0
             self.src_field = field.jt_field()
+        nodes = len(field.grid_x) * len(field.grid_y) * len(field.grid_z)
+        rec = 4 if self.f32 else 8                                           # float32 words per node
         self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
         self.nodes, self.rec = nodes, rec
         self.n_fields = int(self.uid[-1]) + 1 if len(self.uid) else 0
-        self.field_bytes = nodes * rec * 4 + self.tiles * 64
+        self.field_bytes = nodes * rec * 4
         self.side = self.before = self.pending = None
         if self.overlap:
             self.side = torch.cuda.Stream(device=dev, priority=-1)
             self.buf.record_stream(self.side)
-            if self.bbuf is not None:
-                self.bbuf.record_stream(self.side)
         g = L.GridField()
         C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
         g.storage = self.out_storage
         g.n_pairs = self.slots
         g.pair_stride = nodes
         g.pairs = self.buf.data_ptr()
-        if self.bbuf is not None:
-            g.tile_base = self.bbuf.data_ptr()
+        g.tile_base = None
+        g.tiles[:] = [0, 0, 0]
         self.grid = g
         self.field_c = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
 
@@ -935,9 +926,8 @@ class _StageFields:
             sc = self.scales.data_ptr() + lo * 4
             out = self.buf.data_ptr() + (lo % self.slots) * self.nodes * self.rec * 4
             if self.tile:
-                ob = self.bbuf.data_ptr() + (lo % self.slots) * self.tiles * 64
-                L.check(self.lib.jt_stage_tile_fields(C.byref(self.src_field), C.c_void_p(ent), run,
-                                                      C.c_void_p(out), C.c_void_p(ob), stream))
+                L.check(self.lib.jt_stage_tile_fields(C.byref(self.src_field), C.c_void_p(ent), C.c_void_p(sc),
+                                                      run, C.c_void_p(out), stream))
                 continue
             L.check(self.lib.jt_stage_fields(C.byref(self.src_field), C.c_void_p(ent),
                                              C.c_void_p(None if self.f32 else sc), run, self.out_storage,
@@ -958,14 +948,7 @@ def _stage_numbers(entries) -> np.ndarray:
 
 def _stage_node_bytes(field) -> int:
     """Device bytes per grid node of one pre-blended stage field: float32
-    node records (16 B), float16 yz-quads (32 B), or affine tiles (80 residual
-    quads of 32 B and a 64 B base per 64 cells, about 41 B per node)."""
-    if getattr(field, "encoding", "snapshot") == "tile":
-        nodes = len(field.grid_x) * len(field.grid_y) * len(field.grid_z)
-        tiles = 1
-        for n in (len(field.grid_x), len(field.grid_y), len(field.grid_z)):
-            tiles *= (n + L.JT_TILE - 1) // L.JT_TILE
-        return -(-tiles * (L.JT_TILE_QUADS * 32 + 64) // nodes)
+    node records (16 B) or offset float16 yz-quads (32 B)."""
     return 16 if field._storage == L.JT_STORE_F32 else 32
 
 
@@ -1000,6 +983,21 @@ def _stage_plan(uid: np.ndarray, s: int, stop: int, ready: int, slots: int):
         runs.append((lo, run))
         lo += run
     return runs, hi - 1
+
+
+def _tile_stage_scales(src, amax) -> np.ndarray:
+    """Power-of-two bounds of |blend| for affine-tile snapshots, whose
+    entries carry plain weights: the larger of the pair's max |v| times
+    |wa| + |wb| (folded forms) or 1 + 2 |wb| (lerp forms)."""
+    n = len(amax)
+    p = np.clip(src["pair"].astype(np.int64), 0, n - 2)
+    m = np.maximum(amax[p], amax[p + 1])
+    wa = np.abs(src["wa"].astype(np.float64))
+    wb = np.abs(src["wb"].astype(np.float64))
+    lerp = (src["form"] == L.JT_BLEND_LERP_FWD) | (src["form"] == L.JT_BLEND_LERP_BWD)
+    bound = m * np.where(lerp, 1.0 + 2.0 * wb, wa + wb)
+    bound = np.where(np.isfinite(bound) & (bound > 0), bound, 1.0)
+    return np.exp2(np.ceil(np.log2(bound))).astype(F32)
 
 
 def _stage_scales(src) -> np.ndarray:

@@ -59,7 +59,7 @@ class OrcBoundary(C.Structure):
 
 class OrcRun(C.Structure):
     _fields_ = [("precision", i32), ("integrator", i32), ("step_times", vp), ("n_times", i32), ("dt", f64),
-                ("n_threads", i32), ("fallback_count", i64), ("wrapped_count", i64), ("reseed", vp)]
+                ("n_threads", i32), ("fallback_count", i64), ("wrapped_count", i64), ("cell_sig", vp), ("reseed", vp)]
 
 
 def build(force: bool = False) -> Path:
@@ -233,12 +233,15 @@ class FemSpec:
 
 
 def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F32, n_threads=0,
-          record=False, reseed=False):
+          record=False, reseed=False, cell_sig=False):
     """Run the oracle; returns (final positions, trajectory or None, run info).
     In float64 mode a float64 ``x0`` is used as given (no float32 rounding).
     With ``reseed`` the info holds ``"reseed"``: (n,3) int32, each particle's
     last continuous-inlet replacement (step, lattice index 0, lattice index 1),
-    -1 where the inlet never replaced it."""
+    -1 where the inlet never replaced it.  With ``cell_sig`` (float64 mode,
+    grid fields) the info holds ``"cell_sig"``: (n,) uint64, a hash of the
+    cells every field evaluation fell in (a difference quotient whose two
+    runs share it never straddles a cell face)."""
     lib = load()
     x64 = None
     if precision == ORC_F64 and np.asarray(x0).dtype == np.float64:
@@ -253,6 +256,8 @@ def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F
     traj = np.zeros((len(st), n, 3), np.float32) if (record and precision == ORC_F32) else None
     ev = np.full((n, 3), -1, np.int32) if reseed else None
     r.reseed = _p(ev)
+    sig = np.zeros(n, np.uint64) if (cell_sig and precision == ORC_F64) else None
+    r.cell_sig = _p(sig)
     rc = lib.orc_track(C.byref(field.c), C.byref(boundary.c), C.byref(r), n, x0.ctypes.data, _p(out32), _p(out64),
                        _p(traj), _p(x64))
     if rc != 0:
@@ -261,6 +266,8 @@ def track(field, boundary, x0, step_times, dt, integrator="rk4", precision=ORC_F
     info = {"fallback_count": int(r.fallback_count), "wrapped_count": int(r.wrapped_count)}
     if reseed:
         info["reseed"] = ev
+    if sig is not None:
+        info["cell_sig"] = sig
     return out, traj, info
 
 

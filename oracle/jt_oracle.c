@@ -87,6 +87,10 @@ typedef struct {
     int n_threads;
     int64_t fallback_count;  /* out: octree fallback lookups */
     int64_t wrapped_count;   /* out: periodic index == N events */
+    uint64_t* cell_sig;      /* optional out (n), float64 mode, grid fields:
+                                a hash of the sequence of cells every field
+                                evaluation of the particle falls in (equal
+                                for two runs that visit the same cells) */
     int32_t* reseed;         /* optional out (n,3): the last continuous-inlet
                                 replacement of each particle -- its step and
                                 the lattice indices it snapped to; -1 if none */
@@ -780,28 +784,47 @@ static void step_f(const orc_field* F, const orc_run* R, int s, float* x, int64_
     }
 }
 
-static void step_d(const orc_field* F, const orc_run* R, int s, double* x, int64_t* fb) {
+/* Fold the grid cell of p into a running signature (grid fields only). */
+static void cell_sig_d(const orc_field* F, const double* p, uint64_t* sig) {
+    if (sig == NULL || F->kind != FIELD_GRID) return;
+    int i0, i1, j0, j1, k0, k1, v;
+    double w;
+    grid_axis_d(F, 0, p[0], &i0, &i1, &w, &v);
+    grid_axis_d(F, 1, p[1], &j0, &j1, &w, &v);
+    grid_axis_d(F, 2, p[2], &k0, &k1, &w, &v);
+    const uint64_t c = ((uint64_t)(uint32_t)i0 << 42) ^ ((uint64_t)(uint32_t)j0 << 21) ^ (uint64_t)(uint32_t)k0;
+    *sig ^= c + 0x9e3779b97f4a7c15ULL + (*sig << 6) + (*sig >> 2);
+}
+
+static void step_d(const orc_field* F, const orc_run* R, int s, double* x, int64_t* fb, uint64_t* sig) {
     const double tj = R->step_times[s];
     const double dt = (double)(float)R->dt;
     double k1[3], k2[3], k3[3], k4[3], xs[3];
     if (R->integrator == IN_RK4) {
         const stime s0 = {tj, 1}, sh = {tj + 0.5 * dt, 1}, sf = {tj + dt, 1};
+        cell_sig_d(F, x, sig);
         field_d(F, s0, x, k1, fb);
         for (int a = 0; a < 3; ++a) xs[a] = x[a] + 0.5 * dt * k1[a];
+        cell_sig_d(F, xs, sig);
         field_d(F, sh, xs, k2, fb);
         for (int a = 0; a < 3; ++a) xs[a] = x[a] + 0.5 * dt * k2[a];
+        cell_sig_d(F, xs, sig);
         field_d(F, sh, xs, k3, fb);
         for (int a = 0; a < 3; ++a) xs[a] = x[a] + dt * k3[a];
+        cell_sig_d(F, xs, sig);
         field_d(F, sf, xs, k4, fb);
         for (int a = 0; a < 3; ++a) x[a] += dt / 6.0 * (k1[a] + 2.0 * k2[a] + 2.0 * k3[a] + k4[a]);
     } else if (R->integrator == IN_RK2) {
         const stime s0 = {tj, 0}, sm = {tj + 0.5 * dt, 0};
+        cell_sig_d(F, x, sig);
         field_d(F, s0, x, k1, fb);
         for (int a = 0; a < 3; ++a) xs[a] = x[a] + 0.5 * dt * k1[a];
+        cell_sig_d(F, xs, sig);
         field_d(F, sm, xs, k2, fb);
         for (int a = 0; a < 3; ++a) x[a] += dt * k2[a];
     } else {
         const stime s0 = {tj, 0};
+        cell_sig_d(F, x, sig);
         field_d(F, s0, x, k1, fb);
         for (int a = 0; a < 3; ++a) x[a] += dt * k1[a];
     }
@@ -840,13 +863,15 @@ int orc_track(const orc_field* F, const orc_boundary* B, orc_run* R, int n, cons
         } else {
             double x[3];
             for (int a = 0; a < 3; ++a) x[a] = x0_f64 ? x0_f64[3 * (size_t)i + a] : (double)x0[3 * (size_t)i + a];
+            uint64_t sig = 0;
             for (int s = 0; s + 1 < T; ++s) {
                 int ev[2] = {-1, -1};
-                step_d(F, R, s, x, &fb);
+                step_d(F, R, s, x, &fb, R->cell_sig ? &sig : NULL);
                 boundary_d(B, lat[0], lat[1], x, ev);
                 if (ev[0] >= 0) { last[0] = s; last[1] = ev[0]; last[2] = ev[1]; }
             }
             out_f64[3 * (size_t)i] = x[0]; out_f64[3 * (size_t)i + 1] = x[1]; out_f64[3 * (size_t)i + 2] = x[2];
+            if (R->cell_sig) R->cell_sig[i] = sig;
         }
         if (R->reseed) memcpy(R->reseed + 3 * (size_t)i, last, sizeof last);
     }

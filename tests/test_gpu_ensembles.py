@@ -97,7 +97,7 @@ def test_ensembles_16bit_storage_close_to_oracle():
     f, spec, bc, obc = _grid_case()
     g = (np.arange(16) / 16).astype(F32)
     st = f.times
-    f16 = jt.StructuredTimeSeriesField(f.data, st, g, g, g, "periodic", storage="bf16")
+    f16 = jt.StructuredTimeSeriesField(f.data, st, g, g, g, "periodic", storage="bf16", encoding="snapshot")
     xs, rel = _ensembles([500, 1500], seed=4)
     outs = jt.create_tracker("rk4", f16, bc, sort_every=0).track_ensembles(xs, rel, 21, dt=0.01)
     for x, t0, out in zip(xs, rel, outs):

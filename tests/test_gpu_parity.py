@@ -292,7 +292,7 @@ def test_16bit_sampler_matches_oracle_on_quantized_values(golden, storage, mode)
     of the field's largest magnitude."""
     g = golden("structured")
     V, gx, gy, gz, q = (g[f"{mode}_{k}"] for k in ("V", "gx", "gy", "gz", "q"))
-    s = jt.StructuredGridSampler(V, gx, gy, gz, mode, storage=storage)
+    s = jt.StructuredGridSampler(V, gx, gy, gz, mode, storage=storage, encoding="snapshot")
     out = s.sample(q)
     Vq = _quantize(V[None], storage)
     ref, _ = oracle.sample(oracle.GridSpec(Vq, np.zeros(1, F32), gx, gy, gz, mode), q, 0.0)
@@ -303,13 +303,14 @@ def test_16bit_sampler_matches_oracle_on_quantized_values(golden, storage, mode)
 @pytest.mark.parametrize("storage", ["bf16", "f16"])
 def test_16bit_tracking_matches_oracle_on_quantized_values(storage, stage):
     """Pair gathers (stage False) and float16 stage fields (stage True) on
-    BF16/FP16 snapshots against the float32 oracle on the quantized values.
-    Stage fields round the blended node values once more to float16 (at most
-    2^-12 of the field's power-of-two bound), so they get 3e-4 absolute."""
+    BF16/FP16 snapshots (the per-snapshot-scale encoding) against the float32
+    oracle on the quantized values.  Stage fields round the blended values'
+    residuals from their quad's offset to float16 and interpolate them in
+    float16, so they get 3e-4 absolute."""
     from jaxtrace_gb300 import workloads as W
     c = W.precision_case(n=20, n_snap=6, seeds=(16, 16, 16), lattice=16, n_steps=25, dt=0.01)
     g = c["grid"][0]
-    f = jt.StructuredTimeSeriesField(c["data"], c["times"], g, g, g, "clamp", storage=storage)
+    f = jt.StructuredTimeSeriesField(c["data"], c["times"], g, g, g, "clamp", storage=storage, encoding="snapshot")
     bc = jt.continuous_inlet_boundary_factory(W.UNIT, "x", "positive", "grid", c["concentrations"])
     traj = jt.create_tracker("rk4", f, bc, record_final_only=True, stage_fields=stage).track_particles(
         c["x0"], c["time_span"], c["n_timesteps"], dt=c["dt"])

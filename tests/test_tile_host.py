@@ -141,7 +141,7 @@ def test_stage_ring_sizes():
     g = np.linspace(0, 1, 128, dtype=np.float32)
     data = np.zeros((2, 128 ** 3, 3), np.float32)
     f = F.StructuredTimeSeriesField(data, np.array([0, 1], np.float32), g, g, g, storage="bf16", encoding="tile")
-    assert _stage_node_bytes(f) == 41          # 80 quads of 32 B and 64 B of base per 64 nodes
+    assert _stage_node_bytes(f) == 32          # one offset quad per node, as the per-snapshot scale
     f2 = F.StructuredTimeSeriesField(data, np.array([0, 1], np.float32), g, g, g, storage="bf16")
     assert _stage_node_bytes(f2) == 32
     with pytest.raises(ValueError, match="16-bit"):
