@@ -69,6 +69,12 @@ def args_parse():
     p.add_argument("--leg", default=None, choices=["fem", "fem_hash", "batch", "adjoint", "density"],
                    help="run one configuration leg alone and print its JSON (with --profile: the leg's timed "
                         "region bracketed by cudaProfilerStart/Stop)")
+    p.add_argument("--ncu-summary", action="store_true",
+                   help="write profiles/k_track_precision.json from ncu csv logs (--ncu-dram/--ncu-inst) and exit")
+    p.add_argument("--ncu-dram", action="append", default=[], help="KEY=CSV: full-size DRAM bytes capture")
+    p.add_argument("--ncu-inst", action="append", default=[], help="KEY=CSV: small-case instruction capture")
+    p.add_argument("--ncu-steps", type=int, default=32, help="steps per captured tracking launch")
+    p.add_argument("--ncu-command", action="append", default=[], help="a capture command, recorded as given")
     p.add_argument("--profile", action="store_true",
                    help="first variant only, no error/e2e/CPU legs; the timed region is bracketed by "
                         "cudaProfilerStart/Stop for ncu --profile-from-start off")
@@ -784,14 +790,89 @@ def subset_events(tr, x0_sub, case, lat):
     return pos[-1].copy(), reseed_events(pos, lat)
 
 
+CAPTURE_JSON = ROOT / "profiles" / "k_track_precision.json"
+
+
+def capture_key(v):
+    """Variants that launch the same tracking kernel share one capture: every
+    16-bit storage and encoding gathers the same float16 offset quads."""
+    return "16bit" if VARIANTS[v][0] != "f32" else v
+
+
 def captured_figures():
-    """ncu figures of k_track per variant from the committed capture summary
-    (profiles/k_track_precision.json): DRAM bytes per particle-step and warp
-    instructions per warp-step, with the capture's command and date."""
-    f = ROOT / "profiles" / "k_track_precision.json"
-    if not f.exists():
+    """ncu figures of k_track per kernel from the committed capture summary
+    (profiles/k_track_precision.json, written by --ncu-summary): DRAM bytes
+    per particle-step at full size and warp instructions per warp-step, with
+    the capture's commands, date and commit."""
+    if not CAPTURE_JSON.exists():
         return {}
-    return json.loads(f.read_text())
+    return json.loads(CAPTURE_JSON.read_text())
+
+
+def _ncu_rows(path):
+    """Rows of an ncu --csv log: one dict per (launch, metric)."""
+    import csv
+    rows, hdr = [], None
+    for r in csv.reader(open(path)):
+        if "Metric Name" in r and "Kernel Name" in r:
+            hdr = r
+            continue
+        if hdr is not None and len(r) == len(hdr):
+            rows.append(dict(zip(hdr, r)))
+    return rows
+
+
+def _ncu_launches(path):
+    """{launch id: {metric: value}} of the k_track launches in an ncu csv."""
+    out = {}
+    for r in _ncu_rows(path):
+        if "k_track" not in r["Kernel Name"]:
+            continue
+        try:
+            v = float(r["Metric Value"].replace(",", ""))
+        except ValueError:
+            continue
+        unit = r.get("Metric Unit", "")
+        scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "nsecond": 1e-9, "usecond": 1e-6,
+                 "msecond": 1e-3, "second": 1.0, "ns": 1e-9, "us": 1e-6, "ms": 1e-3, "s": 1.0}.get(unit, 1.0)
+        out.setdefault(r["ID"], {})[r["Metric Name"]] = v * scale
+    return out
+
+
+def ncu_summary(a):
+    """Write profiles/k_track_precision.json from ncu csv logs of the tracking
+    kernel: --ncu-dram KEY=CSV (full-size 1-pass DRAM bytes and duration) and
+    --ncu-inst KEY=CSV (small-case warp instructions), KEY one of 16bit, f32,
+    f32c; every captured launch advances --ncu-steps steps of grid x block
+    particles."""
+    import datetime
+    out = {"kernel": "jt::k_track<EXACT, JT_RK4, 0, StageGridField<EXACT, STAGE_F32Q|STAGE_F16, CLAMP>>",
+           "date": datetime.date.today().isoformat(),
+           "commit": subprocess.run(["git", "rev-parse", "--short", "HEAD"], capture_output=True, text=True,
+                                    cwd=ROOT).stdout.strip() or None,
+           "steps_per_launch": a.ncu_steps, "commands": a.ncu_command or [], "variants": {}}
+    for spec, kind in [(s, "dram") for s in a.ncu_dram] + [(s, "inst") for s in a.ncu_inst]:
+        key, path = spec.split("=", 1)
+        ent = out["variants"].setdefault(key, {})
+        L = list(_ncu_launches(path).values())
+        parts = [m["launch__grid_size"] * m["launch__block_size"] for m in L]
+        if kind == "dram":
+            b = [(m["dram__bytes_read.sum"] + m["dram__bytes_write.sum"]) / (p * a.ncu_steps) for m, p in zip(L, parts)]
+            ent["dram_bytes_per_particle_step"] = float(np.mean(b))
+            ent["dram_capture"] = {"launches": len(L), "particles": int(parts[0]),
+                                   "dram_bytes_per_launch": [m["dram__bytes_read.sum"] + m["dram__bytes_write.sum"]
+                                                             for m in L],
+                                   "duration_ms": [m["gpu__time_duration.sum"] * 1e3 for m in L]}
+        else:
+            w = [m["smsp__inst_executed.sum"] / (p / 32.0 * a.ncu_steps) for m, p in zip(L, parts)]
+            ent["warp_inst_per_warp_step"] = float(np.mean(w))
+            ent["inst_capture"] = {"launches": len(L), "particles": int(parts[0]),
+                                   "issue_active_pct": [m.get("smsp__issue_active.avg.pct_of_peak_sustained_active")
+                                                        for m in L],
+                                   "l1tex_throughput_pct": [m.get("l1tex__throughput.avg.pct_of_peak_sustained_active")
+                                                            for m in L]}
+    CAPTURE_JSON.write_text(json.dumps(out, indent=1) + "\n")
+    print(json.dumps(out, indent=1))
 
 
 def roofline_of(v, r, n, peak, from_peaks, cap):
@@ -820,8 +901,8 @@ def roofline_of(v, r, n, peak, from_peaks, cap):
            "fallback 6800 GB/s", "kernel": f"k_track (RK4, stage grid field, {v})", "launch_ms": r["launch_ms"],
            "particle_steps_per_launch": units, "algorithmic_bytes_per_launch": alg,
            "cache_oblivious_gbs": co}
-    c = cap.get("variants", {}).get(v)
-    if c:
+    c = cap.get("variants", {}).get(capture_key(v))
+    if c and "dram_bytes_per_particle_step" in c and "warp_inst_per_warp_step" in c:
         out["traffic"] = c["dram_bytes_per_particle_step"] * units
         out["dram_frac"] = out["traffic"] / sec / 1e9 / peak
         out["issue"] = {"warp_inst_per_warp_step": c["warp_inst_per_warp_step"],
@@ -833,6 +914,9 @@ def roofline_of(v, r, n, peak, from_peaks, cap):
 
 def main():
     a = args_parse()
+    if a.ncu_summary:
+        ncu_summary(a)
+        return
     world, rank, local = dist_setup()
     if a.impl == "reference":
         run_reference(a, world, rank)

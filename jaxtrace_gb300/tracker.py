@@ -816,9 +816,10 @@ class _StageFields:
     times agree) takes the same number u.  Entry u lives in ring slot
     u mod R; the entries of a launch of at most ``chunk`` steps span at most
     3 * chunk numbers, so ``prepare`` finds room for all of them with
-    R = 3 * chunk.  Float32 snapshots give float32 node records blended with
-    the exact arithmetic; 16-bit snapshots give float16 yz-quads divided by a
-    power-of-two bound of the blend.
+    R = 3 * chunk.  Float32 snapshots give float32 yz-quads blended with the
+    exact arithmetic; 16-bit snapshots (per-snapshot scale or affine tiles)
+    give offset float16 yz-quads of the blend divided by a power-of-two bound
+    of it.
 
     Overlap (R = 6 * chunk): ``prefetch`` blends the next launch's fields on a
     side stream while the current launch tracks.  Its writes go to the slots

@@ -350,7 +350,47 @@ def phase_analytics(ref: str):
     print("phase analytics: done")
 
 
-PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem, "analytics": phase_analytics}
+def phase_steps(ref: str):
+    """The standalone step functions (integrators/rk4.py:62-129,
+    rk2.py:117-180, euler.py:111-157) on the trilinear + linear-time field,
+    with a scalar dt and with a per-particle dt (mean-dt stage times), at a
+    float32 time, a Python float time and a time between snapshots."""
+    sys.path.insert(0, ref)
+    import warnings
+    warnings.simplefilter("ignore")
+    from jaxtrace.fields.structured import StructuredGridSampler
+    from jaxtrace.fields.time_series import TimeSeriesField
+    from jaxtrace.integrators.euler import euler_step
+    from jaxtrace.integrators.rk2 import rk2_step
+    from jaxtrace.integrators.rk4 import rk4_step
+    from jaxtrace.utils.jax_utils import JAX_AVAILABLE
+    assert not JAX_AVAILABLE, "phase steps must run without jax"
+    n = 12
+    g = (np.arange(n) / n).astype(F32)
+    nodes = grid_nodes(g, g, g)
+    st = np.linspace(0, 1, 8).astype(F32)
+    D = np.stack([abc(nodes, float(t)) for t in st]).astype(F32)
+    ts = TimeSeriesField(data=D, times=st, positions=nodes)
+
+    def field(p, t):
+        V = np.asarray(ts.sample_at_time(t)).reshape(n, n, n, 3)
+        return StructuredGridSampler(V, g, g, g, bounds_handling="periodic").sample(p)
+
+    rng = np.random.default_rng(77)
+    # positions away from the periodic seam, so no stage lands in (-4e-8, 0)
+    x = rng.uniform(0.05, 0.95, (256, 3)).astype(F32)
+    dt_pp = rng.uniform(0.002, 0.02, 256).astype(F32)
+    out = {"D": D, "st": st, "g": g, "x": x, "dt_pp": dt_pp, "times": np.array([0.13, 0.5, 0.71])}
+    for name, fn in (("rk4", rk4_step), ("rk2", rk2_step), ("euler", euler_step)):
+        for k, t in enumerate((0.13, 0.5, 0.71)):
+            tf = np.float32(t) if k == 0 else t       # a float32 time and Python float times
+            out[f"{name}_scalar_{k}"] = np.asarray(fn(x, tf, 0.01, field), dtype=F32)
+            out[f"{name}_pp_{k}"] = np.asarray(fn(x, tf, dt_pp, field), dtype=F32)
+    np.savez_compressed(HERE / "steps.npz", **out)
+
+
+PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem, "analytics": phase_analytics,
+          "steps": phase_steps}
 
 if __name__ == "__main__":
     if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
