@@ -21,7 +21,7 @@ JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STA
 JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
 JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2
 JT_STORE_STAGE_F32, JT_STORE_STAGE_F16 = 3, 4
-JT_STORE_TILE_BF16, JT_STORE_TILE_F16 = 5, 6
+JT_STORE_TILE_BF16, JT_STORE_TILE_F16, JT_STORE_STAGE_F32Q = 5, 6, 8
 JT_TILE, JT_TILE_NODES = 4, 125
 JT_GRID_CLAMP, JT_GRID_ZERO, JT_GRID_NAN, JT_GRID_PERIODIC = 0, 1, 2, 3
 JT_BLEND_WEIGHTED, JT_BLEND_LERP_FWD, JT_BLEND_LERP_BWD, JT_BLEND_SAME_A, JT_BLEND_SAME_B = 0, 1, 2, 3, 4

@@ -90,7 +90,9 @@ static int check_field(const jt_field* f) {
                 return set_error(JT_ERR_UNSUPPORTED, "affine-tile snapshots are read by jt_stage_tile_fields only");
             if (g->pair_stride < (int64_t)g->nx * g->ny * g->nz)
                 return set_error(JT_ERR_INVALID, "pair_stride smaller than the node count");
-            if (g->storage == JT_STORE_STAGE_F32 || g->storage == JT_STORE_STAGE_F16) return JT_OK;
+            if (g->storage == JT_STORE_STAGE_F32 || g->storage == JT_STORE_STAGE_F16 ||
+                g->storage == JT_STORE_STAGE_F32Q)
+                return JT_OK;
             return check_storage(g->storage);
         }
         case JT_FIELD_MESH: {

@@ -6,7 +6,8 @@ namespace jt {
 typedef Launcher<GridField, jt_grid_field, int> GridL;
 
 int grid_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
-    if (f.storage == JT_STORE_STAGE_F32 || f.storage == JT_STORE_STAGE_F16) return stage_track(f, b, p, s);
+    if (f.storage == JT_STORE_STAGE_F32 || f.storage == JT_STORE_STAGE_F16 || f.storage == JT_STORE_STAGE_F32Q)
+        return stage_track(f, b, p, s);
     return GridL::track(f, 0, f.storage, b, p, s);
 }
 int grid_step(const jt_grid_field& f, int arith, const StageBlends& sb, int integ, StepConst k,

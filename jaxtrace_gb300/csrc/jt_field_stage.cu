@@ -34,6 +34,46 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(jt_grid_field F, const jt_
     }
 }
 
+// float32 pairs -> float32 yz-quads (JT_STORE_STAGE_F32Q), one thread per
+// node: its quad's four nodes (j,k), (j,k1), (j1,k), (j1,k1) blended with
+// the exact arithmetic of k_stage_f32, so the values are the same bits.
+template <bool EXACT>
+__global__ void __launch_bounds__(kBlock) k_stage_f32q(jt_grid_field F, const jt_blend* __restrict__ ent, int n,
+                                                        char* __restrict__ out) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t N = F.pair_stride;
+    if (node >= N) return;
+    const int k = (int)(node % F.nz);
+    const int j = (int)((node / F.nz) % F.ny);
+    const bool per = F.bounds_mode == JT_GRID_PERIODIC;
+    // successors as the sampler computes them (structured.py:311-318)
+    const int k1 = per ? (k + 1 == F.nz ? 0 : k + 1) : min(k + 1, F.nz - 1);
+    const int j1 = per ? (j + 1 == F.ny ? 0 : j + 1) : min(j + 1, F.ny - 1);
+    const int64_t row = node - k - (int64_t)j * F.nz;       // node (i, 0, 0)
+    const int64_t ids[4] = {node, row + (int64_t)j * F.nz + k1, row + (int64_t)j1 * F.nz + k,
+                            row + (int64_t)j1 * F.nz + k1};
+    int cur = -1;
+    PairVal pv[4];
+    for (int jj = 0; jj < n; ++jj) {
+        const jt_blend e = ent[jj];
+        const int pr = min(max(e.pair, 0), F.n_pairs - 1);
+        if (pr != cur) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) pv[c] = load_pair<JT_STORE_F32>(F.pairs, (int64_t)pr * N + ids[c]);
+            cur = pr;
+        }
+        CV v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            v[c] = blend_cv<EXACT, JT_STORE_F32>(pv[c], e, splat(e.wa), splat(e.wb), e.form == JT_BLEND_WEIGHTED);
+        char* slot = out + (int64_t)jj * N * 48;
+        float4* a = reinterpret_cast<float4*>(slot + node * 32);
+        a[0] = make_float4(v[0].xy.x, v[0].xy.y, v[1].xy.x, v[1].xy.y);
+        a[1] = make_float4(v[2].xy.x, v[2].xy.y, v[3].xy.x, v[3].xy.y);
+        reinterpret_cast<float4*>(slot + N * 32)[node] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
+    }
+}
+
 __device__ __forceinline__ CV scale_cv(CV c, float s) {
     return CV{make_float2(c.xy.x * s, c.xy.y * s), c.z * s};
 }
@@ -230,12 +270,15 @@ static cudaError_t stage_launch(const jt_grid_field& f, const jt_boundary& b, co
     if (f.storage == JT_STORE_STAGE_F32)
         return exact ? L::template track_s<true, JT_STORE_STAGE_F32>(f, 0, b, p, s)
                      : L::template track_s<false, JT_STORE_STAGE_F32>(f, 0, b, p, s);
+    if (f.storage == JT_STORE_STAGE_F32Q)
+        return exact ? L::template track_s<true, JT_STORE_STAGE_F32Q>(f, 0, b, p, s)
+                     : L::template track_s<false, JT_STORE_STAGE_F32Q>(f, 0, b, p, s);
     return L::template track_s<false, JT_STORE_STAGE_F16>(f, 0, b, p, s);
 }
 
 int stage_track(const jt_grid_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s) {
     const bool exact = p.arith == JT_ARITH_EXACT;
-    if (f.storage != JT_STORE_STAGE_F32 && exact)
+    if (f.storage == JT_STORE_STAGE_F16 && exact)
         return set_error(JT_ERR_UNSUPPORTED, "exact arithmetic needs float32 stage fields");
     cudaError_t err;
     switch (f.bounds_mode) {
@@ -265,7 +308,11 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     const unsigned g = grid_blocks(N);
     const unsigned g16 = (unsigned)((N + kStageBlock16 - 1) / kStageBlock16);
     cudaStream_t s = (cudaStream_t)stream;
-    if (out_storage == JT_STORE_STAGE_F32) {
+    if (out_storage == JT_STORE_STAGE_F32Q) {
+        if (F.storage != JT_STORE_F32)
+            return set_error(JT_ERR_UNSUPPORTED, "float32 stage fields come from float32 snapshots");
+        k_stage_f32q<true><<<g, kBlock, 0, s>>>(F, entries, n, reinterpret_cast<char*>(out));
+    } else if (out_storage == JT_STORE_STAGE_F32) {
         if (F.storage != JT_STORE_F32)
             return set_error(JT_ERR_UNSUPPORTED, "float32 stage fields come from float32 snapshots");
         k_stage_f32<true><<<g, kBlock, 0, s>>>(F, entries, n, reinterpret_cast<float4*>(out));
@@ -280,7 +327,7 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
         else
             return set_error(JT_ERR_UNSUPPORTED, "float16 stage fields come from 16-bit snapshots");
     } else {
-        return set_error(JT_ERR_INVALID, "out_storage must be JT_STORE_STAGE_F32 or JT_STORE_STAGE_F16");
+        return set_error(JT_ERR_INVALID, "out_storage must be JT_STORE_STAGE_F32, _F32Q or _F16");
     }
     return cuda_status(cudaGetLastError(), "stage field launch");
 }

@@ -846,7 +846,7 @@ class _StageFields:
         self.ready = -1                                                     # last number blended
         self.tile = getattr(field, "encoding", "snapshot") == "tile"
         self.f32 = field._storage == L.JT_STORE_F32
-        self.out_storage = L.JT_STORE_STAGE_F32 if self.f32 else L.JT_STORE_STAGE_F16
+        self.out_storage = L.JT_STORE_STAGE_F32Q if self.f32 else L.JT_STORE_STAGE_F16
         scales = np.ones(len(src), dtype=F32)
         if self.tile:
             field.tile_field()
@@ -873,7 +873,7 @@ class _StageFields:
             g0 = field._cgrid
             self.src_field = field.jt_field()
         nodes = len(field.grid_x) * len(field.grid_y) * len(field.grid_z)
-        rec = 4 if self.f32 else 8                                           # float32 words per node
+        rec = 12 if self.f32 else 8                                          # float32 words per node
         self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
         self.nodes, self.rec = nodes, rec
         self.n_fields = int(self.uid[-1]) + 1 if len(self.uid) else 0
@@ -949,8 +949,8 @@ def _stage_numbers(entries) -> np.ndarray:
 
 def _stage_node_bytes(field) -> int:
     """Device bytes per grid node of one pre-blended stage field: float32
-    node records (16 B) or offset float16 yz-quads (32 B)."""
-    return 16 if field._storage == L.JT_STORE_F32 else 32
+    yz-quads (48 B) or offset float16 yz-quads (32 B)."""
+    return 48 if field._storage == L.JT_STORE_F32 else 32
 
 
 def _stage_chunk(chunk: int, n_steps: int, nodes: int, rec_bytes: int, free_bytes: int) -> int:
