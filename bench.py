@@ -624,8 +624,59 @@ def density_part(P, profile):
     sph_ms = _timed(lambda: sph._density_sum(P), 1)
     kde_ms = _timed(kde.evaluate_3d, 1)
     n = int(P.shape[0])
-    return {"particles": n, "sph_ms": sph_ms, "sph_queries_per_s": n / (sph_ms / 1e3),
-            "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3", "kde_particles_per_s": n / (kde_ms / 1e3)}
+    out = {"particles": n, "sph_ms": sph_ms, "sph_queries_per_s": n / (sph_ms / 1e3),
+           "kde_ms": kde_ms, "kde_bandwidth": kde.h, "kde_grid": "100^3", "kde_particles_per_s": n / (kde_ms / 1e3)}
+    out["roofline"] = density_roofline(sph, kde, P, sph_ms, kde_ms)
+    return out
+
+
+def density_roofline(sph, kde, P, sph_ms, kde_ms):
+    """Work counts of the two density passes from one untimed counting run
+    each (the kernels' counting instances), against the timed runs:
+
+    SPH: candidate pairs examined (each a distance: 3 subtractions, 2 FMAs,
+    1 multiply, a compare) and pairs inside the cubic spline's support (a
+    reciprocal square root and about 8 flops of the polynomial and the
+    accumulation), as pairs/s and as FP32 flop/s against the FP32 FMA peak
+    (SMs x 128 lanes x 2 flops x clock).
+
+    KDE: (particle, tile) visits of the separable 8^3 tiles, each 24
+    exponentials (8 per axis) and 512 FMAs, as exponentials/s against the
+    SFU rate (SMs x 16 per clock) and (grid point, particle) terms/s against
+    the FP32 FMA peak.
+
+    HBM: the compulsory bytes (particles, queries and outputs read or
+    written once) over the time."""
+    import torch
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sms = props.multi_processor_count
+    mhz = 2070.0
+    fma_peak = sms * 128 * 2 * mhz * 1e6
+    sfu_peak = sms * 16 * mhz * 1e6
+    c = torch.zeros(2, dtype=torch.int64, device="cuda")
+    sph.count_into = c
+    sph._density_sum(P)
+    torch.cuda.synchronize()
+    sph.count_into = None
+    cand, inside = (int(v) for v in c.cpu())
+    c.zero_()
+    kde.count_into = c
+    kde.evaluate_3d()
+    torch.cuda.synchronize()
+    kde.count_into = None
+    visits, terms = (int(v) for v in c.cpu())
+    n = int(P.shape[0])
+    ss, ks = sph_ms / 1e3, kde_ms / 1e3
+    sph_flops = 8 * cand + 10 * inside
+    kde_exp = 24 * visits
+    return {"clock_mhz_assumed": mhz, "fp32_fma_peak_flops": fma_peak, "sfu_peak_per_s": sfu_peak,
+            "sph": {"candidate_pairs": cand, "pairs_in_support": inside,
+                    "pairs_in_support_per_query": inside / n, "candidate_pairs_per_s": cand / ss,
+                    "flops_per_s": sph_flops / ss, "fp32_frac": sph_flops / ss / fma_peak,
+                    "hbm_gbs": (n * 16 + n * 12 + n * 8) / ss / 1e9},
+            "kde": {"tile_visits": visits, "terms": terms, "exp_per_s": kde_exp / ks, "sfu_frac": kde_exp / ks / sfu_peak,
+                    "terms_per_s": terms / ks, "fma_frac": terms * 2 / ks / fma_peak,
+                    "hbm_gbs": (n * 12 + 100 ** 3 * 8) / ks / 1e9}}
 
 
 def analytics_part(a, case, g, bc, x0_dev, times, plain_ms, variant):

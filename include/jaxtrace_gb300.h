@@ -525,6 +525,11 @@ typedef struct {
     const uint32_t* cell_end;  /* device, from jt_cell_list                  */
     const float* queries;      /* device (M,3)                               */
     double* out;               /* device (M): sum_j m_j W(|q - p_j|, h_j)    */
+    unsigned long long* counters; /* device [2] or NULL: when set, the call adds
+                                  the candidate pairs it examined and the
+                                  pairs inside the kernel's support (uniform
+                                  h, packed records only; a counting
+                                  instance of the kernel, for measurement) */
 } jt_sph_params;
 
 /* SPH density at M query points: _evaluate_density (density/sph.py:269-292)
@@ -545,6 +550,10 @@ typedef struct {
     const float* particles;    /* device (N,3) in cell order                  */
     const uint32_t* cell_end;  /* device, from jt_cell_list                   */
     double* out;               /* device: grid (x index i, y index j, z index k) at (i*res_y + j)*res_z + k */
+    unsigned long long* counters; /* device [2] or NULL (3-D grids): when set,
+                                  the call adds the (particle, tile) visits of
+                                  its 8^3 tiles and the (grid point,
+                                  particle) kernel terms they sum          */
 } jt_kde_params;
 
 /* Gaussian KDE on a tensor grid: out = sum_j exp(-|g - p_j|^2 h^-2 / 2) at

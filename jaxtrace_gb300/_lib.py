@@ -118,12 +118,13 @@ JT_SPH_CUBIC, JT_SPH_WENDLAND, JT_SPH_GAUSSIAN = 0, 1, 2
 class SphParams(C.Structure):
     _fields_ = [("dims", i32), ("kernel", i32), ("n_particles", i32), ("n_queries", i32), ("radius", f32),
                 ("h_const", f32), ("grid", SortGrid), ("reach", i32 * 3), ("packed", i32), ("particles", vp),
-                ("masses", vp), ("h", vp), ("cell_end", vp), ("queries", vp), ("out", vp)]
+                ("masses", vp), ("h", vp), ("cell_end", vp), ("queries", vp), ("out", vp), ("counters", vp)]
 
 
 class KdeParams(C.Structure):
     _fields_ = [("dims", i32), ("n_particles", i32), ("res", i32 * 3), ("half_inv_h2", f32), ("radius", f32),
-                ("grid", SortGrid), ("axis", vp * 3), ("particles", vp), ("cell_end", vp), ("out", vp)]
+                ("grid", SortGrid), ("axis", vp * 3), ("particles", vp), ("cell_end", vp), ("out", vp),
+                ("counters", vp)]
 
 
 class FemGridInfo(C.Structure):

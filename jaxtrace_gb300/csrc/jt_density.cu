@@ -98,7 +98,16 @@ __device__ __forceinline__ float sph_shape(float q) {
     return expf(-q * q);
 }
 
-template <int DIM, int KERN>
+// Sum of a per-thread count over the warp, added once per warp.
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
+    const unsigned m = __activemask();
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(m, v, o);
+    if ((threadIdx.x & 31) == (__ffs(m) - 1)) atomicAdd(dst, v);
+}
+
+// COUNT: also count the candidate pairs examined and those inside the
+// support (P.counters), a separate instance so the plain one keeps its loop.
+template <int DIM, int KERN, bool COUNT = false>
 __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n_queries) return;
@@ -114,6 +123,7 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
     const int y0 = max(cy - P.reach[1], 0), y1 = min(cy + P.reach[1], lim);
     const int x0 = max(cx - P.reach[0], 0), x1 = min(cx + P.reach[0], lim);
     double acc = 0.0;
+    unsigned long long n_cand = 0, n_in = 0;
     if (P.h == nullptr) {
         // uniform h: sigma and 1/h once; pairs beyond the kernel's support skip
         const float hh = fmaxf(P.h_const, 1e-12f), inv = 1.0f / hh, sigma = sph_sigma<DIM, KERN>(hh);
@@ -142,12 +152,16 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
                     // {x, y, z, m} records; FMA-contracted distance (no parity
                     // constraint on the density passes)
                     const float4* p4 = reinterpret_cast<const float4*>(P.particles);
+                    if (COUNT) n_cand += e - b;
 #pragma unroll 4
                     for (uint32_t j = b; j < e; ++j) {
                         const float4 r = __ldg(p4 + j);
                         const float dx = r.x - qx, dy = r.y - qy, dz = DIM == 3 ? r.z - qz : 0.0f;
                         const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        if (d2 <= r2lim) part = fmaf(r.w, sph_shape<KERN>(fast_dist(d2) * inv), part);
+                        if (d2 <= r2lim) {
+                            part = fmaf(r.w, sph_shape<KERN>(fast_dist(d2) * inv), part);
+                            if (COUNT) ++n_in;
+                        }
                     }
                 } else {
                     for (uint32_t j = b; j < e; ++j) {
@@ -186,6 +200,10 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
         }
     }
     P.out[i] = acc;
+    if (COUNT) {
+        warp_add(P.counters, n_cand);
+        warp_add(P.counters + 1, n_in);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -316,10 +334,12 @@ __global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params 
     const int lo2 = cell_of(gcoord[2][0] - P.radius, g.origin[2], g.inv_cell[2], lim);
     const int hi2 = cell_of(gcoord[2][n2 - 1] + P.radius, g.origin[2], g.inv_cell[2], lim);
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    unsigned long long visits = 0;
     for (int cz = lo2; cz <= hi2; ++cz)
         for (int cy = lo1; cy <= hi1; ++cy) {
             uint32_t b, e;
             row_range(P.cell_end, lo0, hi0, cy, cz, g.bits, b, e);
+            visits += e - b;
             for (uint32_t c0 = b; c0 < e; c0 += kKbChunk) {
                 const int n = (int)min((uint32_t)kKbChunk, e - c0);
                 for (int j = t; j < n; j += kKbThreads) {
@@ -358,6 +378,10 @@ __global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params 
                 __syncthreads();
             }
         }
+    if (P.counters != nullptr && t == 0) {
+        atomicAdd(P.counters, visits);
+        atomicAdd(P.counters + 1, visits * (unsigned long long)(n0 * n1 * n2));
+    }
     if (pa < n0 && pb < n1) {
         const int64_t row = ((int64_t)(b0 + pa) * P.res[1] + (b1 + pb)) * P.res[2] + b2 + pc0;
         if (pc0 < n2) P.out[row] = a0;
@@ -417,6 +441,15 @@ extern "C" int jt_sph_density(const jt_sph_params* p, void* stream) {
         if (p->reach[a] < 0 || p->reach[a] > 127) return set_error(JT_ERR_INVALID, "reach must be 0..127");
     const unsigned gb = grid_blocks(p->n_queries);
     cudaStream_t st = (cudaStream_t)stream;
+    if (p->counters != nullptr) {
+        if (p->h != nullptr || !p->packed)
+            return set_error(JT_ERR_UNSUPPORTED, "SPH counters need a uniform h and packed records");
+        if (p->dims == 3 && p->kernel == JT_SPH_CUBIC) k_sph<3, JT_SPH_CUBIC, true><<<gb, kBlock, 0, st>>>(*p);
+        else if (p->dims == 3 && p->kernel == JT_SPH_WENDLAND) k_sph<3, JT_SPH_WENDLAND, true><<<gb, kBlock, 0, st>>>(*p);
+        else if (p->dims == 3) k_sph<3, JT_SPH_GAUSSIAN, true><<<gb, kBlock, 0, st>>>(*p);
+        else return set_error(JT_ERR_UNSUPPORTED, "SPH counters are for 3-D");
+        return cuda_status(cudaGetLastError(), "SPH kernel launch");
+    }
 #define JT_SPH_LAUNCH(D, K) k_sph<D, K><<<gb, kBlock, 0, st>>>(*p)
     if (p->dims == 3) {
         if (p->kernel == JT_SPH_CUBIC) JT_SPH_LAUNCH(3, JT_SPH_CUBIC);

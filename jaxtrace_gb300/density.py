@@ -122,11 +122,17 @@ class CellList:
         return [int(math.ceil(radius / c)) if math.isfinite(c) and c > 0 else 0 for c in self.cell]
 
 
+# The device the estimators keep their arrays on (the kernels read them
+# there); the host suite substitutes the CPU to drive the multi-rank
+# exchange with host stand-ins for the kernels.
+_DEV = "cuda"
+
+
 def _as_device_f32(positions):
     torch = _torch()
     if isinstance(positions, torch.Tensor):
-        return positions.to(device="cuda", dtype=torch.float32).contiguous()
-    return torch.from_numpy(np.ascontiguousarray(np.asarray(positions, dtype=F32))).cuda()
+        return positions.to(device=_DEV, dtype=torch.float32).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(positions, dtype=F32))).to(_DEV)
 
 
 def _pad3(P2):
@@ -151,6 +157,11 @@ class KDEEstimator:
     resolution: Union[int, Tuple[int, int, int]] = 100
     bounds: Optional[Tuple[Tuple[float, float], ...]] = None
     cutoff_sigmas: float = 5.0
+    # a torch.distributed group whose ranks each hold a share of the
+    # particles: the bandwidth and the grid bounds come from all of them, each
+    # rank sums its share on the grid and one float64 all-reduce adds the
+    # shares (the density is a sum over particles, kde.py:249-270)
+    process_group: Optional[object] = None
 
     def __post_init__(self):
         torch = _torch()
@@ -159,16 +170,40 @@ class KDEEstimator:
             raise ValueError("positions must be (N,2) or (N,3)")
         self.N, self.D = int(P.shape[0]), int(P.shape[1])
         self.P = P
+        self._lohi = None
+        self.N_total = self.N
+        if self.process_group is not None:
+            from .distributed import global_stats
+            n, _, var, lo, hi = global_stats(P, self.process_group)
+            self.N_total, self._lohi = n, (lo, hi)
         if self.bandwidth is None:
             if self.bandwidth_rule not in ("scott", "silverman"):
                 raise ValueError("bandwidth_rule must be 'scott' or 'silverman' if bandwidth is None")
-            if isinstance(self.positions, torch.Tensor):
+            if self.process_group is not None:
+                # the rules of kernels.py:46-68 on the moments of all ranks' particles
+                d = self.D
+                self.h = float(np.mean(np.sqrt(var))) * self.N_total ** (-1.0 / (d + 4.0))
+                if self.bandwidth_rule == "silverman":
+                    self.h *= (4.0 / (d + 2.0)) ** (1.0 / (d + 4.0))
+            elif isinstance(self.positions, torch.Tensor):
                 self.h = _device_bandwidth(P, self.bandwidth_rule)
             else:
                 rule = scott_bandwidth if self.bandwidth_rule == "scott" else silverman_bandwidth
                 self.h = float(rule(np.asarray(self.positions, dtype=F32)))
         else:
             self.h = float(self.bandwidth)
+
+    def _reduce(self, a):
+        """Sum of every rank's array (identity without a process group)."""
+        if self.process_group is None:
+            return a
+        from .distributed import allreduce_array
+        return allreduce_array(a, self.process_group)
+
+    def _count(self, n: int) -> int:
+        if self.process_group is None:
+            return int(n)
+        return int(round(float(self._reduce(np.array([float(n)]))[0])))
 
     # -- helpers (kde.py:101-119) --
     def _axes_for_plane(self):
@@ -213,6 +248,10 @@ class KDEEstimator:
         p.res[:] = res
         for a in range(dims):
             p.axis[a] = ax[a].data_ptr()
+        # work counters for measurement (a device int64 pair), when asked for
+        counters = getattr(self, "count_into", None)
+        if counters is not None and dims == 3:
+            p.counters = counters.data_ptr()
         p.out = out.data_ptr()
         L.check(L.load().jt_kde_grid(C.byref(p), L.stream_ptr()))
         return out.reshape(res[:dims]).cpu().numpy()
@@ -226,8 +265,7 @@ class KDEEstimator:
         p, cl = self._params(pts, d, lo, hi)
         out = torch.empty(Q3.shape[0], dtype=torch.float64, device="cuda")
         L.check(L.load().jt_kde_points(C.byref(p), L.ptr(Q3), Q3.shape[0], L.ptr(out), L.stream_ptr()))
-        norm = (2.0 * math.pi) ** (-0.5 * d)
-        return (out * (norm / max(int(pts.shape[0]), 1))).float().cpu().numpy()
+        return out.cpu().numpy()                       # sum_j exp(-|q - p_j|^2 / 2h^2)
 
     # -- public API --
     def evaluate(self, points) -> np.ndarray:
@@ -250,10 +288,15 @@ class KDEEstimator:
                 Q = Q[:, [0, 1]]
             else:
                 raise ValueError(f"Expected points with 2 or 3 columns, got {Q.shape[1]}")
-        return self._evaluate_points(Q, pts)
+        d = int(Q.shape[1])
+        s = self._reduce(self._evaluate_points(Q, pts))
+        norm = (2.0 * math.pi) ** (-0.5 * d)
+        return (s * (norm / max(self._count(int(pts.shape[0])), 1))).astype(F32)
 
     def _bounds_lohi(self, pts, k):
         if self.bounds is None:
+            if self._lohi is not None and pts is self.P:
+                return self._lohi[0][:k], self._lohi[1][:k]
             return pts.min(dim=0).values.cpu().numpy(), pts.max(dim=0).values.cpu().numpy()
         lo = np.array([b[0] for b in self.bounds[:k]], dtype=float)
         hi = np.array([b[1] for b in self.bounds[:k]], dtype=float)
@@ -268,8 +311,8 @@ class KDEEstimator:
         y = np.linspace(lo[1], hi[1], ny, dtype=np.float32)
         z = np.linspace(lo[2], hi[2], nz, dtype=np.float32)
         X, Y, Z = np.meshgrid(x, y, z, indexing="xy")
-        s = self._grid_sum(self.P, (x, y, z))                  # (nx, ny, nz)
-        D = s.transpose(1, 0, 2) * ((2.0 * math.pi) ** -1.5 / self.N)
+        s = self._reduce(self._grid_sum(self.P, (x, y, z)))   # (nx, ny, nz), all ranks' particles
+        D = s.transpose(1, 0, 2) * ((2.0 * math.pi) ** -1.5 / self.N_total)
         if self.normalize:
             D = self._normalise(D, [X, Y, Z], [1, 0, 2])
         return X, Y, Z, D.astype(F32)
@@ -279,6 +322,9 @@ class KDEEstimator:
         pts = self.P[:, :2].contiguous() if self.D == 2 else self._slice_2d_points()
         if self.bounds is None:
             lo, hi = pts.min(dim=0).values.cpu().numpy(), pts.max(dim=0).values.cpu().numpy()
+            if self.process_group is not None:
+                from .distributed import global_stats
+                _, _, _, lo, hi = global_stats(pts, self.process_group)
         else:
             lo = np.array([self.bounds[0][0], self.bounds[1][0]], dtype=float)
             hi = np.array([self.bounds[0][1], self.bounds[1][1]], dtype=float)
@@ -287,8 +333,8 @@ class KDEEstimator:
         x = np.linspace(lo[0], hi[0], nx, dtype=np.float32)
         y = np.linspace(lo[1], hi[1], ny, dtype=np.float32)
         X, Y = np.meshgrid(x, y, indexing="xy")
-        s = self._grid_sum(pts, (x, y))                        # (nx, ny)
-        Z = s.T * ((2.0 * math.pi) ** -1.0 / max(int(pts.shape[0]), 1))
+        s = self._reduce(self._grid_sum(pts, (x, y)))         # (nx, ny), all ranks' particles
+        Z = s.T * ((2.0 * math.pi) ** -1.0 / max(self._count(int(pts.shape[0])), 1))
         if self.normalize:
             Z = self._normalise(Z, [X, Y], [1, 0])
         return X, Y, Z.astype(F32)
@@ -332,12 +378,23 @@ class SPHDensityEstimator:
     normalize: bool = True
     resolution: Union[int, Tuple[int, int, int]] = 100
     bounds: Optional[Tuple[Tuple[float, float], ...]] = None
+    # a torch.distributed group whose ranks each hold a share of the
+    # particles: every query needs every particle within reach, so the shares
+    # (and masses) are all-gathered first and each rank then evaluates its
+    # own queries against all particles
+    process_group: Optional[object] = None
 
     def __post_init__(self):
         torch = _torch()
         if self.kernel_type not in _SPH_KERNELS:
             raise ValueError(f"Unknown kernel type: {self.kernel_type}")
         P3 = _as_device_f32(self.positions)
+        if self.process_group is not None:
+            from .distributed import gather_all
+            P3 = gather_all(P3, self.process_group).contiguous()
+            if self.masses is not None:
+                self.masses = gather_all(_as_device_f32(np.asarray(self.masses, dtype=F32).reshape(-1)),
+                                         self.process_group).cpu().numpy()
         if self.dimensions.lower() == "2d":
             if P3.shape[1] != 3:
                 raise ValueError("2D SPH requires (N,3) positions for slicing")
@@ -360,7 +417,7 @@ class SPHDensityEstimator:
             self.masses_dev = m
         if self.smoothing_length is not None:
             self.smoothing_lengths = torch.full((self.N,), float(self.smoothing_length), dtype=torch.float32,
-                                                device="cuda")
+                                                device=_DEV)
             self._uniform_h = float(F32(self.smoothing_length))
         else:
             self.smoothing_lengths = self._calculate_smoothing_lengths()
@@ -394,7 +451,7 @@ class SPHDensityEstimator:
         h = domain_size / n_per_dim * 2.0
         h = np.clip(h, 0.01, domain_size * 0.1)
         self._uniform_h = float(F32(h))
-        return torch.full((self.N,), float(h), dtype=torch.float32, device="cuda")
+        return torch.full((self.N,), float(h), dtype=torch.float32, device=_DEV)
 
     def _density_sum(self, Q):
         torch = _torch()
@@ -441,6 +498,10 @@ class SPHDensityEstimator:
         p.queries = qcl.sorted.data_ptr()
         out_sorted = torch.empty(M, dtype=torch.float64, device="cuda")
         p.out = out_sorted.data_ptr()
+        # work counters for measurement (a device int64 pair), when asked for
+        counters = getattr(self, "count_into", None)
+        if counters is not None:
+            p.counters = counters.data_ptr()
         L.check(L.load().jt_sph_density(C.byref(p), L.stream_ptr()))
         out.index_copy_(0, qcl.ids.long(), out_sorted)
         return out

@@ -101,6 +101,68 @@ def allreduce_sum(t):
     return t
 
 
+def gather_all(local, group=None):
+    """Every rank's rows (any count per rank) on every rank, in rank order:
+    the SPH exchange, where each query needs every particle near it."""
+    import torch
+    dist = _dist()
+    local = torch.as_tensor(local)
+    world = dist.get_world_size(group)
+    if world == 1:
+        return local
+    dev = collective_device()
+    x = local.to(dev)
+    n = torch.tensor([x.shape[0]], dtype=torch.int64, device=dev)
+    counts = [torch.zeros_like(n) for _ in range(world)]
+    dist.all_gather(counts, n, group=group)
+    counts = [int(c.item()) for c in counts]
+    width = max(max(counts), 1)
+    pad = torch.zeros((width,) + tuple(x.shape[1:]), dtype=x.dtype, device=dev)
+    pad[: x.shape[0]] = x
+    parts = [torch.empty_like(pad) for _ in range(world)]
+    dist.all_gather(parts, pad, group=group)
+    return torch.cat([p[:c] for p, c in zip(parts, counts)], dim=0).to(local.device)
+
+
+def global_stats(P, group=None):
+    """Count, mean, unbiased variance, minimum and maximum per column of the
+    rows spread over the ranks (float64 sums, one all-reduce each): what the
+    KDE bandwidth rules and the grid bounds need of all particles."""
+    import torch
+    dist = _dist()
+    x = torch.as_tensor(P).double()
+    dev = collective_device()
+    s = torch.cat([torch.tensor([float(x.shape[0])], dtype=torch.float64), x.sum(0).cpu(),
+                   (x * x).sum(0).cpu()]).to(dev)
+    lo = x.min(0).values.cpu().to(dev) if x.shape[0] else torch.full((x.shape[1],), float("inf"), device=dev,
+                                                                         dtype=torch.float64)
+    hi = x.max(0).values.cpu().to(dev) if x.shape[0] else torch.full((x.shape[1],), float("-inf"), device=dev,
+                                                                         dtype=torch.float64)
+    if dist.get_world_size(group) > 1:
+        dist.all_reduce(s, op=dist.ReduceOp.SUM, group=group)
+        dist.all_reduce(lo, op=dist.ReduceOp.MIN, group=group)
+        dist.all_reduce(hi, op=dist.ReduceOp.MAX, group=group)
+    s = s.cpu().numpy()
+    d = x.shape[1]
+    n = s[0]
+    mean = s[1:1 + d] / n
+    var = (s[1 + d:] - n * mean * mean) / max(n - 1.0, 1.0)
+    return int(n), mean, var, lo.cpu().numpy(), hi.cpu().numpy()
+
+
+def allreduce_array(a, group=None):
+    """Float64 sum over ranks of a host or device array (the KDE grid)."""
+    import torch
+    dist = _dist()
+    if dist.get_world_size(group) == 1:
+        return a
+    is_np = isinstance(a, np.ndarray)
+    t = torch.as_tensor(np.ascontiguousarray(a) if is_np else a)
+    acc = t.to(device=collective_device(), dtype=torch.float64)
+    dist.all_reduce(acc, op=dist.ReduceOp.SUM, group=group)
+    return acc.cpu().numpy() if is_np else acc.to(device=t.device)
+
+
 def track_sharded(run: Callable, x0: np.ndarray, to_all: bool = False):
     """Advance this rank's slice of ``x0`` with ``run`` (a function from a
     (n_r, 3) float32 array to its final positions, e.g. a tracker's
@@ -115,4 +177,4 @@ def track_sharded(run: Callable, x0: np.ndarray, to_all: bool = False):
 
 
 __all__ = ["world_and_rank", "shard_bounds", "shard_ensembles", "collective_device", "gather_rows", "allreduce_sum",
-           "track_sharded"]
+           "gather_all", "global_stats", "allreduce_array", "track_sharded"]

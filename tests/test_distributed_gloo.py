@@ -124,3 +124,96 @@ def test_nccl_collectives_take_device_tensors(monkeypatch):
     assert seen == ["meta", "meta"]
     monkeypatch.undo()
     assert D.collective_device() == torch.device("cpu")
+
+
+def _host_stand_ins():
+    """Run the density estimators on the CPU: the device is the host and the
+    two kernels are brute-force float64 sums (the exchange is what these
+    tests check, not the kernels)."""
+    import math
+
+    import torch
+    import jaxtrace_gb300.density as Dn
+
+    Dn._torch = lambda: torch
+    Dn._DEV = "cpu"
+
+    def grid_sum(self, pts, axes):
+        P = pts.double().numpy()
+        g = np.meshgrid(*[np.asarray(a, np.float64) for a in axes], indexing="ij")
+        G = np.stack([x.reshape(-1) for x in g], axis=1)
+        d2 = ((G[:, None, :] - P[None, :, : G.shape[1]]) ** 2).sum(-1)
+        return np.exp(-d2 / (2 * self.h * self.h)).sum(1).reshape([len(a) for a in axes])
+
+    def points_sum(self, Q, pts):
+        q = np.asarray(Q, np.float64)
+        P = pts.double().numpy()[:, : q.shape[1]]
+        d2 = ((q[:, None, :] - P[None]) ** 2).sum(-1)
+        return np.exp(-d2 / (2 * self.h * self.h)).sum(1)
+
+    def density_sum(self, Q):
+        q, P = Q.double(), self.P.double()
+        h = float(self._mean_h)
+        r = torch.cdist(q, P) / h
+        w = torch.where(r <= 1, 1 - 1.5 * r ** 2 + 0.75 * r ** 3, torch.where(r <= 2, 0.25 * (2 - r) ** 3,
+                                                                              torch.zeros_like(r)))
+        return w.sum(1) / (math.pi * h ** 3)
+
+    Dn.KDEEstimator._grid_sum = grid_sum
+    Dn.KDEEstimator._evaluate_points = points_sum
+    Dn.SPHDensityEstimator._density_sum = density_sum
+    return Dn
+
+
+def _density_worker(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        Dn = _host_stand_ins()
+        rng = np.random.default_rng(9)
+        P = rng.normal(0.5, 0.15, (301, 3)).astype(np.float32)
+        lo, hi = D.shard_bounds(len(P), rank, world)
+        mine = P[lo:hi]
+        g = dist.group.WORLD
+        kde_all = Dn.KDEEstimator(P, resolution=6)
+        kde = Dn.KDEEstimator(mine, resolution=6, process_group=g)
+        _, _, _, d_all = kde_all.evaluate_3d()
+        _, _, _, d_sh = kde.evaluate_3d()
+        Q = rng.random((40, 3)).astype(np.float32)
+        e_all, e_sh = kde_all.evaluate(Q), kde.evaluate(Q)
+        sph_all = Dn.SPHDensityEstimator(P, dimensions="3d", smoothing_length=0.1)
+        sph = Dn.SPHDensityEstimator(mine, dimensions="3d", smoothing_length=0.1, process_group=g)
+        q.put({"rank": rank, "h": (kde_all.h, kde.h), "n": (kde_all.N_total, kde.N_total, kde.N),
+               "grid": (d_all, d_sh), "points": (e_all, e_sh),
+               "sph": (sph_all.evaluate(Q), sph.evaluate(Q)), "sph_n": sph.N})
+    finally:
+        dist.destroy_process_group()
+
+
+def test_density_estimators_shard_particles_on_two_gloo_ranks():
+    """KDE: bandwidth and bounds from all ranks' moments, one grid sum per
+    share, a float64 all-reduce; SPH: the shares all-gathered so every query
+    sees every particle.  Each rank's result equals the single-process
+    estimator on all particles."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_density_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=180) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for r in res:
+        h_all, h_sh = r["h"]
+        assert abs(h_all - h_sh) <= 1e-6 * h_all
+        assert r["n"][0] == r["n"][1] == 301 and r["n"][2] in (150, 151)
+        a, b = r["grid"]
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-7 * np.abs(a).max())
+        a, b = r["points"]
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-7 * np.abs(a).max())
+        a, b = r["sph"]
+        assert r["sph_n"] == 301 and np.allclose(a, b, rtol=1e-6)
