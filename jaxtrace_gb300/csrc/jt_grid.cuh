@@ -222,11 +222,19 @@ __device__ __forceinline__ V3 quad_yz(const uint32_t (&q)[8], __half2 WY, __half
 //     divided by the power-of-two scale carried in e.wa.  Two 256-bit loads
 //     per evaluation measured faster than eight 64-bit loads of float16 node
 //     records, although those fit L2 and the quads do not.
+// Blocks of 256 per SM the stage-field kernels are compiled for, measured on
+// the precision configuration: float16 offset quads 6 (42 registers, 12 B
+// of spills; 1.6 % faster than 5 without spills), float32 quads 5 in the
+// exact arithmetic (2.8 % faster than 4 despite spills) and 4 in the fast
+// one (5 was 12 % slower).
 #ifndef JT_STAGE16_MIN_BLOCKS
-#define JT_STAGE16_MIN_BLOCKS 5
+#define JT_STAGE16_MIN_BLOCKS 6
 #endif
 #ifndef JT_STAGE32_MIN_BLOCKS
 #define JT_STAGE32_MIN_BLOCKS 4
+#endif
+#ifndef JT_STAGE32X_MIN_BLOCKS
+#define JT_STAGE32X_MIN_BLOCKS 5
 #endif
 
 //
@@ -237,10 +245,10 @@ __device__ __forceinline__ V3 quad_yz(const uint32_t (&q)[8], __half2 WY, __half
 // lerp form.
 template <bool EXACT, int OUT, int MODE = -1>
 struct StageGridField {
-    // float16 quads at 5 blocks of 256 (48 registers, no spills; 1 % faster
-    // than 6 blocks at 40 registers with spills); float32 records take 64
-    // registers at 4
-    static constexpr int kMinBlocks = OUT == JT_STORE_STAGE_F16 ? JT_STAGE16_MIN_BLOCKS : JT_STAGE32_MIN_BLOCKS;
+    static constexpr int kMinBlocks = OUT == JT_STORE_STAGE_F16
+                                          ? JT_STAGE16_MIN_BLOCKS
+                                          : (EXACT && OUT == JT_STORE_STAGE_F32Q ? JT_STAGE32X_MIN_BLOCKS
+                                                                                 : JT_STAGE32_MIN_BLOCKS);
     // the evaluation is short enough that the kernel is bound by instruction
     // issue: unrolled stages drop the loop's own instructions
     static constexpr bool kUnrollStages = true;
