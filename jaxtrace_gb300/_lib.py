@@ -209,6 +209,13 @@ def load(build_if_missing: bool = True):
         fn.argtypes = args
     if lib.jt_abi_version() != ABI_VERSION:
         raise ImportError("jaxtrace_gb300 native library ABI mismatch")
+    # every descriptor this module hands the library must have the C layout's
+    # size: a shorter mirror would let the library read past it
+    out = (i64 * 16)()
+    n = lib.jt_struct_sizes(out, 16)
+    want = [C.sizeof(st) for st in STRUCTS]
+    if n != len(want) or [int(out[k]) for k in range(n)] != want:
+        raise ImportError(f"jaxtrace_gb300 struct layouts differ from the library's: {list(out)[:max(n, 0)]} vs {want}")
     _lib = lib
     return lib
 
