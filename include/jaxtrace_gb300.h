@@ -207,13 +207,6 @@ typedef struct {
     const jt_octree_node* nodes; /* device (n_nodes)                        */
     const int32_t* elems;   /* device element lists                           */
     const void* pairs;      /* device value pairs, layout as jt_grid_field   */
-    /* optional candidate prefilter (jt_mesh_prefilter), NULL to scan without
-     * it: elem_q, 4 words per element-list slot {tet id, float16 pairs of the
-     * tet's box relative to its list's candidate box, rounded outward: (min x,
-     * min y), (max x, max y), (min z, -max z)}; node_q, 8 floats per node
-     * {candidate box min xyz, 0, 1/extent xyz, 0} */
-    const uint32_t* elem_q;
-    const float* node_q;
 } jt_mesh_field;
 
 /* Nearest-node field: TimeSeriesField spatial sampling (time_series.py:391)
@@ -622,17 +615,6 @@ int jt_octree_build_device(const float* points, int32_t n_points, const int32_t*
  * re-solve the barycentric weights of a flagged tetrahedron in float64;
  * JT_ARITH_EXACT ignores the flag.  Device buffers; *count_out (host, may be
  * NULL) receives the number flagged.  Returns after the pass has finished. */
-/* No reference counterpart (a table derived from the octree): fills the
- * candidate prefilter of a mesh field's element lists, elem_q device
- * (n_elem_entries * 4) uint32 and node_q device (n_nodes * 8) float.  The
- * scan then reads one 16 B record per candidate and rejects those whose
- * quantised box misses the query before reading the exact box, which it
- * still tests for the others: the same first hit, fewer bytes per
- * candidate.  The quantised boxes contain the exact ones with a margin above
- * the query's float16 rounding. */
-int jt_mesh_prefilter(const jt_mesh_field* mesh, int32_t n_elem_entries, uint32_t* elem_q, float* node_q,
-                      void* stream);
-
 int jt_mark_near_degenerate(float* tet_box, const float* tet_geom, int32_t n_tets, int32_t* count_out,
                             void* stream);
 

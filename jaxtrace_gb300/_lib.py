@@ -65,7 +65,7 @@ class MeshField(C.Structure):
     _fields_ = [("n_points", i32), ("n_tets", i32), ("n_nodes", i32), ("max_depth", i32),
                 ("storage", i32), ("n_pairs", i32), ("near_degenerate", i32), ("pad", i32), ("pair_stride", i64),
                 ("points", vp), ("tet_box", vp), ("tet_geom", vp), ("nodes", vp), ("elems", vp),
-                ("pairs", vp), ("elem_q", vp), ("node_q", vp)]
+                ("pairs", vp)]
 
 
 class NearestField(C.Structure):
@@ -201,7 +201,6 @@ def load(build_if_missing: bool = True):
         "jt_adjoint_workspace_bytes": (C.c_size_t, [i64, i32]),
         "jt_stage_fields": (i32, [P(Field), vp, vp, i32, i32, vp, vp]),
         "jt_stage_tile_fields": (i32, [P(Field), vp, vp, i32, vp, vp]),
-        "jt_mesh_prefilter": (i32, [P(MeshField), i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -99,8 +99,6 @@ __device__ __forceinline__ bool tet_bary(const V3& q, const float* tet_box, cons
     return true;
 }
 
-__device__ __forceinline__ __half2 u2h2q(uint32_t w) { return *reinterpret_cast<const __half2*>(&w); }
-
 // jnp.dot(bary, node_values): terms accumulated in vertex order.
 template <bool EXACT>
 __device__ __forceinline__ V3 p1_combine(const float4& b, const V3& n0, const V3& n1, const V3& n2, const V3& n3) {
@@ -150,38 +148,15 @@ struct MeshFieldT {
         const int cnt = oc.y;
         // candidate scan (…optimized.py:309-360): first candidate whose box
         // holds the query and whose barycentrics pass the tolerance test
-        if (F.elem_q != nullptr) {
-            // prefilter (jt_mesh_prefilter): one 16 B record per candidate; a
-            // float16 box containing the exact one rejects most candidates
-            // before their exact box is read, so the first hit is unchanged
-            const float4* nq = reinterpret_cast<const float4*>(F.node_q) + 2 * (int64_t)node;
-            const float4 c0 = __ldg(nq), c1 = __ldg(nq + 1);
-            const float rx = (q.x - c0.x) * c1.x, ry = (q.y - c0.y) * c1.y, rz = (q.z - c0.z) * c1.z;
-            const __half2 qxy = __floats2half2_rn(rx, ry), qz = __floats2half2_rn(rz, -rz);
-            const uint4* E = reinterpret_cast<const uint4*>(F.elem_q) + oc.x;
-            for (int s = 0; s < cnt; ++s) {
-                const uint4 r = __ldg(E + s);
-                if (!(__hbge2(qxy, u2h2q(r.y)) && __hble2(qxy, u2h2q(r.z)) && __hbge2(qz, u2h2q(r.w)))) continue;
-                float4 b;
-                int4 cn;
-                bool near;
-                const int t = (int)r.x;
-                if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
-                if (NEAR && !EXACT && near) b = bary_f64(q, F.tet_geom, t);
-                return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
-                                         node_value(cn.w, e));
-            }
-        } else {
-            for (int s = 0; s < cnt; ++s) {
-                float4 b;
-                int4 cn;
-                bool near;
-                const int t = __ldg(L + s);
-                if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
-                if (NEAR && !EXACT && near) b = bary_f64(q, F.tet_geom, t);
-                return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
-                                         node_value(cn.w, e));
-            }
+        for (int s = 0; s < cnt; ++s) {
+            float4 b;
+            int4 cn;
+            bool near;
+            const int t = __ldg(L + s);
+            if (!tet_bary<EXACT>(q, F.tet_box, F.tet_geom, t, b, cn, near)) continue;
+            if (NEAR && !EXACT && near) b = bary_f64(q, F.tet_geom, t);
+            return p1_combine<EXACT>(b, node_value(cn.x, e), node_value(cn.y, e), node_value(cn.z, e),
+                                     node_value(cn.w, e));
         }
         // cheap fallback (…optimized.py:364-376): nearest of the four vertices
         // of the first candidate; an empty list reads slot -1, which indexes

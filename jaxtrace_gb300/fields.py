@@ -978,11 +978,9 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
                  max_elements_per_leaf: int = 32, max_depth: int = 12, *, storage: str = "f32",
-                 octree_build: str = "auto", prefilter: bool = True):
+                 octree_build: str = "auto"):
         data = _as_f32(data)
         positions = ensure_positions_shape(positions)
-        # candidate prefilter of the octree scan (same results, fewer bytes per candidate)
-        self.prefilter = bool(prefilter)
         if data.ndim != 3 or data.shape[2] != 3:
             raise ValueError(f"data must have 3 dims (T,N,3), got {data.shape}")
         T, N, _ = data.shape
@@ -1022,15 +1020,6 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         f.points, f.tet_box, f.tet_geom = d["points"].data_ptr(), d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
         f.nodes, f.elems, f.pairs = d["nodes"].data_ptr(), d["elems"].data_ptr(), pairs.data_ptr()
         f.near_degenerate = int(self.n_near_degenerate > 0)
-        if self.prefilter:
-            # float16 candidate boxes per element-list slot (jt_mesh_prefilter):
-            # most candidates are rejected from one 16 B record
-            n_ent = int(d["elems"].numel())
-            d["elem_q"] = torch.empty((max(n_ent, 1), 4), dtype=torch.int32, device="cuda")
-            d["node_q"] = torch.empty((f.n_nodes, 8), dtype=torch.float32, device="cuda")
-            L.check(L.load().jt_mesh_prefilter(C.byref(f), n_ent, L.ptr(d["elem_q"]), L.ptr(d["node_q"]),
-                                               L.stream_ptr()))
-            f.elem_q, f.node_q = d["elem_q"].data_ptr(), d["node_q"].data_ptr()
         self._cmesh = f
         self._cfield = L.Field(kind=L.JT_FIELD_MESH, mesh=C.pointer(f))
 

@@ -440,30 +440,3 @@ def test_sorted_compensated_precision_matches_unsorted():
     # FMA contraction is the same per particle whatever its slot
     assert same(outs[0], outs[1])
 
-
-def test_octree_prefilter_changes_no_result(golden):
-    """The float16 candidate prefilter only skips tetrahedra whose exact box
-    misses the query: sampling and tracking with and without it give the same
-    bits, exact and compensated, on the reference's octree fixture and on a
-    jittered mesh with queries inside, outside and on element faces."""
-    from jaxtrace_gb300 import workloads as W
-    g = golden("octree")
-    P, T4 = W.kuhn_mesh(6, 0.2, 1)
-    st = np.linspace(0, 1, 3).astype(F32)
-    data = W.abc_snapshots(P, st)
-    rng = np.random.default_rng(4)
-    q = np.concatenate([rng.uniform(-0.2, 1.2, (4000, 3)), P[::3], (P[T4[:200, 0]] + P[T4[:200, 1]]) / 2,
-                        [[np.nan, 0.5, 0.5], [np.inf, 0.1, 0.1]]]).astype(F32)
-    for D, tm, pts, tets, qq in ((g["D"], g["st"], g["P"], g["T4"], g["q"]), (data, st, P, T4, q)):
-        a = jt.OctreeFEMTimeSeriesFieldOptimized(D, tm, pts, tets)
-        b = jt.OctreeFEMTimeSeriesFieldOptimized(D, tm, pts, tets, prefilter=False)
-        for t in (0.3, 0.71):
-            assert same(a.sample_at_positions(qq, F32(t)), b.sample_at_positions(qq, F32(t)))
-        x0 = rng.random((2000, 3)).astype(F32)
-        bc = jt.mixed_boundary(((0, 0, 0), (1, 1, 1)), {"x": "periodic", "y": "reflective", "z": "periodic"})
-        for prec in ("exact", "compensated"):
-            ra = jt.create_tracker("rk4", a, bc, precision=prec, record_final_only=True).track_particles(
-                x0, (0.0, 0.2), 21, dt=0.01)
-            rb = jt.create_tracker("rk4", b, bc, precision=prec, record_final_only=True).track_particles(
-                x0, (0.0, 0.2), 21, dt=0.01)
-            assert same(ra.positions, rb.positions)
