@@ -190,6 +190,21 @@ def oracle_subset_events(case, idx, precision):
                         n_threads=os.cpu_count() or 1, reseed=True)
 
 
+def reference_numpy_record():
+    """The reference's own NumPy path on the precision configuration, as
+    oracle/reference_timing.py measured it on the machine that holds the
+    reference sources (its CPU model and core count are in the record); the
+    sources are not on this host, so the figure is read, not re-measured."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "reference_timing.json")
+    try:
+        rows = json.load(open(path))["reference_numpy"]
+    except (OSError, KeyError, ValueError):
+        return None
+    keep = ("value", "unit", "processes", "particles", "steps", "seconds", "cpu", "host_cores", "machine", "sample")
+    return {"kind": "reference", "measured_by": "oracle/reference_timing.py on a machine with the reference sources (CPU in each row)",
+            "rows": [{k: r.get(k) for k in keep} for r in rows]}
+
+
 def run_reference(a, world, rank):
     """CPU restatement of the reference on all host cores (oracle port)."""
     if rank != 0:
@@ -218,6 +233,9 @@ def run_reference(a, world, rank):
                              "sample": f"{sample} of the {n} particles x {a.n_steps} RK4 steps per bench step, "
                                        f"float32 C restatement of the NumPy reference path, OpenMP"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    ref_np = reference_numpy_record()
+    if ref_np is not None:
+        line["cpu_baseline"]["reference_numpy"] = ref_np
     print(json.dumps(line), flush=True)
 
 
@@ -1134,6 +1152,9 @@ def main():
     if parity is not None:
         line["parity_f32_oracle"] = parity
     if cpu is not None:
+        ref_np = reference_numpy_record()
+        if ref_np is not None:
+            cpu["reference_numpy"] = ref_np
         line["cpu_baseline"] = cpu
     if not a.profile and not a.no_e2e:
         tr = jt.create_tracker("rk4", fields[head], bc, record_final_only=True, precision=VARIANTS[head][1], **topt)
