@@ -54,8 +54,9 @@ extern "C" {
 #define JT_STORE_F32 0  /* float32 x,y,z                                   */
 #define JT_STORE_BF16 1 /* bfloat16 x,y,z with a per-snapshot float32 scale */
 #define JT_STORE_F16 2  /* float16  x,y,z with a per-snapshot float32 scale */
-/* Pre-blended stage fields of a regular grid (jt_stage_fields), tracking only:
- * one time level per schedule entry, entry.pair = the field slot. */
+/* Pre-blended stage fields of a regular grid (jt_stage_fields), tracking only
+ * (no velocity recording: JT_ERR_UNSUPPORTED when vel is set): one time level
+ * per schedule entry, entry.pair = the field slot. */
 #define JT_STORE_STAGE_F32 3 /* float32 {x,y,z,0} per node (16 B)               */
 #define JT_STORE_STAGE_F16 4 /* offset float16 yz-quads per node (32 B) of the
                                 values divided by the power-of-two scale held

@@ -188,6 +188,10 @@ extern "C" int jt_track(const jt_field* field, const jt_boundary* bc, const jt_t
         return set_error(JT_ERR_INVALID, "recording needs record_every >= 1 and n_rows >= 0");
     if (p->vel != nullptr && p->traj == nullptr)
         return set_error(JT_ERR_INVALID, "velocity recording needs a trajectory buffer");
+    if (p->vel != nullptr && field->kind == JT_FIELD_GRID &&
+        (field->grid->storage == JT_STORE_STAGE_F32 || field->grid->storage == JT_STORE_STAGE_F32Q ||
+         field->grid->storage == JT_STORE_STAGE_F16))
+        return set_error(JT_ERR_UNSUPPORTED, "stage fields do not record velocities: track on snapshot pairs");
     if (p->block_size != 0 && p->block_size != 64 && p->block_size != 128 && p->block_size != 256)
         return set_error(JT_ERR_INVALID, "block_size must be 0, 64, 128 or 256, got %d", p->block_size);
     if (p->ens_offsets != nullptr && (p->n_ens < 1 || p->schedule_stride < 4LL * p->step_end))

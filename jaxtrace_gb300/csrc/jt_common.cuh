@@ -367,6 +367,29 @@ __device__ __forceinline__ void bc_inlet(const jt_boundary& B, const InletFrame&
     }
 }
 
+// bc_inlet for its most common form, fixed at compile time: grid
+// replacement, flow along +x.  The same operations as bc_inlet with a = 0,
+// without the run-time selects by axis, direction and mode.
+template <bool EXACT>
+__device__ __forceinline__ void bc_inlet_xpos(const jt_boundary& B, const InletFrame& I, float& x, float& y,
+                                              float& z) {
+    typedef Ar<EXACT> A;
+    if (x > I.amax) {
+        y = nearest_lattice(B.inlet_coords[0], B.inlet_res[0], y);
+        z = nearest_lattice(B.inlet_coords[1], B.inlet_res[1], z);
+        x = I.amin;
+    }
+    if (x < I.amin) x = B.inlet_nudge;
+    if (y < I.lo0) y = A::sub(I.lo0x2, y);
+    else if (y > I.hi0) y = A::sub(I.hi0x2, y);
+    if (z < I.lo1) z = A::sub(I.lo1x2, z);
+    else if (z > I.hi1) z = A::sub(I.hi1x2, z);
+}
+
+// Boundary forms a kernel can be specialised for (BK): any (read from the
+// descriptor at run time) or the +x grid inlet.
+enum { JT_BK_ANY = 0, JT_BK_INLET_XPOS = 1 };
+
 template <bool EXACT>
 __device__ __forceinline__ void apply_boundary(const jt_boundary& B, const InletFrame& I, float& x, float& y,
                                                float& z) {
@@ -491,6 +514,18 @@ JT_UNROLL(JT_STAGE_UNROLL)
     }
 }
 
+// Whether a field's tracking kernels record velocities (a field type may
+// set kRecordsVelocity false when its host never asks: the unused fifth
+// evaluation then leaves the kernel).
+template <class F, class = void>
+struct RecordsVelocityOf {
+    static constexpr bool value = true;
+};
+template <class F>
+struct RecordsVelocityOf<F, decltype(void(F::kRecordsVelocity))> {
+    static constexpr bool value = F::kRecordsVelocity;
+};
+
 // OR the per-thread status flags into the device status word, one atomic
 // per warp.
 __device__ __forceinline__ void report_flags(int32_t* status, int flags) {
@@ -514,7 +549,7 @@ __device__ __forceinline__ int find_ensemble(const int32_t* off, int n_ens, int 
 // registers, boundary fused after every step, optional strided recording.
 // PATH: P.path is set (the per-particle path length is accumulated); a
 // template argument so that runs without it keep the register budget.
-template <bool EXACT, int INTEG, bool PATH, class Field>
+template <bool EXACT, int INTEG, bool PATH, int BK, class Field>
 __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B, const InletFrame& I,
                                            const jt_track_params& P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -548,7 +583,8 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
         const V3 xo = x;
         if (comp) integrate<EXACT, INTEG, true>(f, e, k, x, c, flags);
         else integrate<EXACT, INTEG, false>(f, e, k, x, c, flags);
-        apply_boundary<EXACT>(B, I, x.x, x.y, x.z);
+        if constexpr (BK == JT_BK_INLET_XPOS) bc_inlet_xpos<EXACT>(B, I, x.x, x.y, x.z);
+        else apply_boundary<EXACT>(B, I, x.x, x.y, x.z);
         if (PATH) {
             const float dx = __fsub_rn(x.x, xo.x), dy = __fsub_rn(x.y, xo.y), dz = __fsub_rn(x.z, xo.z);
             plen = __fadd_rn(plen, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
@@ -562,7 +598,7 @@ __device__ __forceinline__ void track_body(const Field& f, const jt_boundary& B,
                     const int64_t id = P.ids != nullptr ? (int64_t)P.ids[i] : (int64_t)i;
                     float* o = P.traj + ((int64_t)row * n + id) * 3;
                     o[0] = x.x; o[1] = x.y; o[2] = x.z;
-                    if (P.vel != nullptr) {
+                    if (RecordsVelocityOf<Field>::value && P.vel != nullptr) {
                         const jt_blend er = e[3];
                         V3 v = f(x, er, flags);
                         float* ov = P.vel + ((int64_t)row * n + id) * 3;

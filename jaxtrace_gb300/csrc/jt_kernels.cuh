@@ -29,10 +29,25 @@ struct MinBlocksOf<F, decltype(void(F::kMinBlocks))> {
     static constexpr int value = F::kMinBlocks;
 };
 
-template <bool EXACT, int INTEG, bool PATH, class Field>
+template <bool EXACT, int INTEG, bool PATH, int BK, class Field>
 __global__ void __launch_bounds__(kBlock, MinBlocksOf<Field>::value)
     k_track(Field f, jt_boundary B, InletFrame I, jt_track_params P) {
-    track_body<EXACT, INTEG, PATH>(f, B, I, P);
+    track_body<EXACT, INTEG, PATH, BK>(f, B, I, P);
+}
+
+// Whether a field type gets an RK4 kernel specialised for the +x grid inlet
+// (kInletXpos), besides the one that reads the boundary at run time.
+template <class F, class = void>
+struct InletXposOf {
+    static constexpr bool value = false;
+};
+template <class F>
+struct InletXposOf<F, decltype(void(F::kInletXpos))> {
+    static constexpr bool value = F::kInletXpos;
+};
+
+inline bool is_inlet_xpos(const jt_boundary& B) {
+    return B.inlet_mode == JT_INLET_GRID && B.inlet_axis == 0 && B.inlet_positive != 0;
 }
 
 // Field evaluation at M points with one blend: sample_at_positions(pos, t).
@@ -105,10 +120,16 @@ struct Launcher {
     template <bool EXACT, bool PATH, class FF>
     static cudaError_t launch_track(const FF& f, const jt_boundary& B, const InletFrame& I, const jt_track_params& P,
                                     unsigned g, int bs, cudaStream_t st) {
+        if constexpr (InletXposOf<FF>::value && !PATH) {
+            if (P.integrator == JT_RK4 && is_inlet_xpos(B)) {
+                k_track<EXACT, JT_RK4, PATH, JT_BK_INLET_XPOS><<<g, bs, 0, st>>>(f, B, I, P);
+                return cudaGetLastError();
+            }
+        }
         switch (P.integrator) {
-            case JT_EULER: k_track<EXACT, JT_EULER, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
-            case JT_RK2: k_track<EXACT, JT_RK2, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
-            default: k_track<EXACT, JT_RK4, PATH><<<g, bs, 0, st>>>(f, B, I, P); break;
+            case JT_EULER: k_track<EXACT, JT_EULER, PATH, JT_BK_ANY><<<g, bs, 0, st>>>(f, B, I, P); break;
+            case JT_RK2: k_track<EXACT, JT_RK2, PATH, JT_BK_ANY><<<g, bs, 0, st>>>(f, B, I, P); break;
+            default: k_track<EXACT, JT_RK4, PATH, JT_BK_ANY><<<g, bs, 0, st>>>(f, B, I, P); break;
         }
         return cudaGetLastError();
     }

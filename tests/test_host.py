@@ -190,6 +190,15 @@ def test_new_entry_points_validate_before_touching_the_device():
     g.storage = L.JT_STORE_F32
     with pytest.raises(ValueError, match="block_size"):
         L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    # stage fields track without velocity recording (the host gathers pairs for it)
+    p.block_size = 0
+    p.traj, p.vel, p.record_every = 16, 16, 1
+    for st in (L.JT_STORE_STAGE_F32, L.JT_STORE_STAGE_F32Q, L.JT_STORE_STAGE_F16):
+        g.storage = st
+        with pytest.raises(NotImplementedError, match="velocities"):
+            L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    p.traj, p.vel, p.record_every, p.block_size = None, None, 0, 96
+    g.storage = L.JT_STORE_F32
     # FEM hash-grid descriptors
     h = L.FemField()
     ff = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(h))
