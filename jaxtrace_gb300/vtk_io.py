@@ -360,9 +360,13 @@ def read_vtk_xml(path: str, geometry: bool = True, names: Optional[List[str]] = 
 
 
 def _velocity3(v: np.ndarray) -> np.ndarray:
+    """(N, 3) float32 from an (N, components) array (_ensure_3d_velocity,
+    vtk_reader.py:77-103): zero-padded or cut to three components.  A
+    one-component array reads as 1-D, as vtk_to_numpy returns it, and is
+    refused like the reference refuses it."""
     v = np.asarray(v, dtype=F32)
-    if v.ndim == 1:
-        v = v[:, None]
+    if v.ndim != 2:
+        raise ValueError(f"Velocity must be 2D array (N, D), got shape {v.shape}")
     if v.shape[1] < 3:
         v = np.concatenate([v, np.zeros((len(v), 3 - v.shape[1]), dtype=F32)], axis=1)
     return np.ascontiguousarray(v[:, :3])
@@ -411,7 +415,9 @@ class VTKUnstructuredTimeSeriesReader:
             if name in pdata:
                 self.velocity_field_name = name
                 return name
-        raise ValueError(f"Velocity field not found. Available point data fields: {sorted(pdata)}")
+        avail = [f"{k} ({1 if np.ndim(a) < 2 else np.shape(a)[1]}D)" for k, a in pdata.items() if k]
+        raise ValueError(f"Velocity field not found. Available point data fields: {avail}\n"
+                         f"Specify velocity_field_name explicitly if using non-standard field names.")
 
     def load_single_timestep(self, time_idx: int) -> np.ndarray:
         if not 0 <= time_idx < len(self.time_files):
@@ -475,10 +481,19 @@ class VTKUnstructuredTimeSeriesReader:
         return tuple(float(v) for v in (*lo, *hi))
 
     def get_grid_info(self) -> Dict[str, Any]:
+        """The reference's keys (vtk_reader.py:773-788); no spatial index is
+        built (nothing here queries the nodes by position)."""
         if self.grid_points is None:
             self.load_single_timestep(0)
-        return {"n_points": int(len(self.grid_points)), "bounds": self.get_bounds(),
-                "n_timesteps": len(self.time_files), "velocity_field": self.velocity_field_name}
+        try:
+            import psutil
+            mem = psutil.Process().memory_info().rss / 1024 ** 3
+        except ImportError:
+            mem = 0.0
+        return {"grid_points": self.grid_points, "n_points": int(len(self.grid_points)),
+                "n_timesteps": len(self.time_files), "bounds": self.get_bounds(), "time_files": self.time_files,
+                "velocity_field_name": self.velocity_field_name, "cache_size": len(self.velocity_cache),
+                "memory_usage_gb": mem, "has_spatial_index": False}
 
 
 def open_vtk_time_series(file_pattern: str, max_time_steps: Optional[int] = None,

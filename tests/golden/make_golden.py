@@ -13,6 +13,7 @@ only the .npz files.
 """
 from __future__ import annotations
 
+import json
 import os
 import subprocess
 import sys
@@ -389,8 +390,133 @@ def phase_steps(ref: str):
     np.savez_compressed(HERE / "steps.npz", **out)
 
 
+def _vtk_scenarios():
+    """The time-series directories of phase vtk: per scenario its files
+    (name, points, point-data arrays, pieces of a .pvtu) and the reader's
+    arguments.  Points and arrays are small seeded random sets."""
+    rng = np.random.default_rng(31)
+
+    def pts(n):
+        return rng.uniform(-1.0, 2.0, (n, 3)).astype(F32)
+
+    def vtu(name, p, arrays):
+        return {"name": name, "kind": "vtu", "points": p, "arrays": arrays}
+
+    sc = []
+    # serial files in natural (not lexical) order, a scalar beside the velocity, a stray file
+    p1 = pts(37)
+    files = [vtu(f"flow_{k}.vtu", p1, [("p", rng.normal(size=37)), ("Velocity", rng.normal(size=(37, 3)).astype(F32))])
+             for k in (10, 2, 0, 1)]
+    files.append({"name": "notes.txt", "kind": "txt"})
+    sc.append({"tag": "serial", "files": files, "pattern": "*", "kwargs": {}})
+    # .pvtu files preferred over every .vtu, two pieces each, 2-component "U" padded to 3
+    p2a, p2b = pts(11), pts(9)
+    files = []
+    for k in (0, 1):
+        ua, ub = rng.normal(size=(11, 2)).astype(F32), rng.normal(size=(9, 2)).astype(F32)
+        files.append(vtu(f"a_{k}_p0.vtu", p2a, [("U", ua)]))
+        files.append(vtu(f"a_{k}_p1.vtu", p2b, [("U", ub)]))
+        files.append({"name": f"a_{k}.pvtu", "kind": "pvtu", "pieces": [f"a_{k}_p0.vtu", f"a_{k}_p1.vtu"],
+                      "points": np.concatenate([p2a, p2b]), "arrays": [("U", np.concatenate([ua, ub]))]})
+    files.append(vtu("b_5.vtu", p2a, [("U", rng.normal(size=(11, 2)).astype(F32))]))
+    sc.append({"tag": "parallel", "files": files, "pattern": "*", "kwargs": {}})
+    # the last max_time_steps files, a named 4-component array cut to 3
+    p3 = pts(23)
+    files = [vtu(f"s_{k}.vtu", p3, [("velocity", rng.normal(size=(23, 3)).astype(F32)),
+                                    ("w4", rng.normal(size=(23, 4)).astype(F32))]) for k in (1, 3, 2)]
+    sc.append({"tag": "named_last2", "files": files, "pattern": "s_*.vtu",
+               "kwargs": {"max_time_steps": 2, "velocity_field_name": "w4"}})
+    # a scalar named as the velocity: VTK hands back a 1-D array, which the reader refuses
+    sc.append({"tag": "scalar_named", "files": files, "pattern": "s_*.vtu", "kwargs": {"velocity_field_name": "p"}})
+    # no array with a velocity name
+    p5 = pts(8)
+    files = [vtu(f"t_{k}.vtu", p5, [("pressure", rng.normal(size=8)), ("T", rng.normal(size=(8, 3)).astype(F32))])
+             for k in (0, 1)]
+    sc.append({"tag": "no_velocity", "files": files, "pattern": "*.vtu", "kwargs": {}})
+    for s in sc:
+        if s["tag"] == "scalar_named":
+            s["files"] = [dict(f, arrays=f["arrays"] + [("p", rng.normal(size=23))]) for f in s["files"]]
+    return sc
+
+
+def write_vtk_scenario(root, scenario):
+    """Write a scenario's files under root with this repository's writers."""
+    sys.path.insert(0, str(REPO))
+    from jaxtrace_gb300 import vtk_io as V
+    os.makedirs(root, exist_ok=True)
+    for f in scenario["files"]:
+        path = os.path.join(root, f["name"])
+        if f["kind"] == "txt":
+            Path(path).write_text("not a VTK file\n")
+        elif f["kind"] == "vtu":
+            V.write_vtu(path, f["points"], None, dict(f["arrays"]), vertices=True)
+        else:
+            types = {np.dtype(np.float32): "Float32", np.dtype(np.float64): "Float64"}
+            arrs = {n: (types[np.asarray(a).dtype], 1 if np.ndim(a) == 1 else np.shape(a)[1]) for n, a in f["arrays"]}
+            V.write_pvtu(path, f["pieces"], arrs)
+
+
+def phase_vtk(ref: str):
+    """The reference's VTKUnstructuredTimeSeriesReader (io/vtk_reader.py:426-940)
+    over series written by this repository's writers, with the VTK library
+    replaced by the stand-in oracle/vtkshim: its file selection and order,
+    velocity-name detection, component padding, bounds and time values."""
+    import contextlib
+    import io
+    import tempfile
+    import warnings
+    warnings.simplefilter("ignore")
+    sys.path.insert(0, str(REPO / "oracle" / "vtkshim"))
+    sys.path.insert(1, ref)
+    import vtk as fake
+    from jaxtrace.io import vtk_reader as R
+    assert R.VTK_AVAILABLE
+    out, manifest = {}, []
+    for s in _vtk_scenarios():
+        with tempfile.TemporaryDirectory() as tmp:
+            write_vtk_scenario(tmp, s)
+            fake.REGISTRY.clear()
+            for f in s["files"]:
+                if f["kind"] != "txt":
+                    fake.REGISTRY[os.path.abspath(os.path.join(tmp, f["name"]))] = {
+                        "points": f["points"], "point_data": f["arrays"]}
+            tag = s["tag"]
+            rec = {"tag": tag, "pattern": s["pattern"], "kwargs": s["kwargs"], "files": []}
+            for i, f in enumerate(s["files"]):
+                entry = {"name": f["name"], "kind": f["kind"], "pieces": f.get("pieces", [])}
+                if f["kind"] != "txt":
+                    out[f"{tag}_f{i}_points"] = f["points"]
+                    entry["arrays"] = [n for n, _ in f["arrays"]]
+                    for n, a in f["arrays"]:
+                        out[f"{tag}_f{i}_{n}"] = np.asarray(a)
+                rec["files"].append(entry)
+            try:
+                with contextlib.redirect_stdout(io.StringIO()):
+                    rd = R.VTKUnstructuredTimeSeriesReader(os.path.join(tmp, s["pattern"]), **s["kwargs"])
+                    ts = rd.load_time_series()
+                    bounds = rd.get_bounds()
+                    info = rd.get_grid_info()
+                rec["order"] = [os.path.basename(f) for f in rd.time_files]
+                rec["velocity_field_name"] = ts["velocity_field_name"]
+                rec["source"] = ts["source"]
+                rec["info"] = {"n_points": int(info["n_points"]), "n_timesteps": int(info["n_timesteps"]),
+                               "velocity_field_name": info["velocity_field_name"],
+                               "time_files": [os.path.basename(f) for f in info["time_files"]],
+                               "has_spatial_index": bool(info["has_spatial_index"]), "keys": sorted(info)}
+                out[f"{tag}_velocity_data"] = ts["velocity_data"]
+                out[f"{tag}_positions"] = ts["positions"]
+                out[f"{tag}_times"] = ts["times"]
+                out[f"{tag}_bounds"] = np.asarray(bounds, dtype=np.float64)
+            except Exception as e:  # noqa: BLE001 -- the reference's refusal is the fixture
+                rec["error"] = {"type": type(e).__name__, "message": str(e).split("\n")[0]}
+            manifest.append(rec)
+    out["manifest"] = np.array(json.dumps(manifest))
+    np.savez_compressed(HERE / "vtk_reader.npz", **out)
+    print("phase vtk: done")
+
+
 PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem, "analytics": phase_analytics,
-          "steps": phase_steps}
+          "steps": phase_steps, "vtk": phase_vtk}
 
 if __name__ == "__main__":
     if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
