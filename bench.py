@@ -197,12 +197,15 @@ def reference_numpy_record():
     sources are not on this host, so the figure is read, not re-measured."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle", "reference_timing.json")
     try:
-        rows = json.load(open(path))["reference_numpy"]
-    except (OSError, KeyError, ValueError):
+        legs = json.load(open(path))["legs"]
+        first = next(iter(legs.values()))[0]
+    except (OSError, KeyError, ValueError, StopIteration, IndexError):
         return None
-    keep = ("value", "unit", "processes", "particles", "steps", "seconds", "cpu", "host_cores", "machine", "sample")
-    return {"kind": "reference", "measured_by": "oracle/reference_timing.py on a machine with the reference sources (CPU in each row)",
-            "rows": [{k: r.get(k) for k in keep} for r in rows]}
+    keep = ("value", "unit", "processes", "seconds", "sample")
+    return {"kind": "reference",
+            "measured_by": "oracle/reference_timing.py on a machine with the reference sources",
+            "cpu": first.get("cpu"), "host_cores": first.get("host_cores"), "machine": first.get("machine"),
+            "legs": {leg: [{k: r.get(k) for k in keep} for r in rows] for leg, rows in legs.items()}}
 
 
 def run_reference(a, world, rank):
