@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JT_ABI_VERSION 2
+#define JT_ABI_VERSION 3
 
 /* ---- return codes ------------------------------------------------------ */
 #define JT_OK 0
@@ -336,6 +336,22 @@ typedef struct {
 
 /* ABI / diagnostics */
 int jt_abi_version(void);
+
+/* Device memory for the library's own scratch: the device builds
+ * (jt_octree_build_device, jt_fem_grid_build_device) and the arrays their
+ * handles hold until the matching _free_device, and the count of
+ * jt_mark_near_degenerate.  Every other entry point works in caller buffers.
+ * By default that scratch comes from cudaMallocAsync / cudaFreeAsync on the
+ * call's stream; a caller that owns the device's memory (a framework's pool)
+ * installs its own pair here and the library allocates nothing itself.
+ * alloc(bytes, stream, ctx) returns a device pointer usable in stream order
+ * on `stream`, or NULL (the call then fails with JT_ERR_CUDA); free(ptr,
+ * stream, ctx) releases it in stream order.  Both NULL restore the default.
+ * Install before the calls that allocate, not while one runs, and release
+ * handles with the allocator that made them. */
+typedef void* (*jt_alloc_fn)(size_t bytes, void* stream, void* ctx);
+typedef void (*jt_free_fn)(void* ptr, void* stream, void* ctx);
+int jt_set_allocator(jt_alloc_fn alloc, jt_free_fn free_fn, void* ctx);
 const char* jt_last_error(void);
 /* sizes of the public structs, in the order: jt_blend, jt_grid_field,
  * jt_octree_node, jt_mesh_field, jt_nearest_field, jt_field, jt_boundary,

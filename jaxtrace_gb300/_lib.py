@@ -16,7 +16,7 @@ from . import _build
 i32, i64, f32, vp = C.c_int32, C.c_int64, C.c_float, C.c_void_p
 
 # ---- constants (mirror of the header) ------------------------------------
-ABI_VERSION = 2
+ABI_VERSION = 3
 JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STATUS = 0, -1, -2, -3, -4, -5
 JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
 JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2
@@ -201,6 +201,7 @@ def load(build_if_missing: bool = True):
         "jt_adjoint_workspace_bytes": (C.c_size_t, [i64, i32]),
         "jt_stage_fields": (i32, [P(Field), vp, vp, i32, i32, vp, vp]),
         "jt_stage_tile_fields": (i32, [P(Field), vp, vp, i32, vp, vp]),
+        "jt_set_allocator": (i32, [ALLOC_FN, FREE_FN, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -216,7 +217,44 @@ def load(build_if_missing: bool = True):
     if n != len(want) or [int(out[k]) for k in range(n)] != want:
         raise ImportError(f"jaxtrace_gb300 struct layouts differ from the library's: {list(out)[:max(n, 0)]} vs {want}")
     _lib = lib
+    use_torch_allocator(lib)
     return lib
+
+
+# jt_set_allocator callback types: alloc(bytes, stream, ctx) -> ptr, free(ptr, stream, ctx)
+ALLOC_FN = C.CFUNCTYPE(vp, C.c_size_t, vp, vp)
+FREE_FN = C.CFUNCTYPE(None, vp, vp, vp)
+_ALLOCATOR = []       # the installed callbacks, kept alive while the library holds them
+
+
+def _torch_alloc(nbytes, stream, ctx):
+    try:
+        import torch
+        return torch.cuda.caching_allocator_alloc(max(int(nbytes), 1), stream=int(stream or 0))
+    except Exception:      # noqa: BLE001 -- NULL is the allocator's failure value; the call reports it
+        return None
+
+
+def _torch_free(ptr, stream, ctx):
+    if ptr:
+        import torch
+        torch.cuda.caching_allocator_delete(int(ptr))
+
+
+def use_torch_allocator(lib=None) -> bool:
+    """Route the library's own device scratch (the device octree and hash-grid
+    builds, the near-degenerate count) through torch's caching allocator, so
+    that all device memory the library touches belongs to the caller's pool
+    (jt_set_allocator).  Done on load when CUDA is visible; returns whether it
+    was installed."""
+    import torch
+    if not torch.cuda.is_available():
+        return False
+    lib = lib or load()
+    if not _ALLOCATOR:
+        _ALLOCATOR.extend([ALLOC_FN(_torch_alloc), FREE_FN(_torch_free)])
+    check(lib.jt_set_allocator(_ALLOCATOR[0], _ALLOCATOR[1], None))
+    return True
 
 
 def check(rc: int) -> int:

@@ -156,6 +156,36 @@ static int check_integ(int i) {
 
 using namespace jt;
 
+namespace jt {
+
+static jt_alloc_fn g_alloc = nullptr;
+static jt_free_fn g_free = nullptr;
+static void* g_alloc_ctx = nullptr;
+
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+    *p = nullptr;
+    if (g_alloc == nullptr) return cudaMallocAsync(p, bytes, s);
+    *p = g_alloc(bytes, (void*)s, g_alloc_ctx);
+    return *p != nullptr ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+
+void dev_free(void* p, cudaStream_t s) {
+    if (p == nullptr) return;
+    if (g_free == nullptr) cudaFreeAsync(p, s);
+    else g_free(p, (void*)s, g_alloc_ctx);
+}
+
+}  // namespace jt
+
+extern "C" int jt_set_allocator(jt_alloc_fn alloc, jt_free_fn free_fn, void* ctx) {
+    if ((alloc == nullptr) != (free_fn == nullptr))
+        return set_error(JT_ERR_INVALID, "give both alloc and free, or neither (the default)");
+    g_alloc = alloc;
+    g_free = free_fn;
+    g_alloc_ctx = ctx;
+    return JT_OK;
+}
+
 extern "C" int jt_abi_version(void) { return JT_ABI_VERSION; }
 
 extern "C" const char* jt_last_error(void) { return g_last_error.c_str(); }

@@ -192,7 +192,7 @@ struct DevFemGrid {
     cudaStream_t s = nullptr;
     ~DevFemGrid() {
         for (void* p : {(void*)cell_start, (void*)cell_elems, (void*)sub_start, (void*)sub_elems})
-            if (p != nullptr) cudaFreeAsync(p, s);
+            if (p != nullptr) dev_free(p, s);
     }
 };
 
@@ -205,21 +205,22 @@ struct Scratch {
     template <class T>
     T* get(size_t count) {
         void* p = nullptr;
-        if (err == cudaSuccess && n < 16) err = cudaMallocAsync(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16, s);
+        if (err == cudaSuccess && n >= 16) err = cudaErrorMemoryAllocation;  // more scratch arrays than slots
+        if (err == cudaSuccess) err = dev_alloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16, s);
         if (err != cudaSuccess || p == nullptr) return nullptr;
         ptrs[n++] = p;
         return static_cast<T*>(p);
     }
     ~Scratch() {
         for (int i = 0; i < n; ++i)
-            if (ptrs[i] != nullptr) cudaFreeAsync(ptrs[i], s);
+            if (ptrs[i] != nullptr) dev_free(ptrs[i], s);
     }
 };
 
 template <class T>
-T* dev_alloc(size_t count, cudaStream_t s, cudaError_t& err) {
+T* dev_array(size_t count, cudaStream_t s, cudaError_t& err) {
     void* p = nullptr;
-    if (err == cudaSuccess) err = cudaMallocAsync(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16, s);
+    if (err == cudaSuccess) err = dev_alloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 16, s);
     return static_cast<T*>(p);
 }
 
@@ -297,7 +298,7 @@ extern "C" int jt_fem_grid_build_device(const float* points, int32_t n_points, c
     // the scanned counts are the cell starts; a second counter array gives the cursors
     H->cell_start = reinterpret_cast<int32_t*>(ccount);
     sc.ptrs[2] = nullptr;  // owned by the handle from here
-    H->cell_elems = dev_alloc<int32_t>(n_entries, s, e);
+    H->cell_elems = dev_array<int32_t>(n_entries, s, e);
     int* ctmp = sc.get<int>(n_entries);
     uint32_t* cursor = sc.get<uint32_t>((size_t)n_cells);
     if (e == cudaSuccess) e = sc.err;
@@ -325,7 +326,7 @@ extern "C" int jt_fem_grid_build_device(const float* points, int32_t n_points, c
     }
     k_fem_rank_sort<<<fem_blocks(n_cells * 32), kFemBlock, 0, s>>>(n_cells, ccount, ctmp, H->cell_elems);
     if (sub_div > 0 && n_entries > 0) {
-        uint32_t* scount = dev_alloc<uint32_t>((size_t)n_sub + 1, s, e);
+        uint32_t* scount = dev_array<uint32_t>((size_t)n_sub + 1, s, e);
         H->sub_start = reinterpret_cast<int32_t*>(scount);
         if (e == cudaSuccess) e = cudaMemsetAsync(scount, 0, sizeof(uint32_t) * ((size_t)n_sub + 1), s);
         if (e != cudaSuccess) {
@@ -344,7 +345,7 @@ extern "C" int jt_fem_grid_build_device(const float* points, int32_t n_points, c
         }
         H->n_sub = n_sub;
         H->n_sub_entries = n_sub_entries;
-        H->sub_elems = dev_alloc<int32_t>(n_sub_entries, s, e);
+        H->sub_elems = dev_array<int32_t>(n_sub_entries, s, e);
         int* stmp = sc.get<int>(n_sub_entries);
         uint32_t* scursor = sc.get<uint32_t>((size_t)n_sub);
         if (e == cudaSuccess) e = sc.err;
@@ -356,7 +357,7 @@ extern "C" int jt_fem_grid_build_device(const float* points, int32_t n_points, c
         k_fem_subs<1><<<gb, kFemBlock, 0, s>>>(n_tets, crange, tet_box, G, scursor, scount, stmp);
         k_fem_rank_sort<<<fem_blocks(n_sub * 32), kFemBlock, 0, s>>>(n_sub, scount, stmp, H->sub_elems);
     } else {
-        H->sub_start = dev_alloc<int32_t>(1, s, e);
+        H->sub_start = dev_array<int32_t>(1, s, e);
         if (e == cudaSuccess) e = cudaMemsetAsync(H->sub_start, 0, sizeof(int32_t), s);
         if (e != cudaSuccess) {
             delete H;

@@ -18,6 +18,12 @@ int check_grid_shape(const jt_grid_field& g);
 // tiles[] of an affine-tile storage against the grid shape, and its base array
 int check_tiles(const jt_grid_field& g);
 
+// Device scratch of the library's own (the device builds and their handles,
+// the near-degenerate count): through the allocator jt_set_allocator
+// installed, else cudaMallocAsync / cudaFreeAsync, ordered on `s`.
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+
 // Exclusive scan of n uint32 values in place (n <= scan_capacity()); sums
 // holds scan_partials(n) values, sums2 one.
 int64_t scan_capacity();

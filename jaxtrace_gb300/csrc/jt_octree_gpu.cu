@@ -373,13 +373,13 @@ struct Pool {
     template <class T>
     T* get(size_t n) {
         void* p = nullptr;
-        if (err == cudaSuccess) err = cudaMallocAsync(&p, n * sizeof(T) > 0 ? n * sizeof(T) : 16, s);
+        if (err == cudaSuccess) err = dev_alloc(&p, n * sizeof(T) > 0 ? n * sizeof(T) : 16, s);
         if (err != cudaSuccess) return nullptr;
         ptrs.push_back(p);
         return static_cast<T*>(p);
     }
     ~Pool() {
-        for (void* p : ptrs) cudaFreeAsync(p, s);
+        for (void* p : ptrs) dev_free(p, s);
     }
 };
 
@@ -503,9 +503,9 @@ extern "C" int jt_octree_build_device(const float* points, int32_t n_points, con
     DevOctree* T = new (std::nothrow) DevOctree();
     if (T == nullptr) return set_error(JT_ERR_NOMEM, "out of host memory");
     T->n_nodes = n_nodes;
-    if ((e = cudaMallocAsync((void**)&T->nodes, sizeof(jt_octree_node) * (size_t)n_nodes, s)) != cudaSuccess ||
-        (e = cudaMallocAsync((void**)&T->bounds, 6 * sizeof(float) * (size_t)n_nodes, s)) != cudaSuccess) {
-        if (T->nodes) cudaFreeAsync(T->nodes, s);
+    if ((e = dev_alloc((void**)&T->nodes, sizeof(jt_octree_node) * (size_t)n_nodes, s)) != cudaSuccess ||
+        (e = dev_alloc((void**)&T->bounds, 6 * sizeof(float) * (size_t)n_nodes, s)) != cudaSuccess) {
+        if (T->nodes) dev_free(T->nodes, s);
         delete T;
         return cuda_status(e, "octree node allocation");
     }
@@ -515,8 +515,8 @@ extern "C" int jt_octree_build_device(const float* points, int32_t n_points, con
     int* tmp = pool.get<int>(n);
     if (pool.err == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)n_nodes, s);
     if (pool.err != cudaSuccess || e != cudaSuccess) {
-        cudaFreeAsync(T->nodes, s);
-        cudaFreeAsync(T->bounds, s);
+        dev_free(T->nodes, s);
+        dev_free(T->bounds, s);
         delete T;
         return cuda_status(pool.err != cudaSuccess ? pool.err : e, "octree element allocation");
     }
@@ -531,8 +531,8 @@ extern "C" int jt_octree_build_device(const float* points, int32_t n_points, con
     k_oct_scatter<<<blocks(n), kOctBlock, 0, s>>>(n, leaf_of, flat_off, cursor, tmp);
     k_oct_sort_leaves<<<blocks((int64_t)n_nodes * 32), kOctBlock, 0, s>>>(n_nodes, flat_off, flat_cnt, tmp, elems);
     if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess) {
-        cudaFreeAsync(T->nodes, s);
-        cudaFreeAsync(T->bounds, s);
+        dev_free(T->nodes, s);
+        dev_free(T->bounds, s);
         delete T;
         return cuda_status(e, "octree build kernels");
     }
@@ -562,8 +562,8 @@ extern "C" void jt_octree_free_device(void* handle, void* stream) {
     DevOctree* T = static_cast<DevOctree*>(handle);
     if (T == nullptr) return;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaFreeAsync(T->nodes, s);
-    cudaFreeAsync(T->bounds, s);
+    dev_free(T->nodes, s);
+    dev_free(T->bounds, s);
     delete T;
 }
 
@@ -574,7 +574,7 @@ extern "C" int jt_mark_near_degenerate(float* tet_box, const float* tet_geom, in
         return set_error(JT_ERR_INVALID, "tet_box and tet_geom are required");
     cudaStream_t s = (cudaStream_t)stream;
     int* d = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&d, sizeof(int), s);
+    cudaError_t e = dev_alloc((void**)&d, sizeof(int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(int), s);
     if (e == cudaSuccess && n_tets > 0) {
         k_mark_near_degenerate<<<(unsigned)((n_tets + kOctBlock - 1) / kOctBlock), kOctBlock, 0, s>>>(tet_box, tet_geom,
@@ -584,7 +584,7 @@ extern "C" int jt_mark_near_degenerate(float* tet_box, const float* tet_geom, in
     int h = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (d != nullptr) cudaFreeAsync(d, s);
+    if (d != nullptr) dev_free(d, s);
     if (e != cudaSuccess) return cuda_status(e, "near-degenerate marking");
     if (count_out != nullptr) *count_out = h;
     return JT_OK;

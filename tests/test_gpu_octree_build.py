@@ -75,3 +75,38 @@ def test_octree_field_runs_on_the_device_build(golden):
         tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
         out.append(tr.track_particles(c["x0"], c["time_span"], c["n_timesteps"], dt=c["dt"]).positions)
     assert np.array_equal(out[0], out[1])
+
+
+def test_device_builds_allocate_through_the_installed_allocator():
+    """jt_set_allocator: the device builds take every scratch and handle
+    array from the caller's allocator (here a counting wrapper around
+    torch's caching allocator) and give all of it back."""
+    import torch
+    calls = {"alloc": 0, "free": 0, "live": set()}
+
+    def alloc(n, stream, ctx):
+        p = torch.cuda.caching_allocator_alloc(max(int(n), 1), stream=int(stream or 0))
+        calls["alloc"] += 1
+        calls["live"].add(p)
+        return p
+
+    def free(p, stream, ctx):
+        calls["free"] += 1
+        calls["live"].discard(int(p))
+        torch.cuda.caching_allocator_delete(int(p))
+
+    fa, ff = L.ALLOC_FN(alloc), L.FREE_FN(free)
+    lib = L.load()
+    L.check(lib.jt_set_allocator(fa, ff, None))
+    try:
+        P, T4 = W.kuhn_mesh(8, 0.2, 1)
+        h, d = _same_build(P, T4, 32, 12)
+        n_oct = calls["alloc"]
+        g = jt.FemHashGrid(P, T4, 8, build="device")
+        assert g.dev is not None and calls["alloc"] > n_oct
+        del g, d
+        torch.cuda.synchronize()
+    finally:
+        L.check(lib.jt_set_allocator(L._ALLOCATOR[0], L._ALLOCATOR[1], None))
+    assert calls["alloc"] > 10
+    assert calls["free"] == calls["alloc"] and not calls["live"]
