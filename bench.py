@@ -63,6 +63,7 @@ def args_parse():
     p.add_argument("--no-fem", action="store_true")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--fem-steps", type=int, default=1000)
+    p.add_argument("--fem-hash-sub-div", type=int, default=None, help="hash-grid sub-cells per axis of a cell (default: automatic)")
     p.add_argument("--adj-lattice", default="256,256,64", help="seed lattice of the adjoint leg")
     p.add_argument("--adj-steps", type=int, default=500)
     p.add_argument("--density-particles", type=int, default=16_000_000)
@@ -471,14 +472,14 @@ def octree_build_times(c):
 
 def fem_hash_leg(a, profile=False):
     """The unstructured FEM configuration through the hash-grid field alone
-    (FEMTimeSeriesField, 32^3 cells, 4^3 sub-cells): one timed pass of
+    (FEMTimeSeriesField, 32^3 cells, automatic sub-cells): one timed pass of
     ``--fem-steps`` steps (with --profile bracketed by cudaProfilerStart/Stop)."""
     import torch
 
     import jaxtrace_gb300 as jt
     from jaxtrace_gb300 import workloads as W
     c = W.fem_case(n_steps=a.fem_steps)
-    f = jt.FEMTimeSeriesField(c["data"], c["times"], c["points"], c["tets"])
+    f = jt.FEMTimeSeriesField(c["data"], c["times"], c["points"], c["tets"], sub_div=a.fem_hash_sub_div)
     bc = jt.mixed_boundary(W.UNIT, c["conditions"])
     tr = jt.create_tracker("rk4", f, bc, record_final_only=True)
     times = np.linspace(c["time_span"][0], c["time_span"][1], c["n_timesteps"], dtype=np.float32)
@@ -504,7 +505,7 @@ def fem_hash_leg(a, profile=False):
 
 
 def fem_grid_build_times(c):
-    """Hash grid (32^3 cells, 4^3 sub-cells each) of the FEM mesh from host
+    """Hash grid (32^3 cells, automatic sub-cells) of the FEM mesh from host
     arrays: the host builder with its NumPy element records, and the device
     builder (host->device copy of points and connectivity included)."""
     import torch

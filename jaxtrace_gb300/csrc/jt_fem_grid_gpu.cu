@@ -229,7 +229,7 @@ inline unsigned fem_blocks(int64_t n) { return (unsigned)((n + kFemBlock - 1) / 
 // counts -> CSR start (n_lists + 1 values, the last the total), in place
 int csr_start(uint32_t* count, int64_t n_lists, Scratch& sc, uint32_t* total, cudaStream_t s) {
     uint32_t* sums = sc.get<uint32_t>((size_t)scan_partials(n_lists + 1));
-    uint32_t* sums2 = sc.get<uint32_t>(1);
+    uint32_t* sums2 = sc.get<uint32_t>((size_t)scan_partials2(n_lists + 1));
     if (sc.err != cudaSuccess) return cuda_status(sc.err, "hash grid scan allocation");
     int rc = exclusive_scan_u32(count, n_lists + 1, sums, sums2, s);
     if (rc != JT_OK) return rc;

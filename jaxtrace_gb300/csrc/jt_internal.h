@@ -25,9 +25,11 @@ cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
 void dev_free(void* p, cudaStream_t s);
 
 // Exclusive scan of n uint32 values in place (n <= scan_capacity()); sums
-// holds scan_partials(n) values, sums2 one.
+// holds scan_partials(n) values, sums2 scan_partials2(n) (one up to
+// 2^22 items).
 int64_t scan_capacity();
 int64_t scan_partials(int64_t n);
+int64_t scan_partials2(int64_t n);
 int exclusive_scan_u32(uint32_t* data, int64_t n, uint32_t* sums, uint32_t* sums2, cudaStream_t st);
 
 struct StageBlends;

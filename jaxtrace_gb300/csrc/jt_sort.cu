@@ -104,17 +104,32 @@ static int64_t n_bins(int bits) { return (int64_t)1 << (3 * bits); }
 
 static int64_t scan_blocks(int64_t n) { return (n + kScanItems - 1) / kScanItems; }
 
-int64_t scan_capacity() { return (int64_t)kScanItems * kScanItems; }
+int64_t scan_capacity() { return (int64_t)kScanItems * kScanItems * kScanItems; }
 
 int64_t scan_partials(int64_t n) { return scan_blocks(n); }
 
+int64_t scan_partials2(int64_t n) {
+    const int64_t nb = scan_blocks(n);
+    return nb > kScanItems ? scan_blocks(nb) + 1 : 1;
+}
+
+// Block scans, then the scan of the block totals: one block when they fit
+// one (n <= kScanItems^2), else the same two levels again on them (sums2
+// holds their block totals and the last total).
 int exclusive_scan_u32(uint32_t* data, int64_t n, uint32_t* sums, uint32_t* sums2, cudaStream_t st) {
     if (n <= 0) return JT_OK;
     if (n > scan_capacity()) return set_error(JT_ERR_UNSUPPORTED, "scan of %lld items exceeds %lld", (long long)n,
                                               (long long)scan_capacity());
     const int64_t nb = scan_blocks(n);
     k_scan_blocks<<<(unsigned)nb, kScanBlock, 0, st>>>(data, n, sums);
-    k_scan_blocks<<<1, kScanBlock, 0, st>>>(sums, nb, sums2);
+    if (nb <= kScanItems) {
+        k_scan_blocks<<<1, kScanBlock, 0, st>>>(sums, nb, sums2);
+    } else {
+        const int64_t nb2 = scan_blocks(nb);
+        k_scan_blocks<<<(unsigned)nb2, kScanBlock, 0, st>>>(sums, nb, sums2);
+        k_scan_blocks<<<1, kScanBlock, 0, st>>>(sums2, nb2, sums2 + nb2);
+        k_scan_add<<<(unsigned)nb2, kScanBlock, 0, st>>>(sums, nb, sums2);
+    }
     k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(data, n, sums);
     return cuda_status(cudaGetLastError(), "scan launch");
 }

@@ -634,6 +634,28 @@ class TimeSeriesField(_DeviceField):
 
 
 # ---------------------------------------------------------------------------
+def auto_sub_div(P, T4, cell64, sample: int = 4096, max_entries: int = 1 << 30) -> int:
+    """Sub-cells per hash-cell axis such that a sub-cell edge is about a sixth
+    of the median element box edge (measured on an even sample of elements),
+    in 1..16, lowered while the estimated list entries (elements x sub-cells
+    their boxes meet) exceed ``max_entries``.  On the FEM configuration
+    (64^3 x 6 jittered tetrahedra, 32^3 cells) it gives 10: 1.60e9
+    particle-steps/s against 1.30e9 with 4 and 1.49e9 with 8."""
+    M = len(T4)
+    if M == 0:
+        return 1
+    idx = np.linspace(0, M - 1, min(M, sample)).astype(np.int64)
+    V = np.asarray(P, dtype=np.float64)[np.asarray(T4)[idx]]
+    edge = float(np.median((V.max(axis=1) - V.min(axis=1)).max(axis=1)))
+    cell = float(np.min(cell64))
+    if not edge > 0 or not cell > 0:
+        return 1
+    S = int(min(16, max(1, round(6.0 * cell / edge))))
+    while S > 1 and M * (edge / (cell / S) + 1.0) ** 3 > max_entries:
+        S -= 1
+    return S
+
+
 class FemHashGrid:
     """Spatial hash grid of build_tetrahedral_mesh (fem_interpolator.py:36-143),
     built with array operations instead of the per-element loop but with the
@@ -652,11 +674,15 @@ class FemHashGrid:
     _HOST = ("cell_start", "cell_elems", "sub_start", "sub_elems", "cell_elem_counts", "tet_box", "tet_geom",
              "element_bounds")
 
-    def __init__(self, points, connectivity, grid_resolution: int = 32, sub_div: int = 4, build: str = "auto"):
+    def __init__(self, points, connectivity, grid_resolution: int = 32, sub_div: Optional[int] = None,
+                 build: str = "auto"):
         """``build``: "host" (jt_fem_grid_build and NumPy element records),
         "device" (jt_fem_grid_build_device: the same arrays, kept on the GPU
         in ``dev``, host copies made on first use) or "auto" (device when
-        CUDA is visible and the grid is within the device build's limits)."""
+        CUDA is visible and the grid is within the device build's limits).
+        ``sub_div``: sub-cells per cell axis (any value gives the same first
+        hits); None picks sub-cells about a sixth of a typical element box
+        (``auto_sub_div``)."""
         if build not in ("auto", "host", "device"):
             raise ValueError(f"build must be 'auto', 'host' or 'device', got {build!r}")
         P = np.asarray(points, dtype=F32)
@@ -678,6 +704,8 @@ class FemHashGrid:
         self.grid_min = bmin.astype(F32)
         self.cell_size64 = cell64
         self.grid_cell_size = cell64.astype(F32)
+        if sub_div is None:
+            sub_div = auto_sub_div(P, T4, cell64)
         self.dev = None
         use_device = build == "device"
         if build == "auto":
@@ -818,7 +846,7 @@ class FEMTimeSeriesField(TimeSeriesField):
 
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
-                 fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: int = 4,
+                 fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: Optional[int] = None,
                  grid_build: str = "auto"):
         super().__init__(data, times, positions, interpolation, extrapolation, _source_info, storage=storage,
                          time_semantics="jax")

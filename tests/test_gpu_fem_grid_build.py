@@ -51,14 +51,19 @@ def test_device_hash_grid_on_a_shuffled_mesh():
     _same(P, T4[np.random.default_rng(9).permutation(len(T4))], 12, 4)
 
 
-def test_grids_beyond_the_device_build_go_to_the_host_builder():
-    """64^3 cells x 4^3 sub-cells exceed the device build's scan: "device"
-    says so, "auto" builds on the host."""
+def test_grids_beyond_the_device_build_are_refused_before_allocating():
+    """128^3 cells x 16^3 sub-cells (8.6e9 lists) exceed the device build's
+    three-level scan: "device" says so before it allocates anything."""
     P, T4 = W.kuhn_mesh(4)[:2]
     with pytest.raises(NotImplementedError, match="exceeds"):
-        jt.FemHashGrid(P, T4, 64, sub_div=4, build="device")
-    a = jt.FemHashGrid(P, T4, 64, sub_div=4)
-    assert a.dev is None and a.sub_div == 4
+        jt.FemHashGrid(P, T4, 128, sub_div=16, build="device")
+
+
+def test_device_build_with_more_lists_than_one_scan_level():
+    """32^3 cells x 10^3 sub-cells: 32.8M sub-cell lists, beyond the
+    two-level scan (2^22), built on the device identical to the host."""
+    P, T4 = W.kuhn_mesh(10)[:2]
+    _same(P, T4, 32, 10)
 
 
 def test_fem_field_runs_on_the_device_build():
