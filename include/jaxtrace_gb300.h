@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JT_ABI_VERSION 3
+#define JT_ABI_VERSION 4
 
 /* ---- return codes ------------------------------------------------------ */
 #define JT_OK 0
@@ -208,6 +208,16 @@ typedef struct {
     const jt_octree_node* nodes; /* device (n_nodes)                        */
     const int32_t* elems;   /* device element lists                           */
     const void* pairs;      /* device value pairs, layout as jt_grid_field   */
+    /* Optional compact copy of the tree for the descent (NULL: descend on
+     * nodes).  Nodes in breadth-first order, the root first and the present
+     * children of a node consecutive in octant order: desc (n_nodes,4) holds
+     * the centre's float32 bits and mask | first << 8, mask the present
+     * octants (0 for a leaf) and first the breadth-first index of the first
+     * child (< 2^24); dtab (n_nodes,2) holds the node's elem_offset and
+     * elem_count.  One 16-byte load per level instead of two dependent
+     * loads, the same moves as the node records. */
+    const int32_t* desc;
+    const int32_t* dtab;
 } jt_mesh_field;
 
 /* Nearest-node field: TimeSeriesField spatial sampling (time_series.py:391)

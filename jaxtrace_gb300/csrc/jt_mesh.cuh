@@ -134,16 +134,33 @@ struct MeshFieldT {
         // fixed-depth descent (…optimized.py:278-302): at most max_depth moves,
         // stopping at a leaf or where the query's octant has no child
         int node = 0;
-        for (int d = 0; d < F.max_depth; ++d) {
-            const int4 h = __ldg(reinterpret_cast<const int4*>(F.nodes + node));
-            if (h.w) break;  // is_leaf
-            const int oct = (q.x >= __int_as_float(h.x) ? 1 : 0) + (q.y >= __int_as_float(h.y) ? 2 : 0) +
-                            (q.z >= __int_as_float(h.z) ? 4 : 0);
-            const int ch = __ldg(&F.nodes[node].children[oct]);
-            if (ch < 0) break;
-            node = ch;
+        int2 oc;
+        if (F.desc != nullptr) {
+            // the same moves on the breadth-first copy: a child's index is the
+            // node's first child plus the present octants below its own
+            const int4* D = reinterpret_cast<const int4*>(F.desc);
+            for (int d = 0; d < F.max_depth; ++d) {
+                const int4 h = __ldg(D + node);
+                const unsigned w = (unsigned)h.w, m = w & 0xffu;
+                if (m == 0u) break;  // a leaf (or a node without children)
+                const int oct = (q.x >= __int_as_float(h.x) ? 1 : 0) + (q.y >= __int_as_float(h.y) ? 2 : 0) +
+                                (q.z >= __int_as_float(h.z) ? 4 : 0);
+                if (!((m >> oct) & 1u)) break;
+                node = (int)(w >> 8) + __popc(m & ((1u << oct) - 1u));
+            }
+            oc = __ldg(reinterpret_cast<const int2*>(F.dtab) + node);
+        } else {
+            for (int d = 0; d < F.max_depth; ++d) {
+                const int4 h = __ldg(reinterpret_cast<const int4*>(F.nodes + node));
+                if (h.w) break;  // is_leaf
+                const int oct = (q.x >= __int_as_float(h.x) ? 1 : 0) + (q.y >= __int_as_float(h.y) ? 2 : 0) +
+                                (q.z >= __int_as_float(h.z) ? 4 : 0);
+                const int ch = __ldg(&F.nodes[node].children[oct]);
+                if (ch < 0) break;
+                node = ch;
+            }
+            oc = __ldg(reinterpret_cast<const int2*>(&F.nodes[node].elem_offset));
         }
-        const int2 oc = __ldg(reinterpret_cast<const int2*>(&F.nodes[node].elem_offset));
         const int32_t* L = F.elems + oc.x;
         const int cnt = oc.y;
         // candidate scan (…optimized.py:309-360): first candidate whose box

@@ -891,6 +891,37 @@ class FEMTimeSeriesField(TimeSeriesField):
                 f"interpolation='{self.interpolation}', extrapolation='{self.extrapolation}')")
 
 
+def breadth_first_descent(nodes: np.ndarray):
+    """The compact descent arrays of jt_mesh_field (desc, dtab) from the
+    octree's node records: nodes renumbered breadth-first from the root, the
+    present children of a node consecutive in octant order, so that a child's
+    index is the node's first child plus the present octants below it.
+    Returns (desc (K,4) int32: centre bits and mask | first << 8, dtab (K,2)
+    int32: elem_offset, elem_count), or None when a first-child index would
+    not fit 24 bits."""
+    K = len(nodes)
+    children = np.asarray(nodes["children"], dtype=np.int64)
+    order, level = [], np.array([0], dtype=np.int64)
+    while len(level):
+        order.append(level)
+        ch = children[level]
+        level = ch[ch >= 0]                    # node order, then octant order
+    order = np.concatenate(order)
+    if len(order) != K or K >= (1 << 24):
+        return None
+    ch = children[order]                        # (K, 8) DFS ids, -1 absent
+    present = ch >= 0
+    mask = (present * (1 << np.arange(8))).sum(axis=1)
+    count = present.sum(axis=1)
+    first = 1 + np.concatenate([[0], np.cumsum(count)[:-1]])   # children follow in BFS order
+    first = np.where(count > 0, first, 0)
+    desc = np.empty((K, 4), dtype=np.int32)
+    desc[:, :3] = np.asarray(nodes["c"], dtype=np.float32)[order].view(np.int32)
+    desc[:, 3] = (mask | (first << 8)).astype(np.uint32).view(np.int32)
+    dtab = np.stack([nodes["elem_offset"][order], nodes["elem_count"][order]], axis=1).astype(np.int32)
+    return desc, dtab
+
+
 class OctreeMesh:
     """The octree in the reference's array layout (OctreeMeshOptimized,
     octree_fem_interpolator_optimized.py:18-38).
@@ -1048,6 +1079,10 @@ class OctreeFEMTimeSeriesFieldOptimized(_DeviceField):
         f.points, f.tet_box, f.tet_geom = d["points"].data_ptr(), d["tet_box"].data_ptr(), d["tet_geom"].data_ptr()
         f.nodes, f.elems, f.pairs = d["nodes"].data_ptr(), d["elems"].data_ptr(), pairs.data_ptr()
         f.near_degenerate = int(self.n_near_degenerate > 0)
+        bfs = breadth_first_descent(m.nodes)
+        if bfs is not None:
+            d["desc"], d["dtab"] = (torch.from_numpy(a).cuda() for a in bfs)
+            f.desc, f.dtab = d["desc"].data_ptr(), d["dtab"].data_ptr()
         self._cmesh = f
         self._cfield = L.Field(kind=L.JT_FIELD_MESH, mesh=C.pointer(f))
 
