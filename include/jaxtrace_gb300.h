@@ -70,8 +70,10 @@ extern "C" {
 #define JT_STORE_STAGE_F32Q 8 /* float32 yz-quads per node (48 B): the (x,y) of
                                 nodes (j,k), (j,k1), (j1,k), (j1,k1) in a
                                 32 B part A; their z in a 16 B part B stored
-                                after the part-A records of all nodes of the
-                                slot (slot = nodes * 48 B)                   */
+                                after the part-A records of the slot.  A
+                                slot holds S = nodes rounded up to even
+                                records (S * 48 B; pair_stride = S), so each
+                                starts 32-byte aligned                       */
 /* Affine-tile snapshots of a regular grid (input of jt_stage_tile_fields).
  * The grid's cells are cut into tiles of JT_TILE^3 cells; tile (tx,ty,tz)
  * covers cells [JT_TILE*t, JT_TILE*t + JT_TILE) per axis and its
@@ -409,11 +411,12 @@ int jt_integrator_step(const jt_field* field, const jt_blend* stage_blends,
  * device (n) power-of-two scales for JT_STORE_STAGE_F16 (NULL for F32).
  * out_storage: JT_STORE_STAGE_F32 / _F32Q (from float32 snapshots, exact
  * blend) or JT_STORE_STAGE_F16 (from 16-bit snapshots).
- * out: device, n fields of nodes records of out_storage, field j at
- * out + j * nodes * record_bytes (16, 48 or 32 B).  The tracking launch then takes a
- * jt_grid_field with storage = out_storage, pairs = out, n_pairs = n,
- * pair_stride = nodes and entries whose pair is the slot j (and, for F16,
- * wa = out_scales[j]). */
+ * out: device (32-byte aligned; so must the field's pairs be), n fields of
+ * S records of out_storage, field j at out + j * S * record_bytes (16, 48 or
+ * 32 B), S = nodes, or nodes rounded up to even for F32Q.  The tracking
+ * launch then takes a jt_grid_field with storage = out_storage, pairs = out,
+ * n_pairs = n, pair_stride = S and entries whose pair is the slot j (and,
+ * for F16, wa = out_scales[j]). */
 int jt_stage_fields(const jt_field* field, const jt_blend* entries, const float* out_scales, int32_t n,
                     int32_t out_storage, void* out, void* stream);
 

@@ -51,6 +51,8 @@ static int check_nearest(const jt_nearest_field* q) {
         q->n_pairs < 1)
         return set_error(JT_ERR_INVALID, "nearest field has a NULL array");
     if (q->pair_stride < q->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
+    if (((uintptr_t)q->pairs & 31u) != 0)
+        return set_error(JT_ERR_INVALID, "pairs must be 32-byte aligned (256-bit records)");
     return check_storage(q->storage);
 }
 
@@ -90,6 +92,12 @@ static int check_field(const jt_field* f) {
                 return set_error(JT_ERR_UNSUPPORTED, "affine-tile snapshots are read by jt_stage_tile_fields only");
             if (g->pair_stride < (int64_t)g->nx * g->ny * g->nz)
                 return set_error(JT_ERR_INVALID, "pair_stride smaller than the node count");
+            // the gathers read 256-bit records (32-byte aligned); a float32-quad
+            // slot of pair_stride records keeps that alignment only for an even stride
+            if (((uintptr_t)g->pairs & 31u) != 0)
+                return set_error(JT_ERR_INVALID, "pairs must be 32-byte aligned (256-bit records)");
+            if (g->storage == JT_STORE_STAGE_F32Q && (g->pair_stride & 1) != 0)
+                return set_error(JT_ERR_INVALID, "JT_STORE_STAGE_F32Q needs an even pair_stride (slots of 32-byte records)");
             if (g->storage == JT_STORE_STAGE_F32 || g->storage == JT_STORE_STAGE_F16 ||
                 g->storage == JT_STORE_STAGE_F32Q)
                 return JT_OK;
@@ -105,6 +113,8 @@ static int check_field(const jt_field* f) {
                 return set_error(JT_ERR_INVALID, "mesh field has a NULL array");
             if (m->max_depth < 0) return set_error(JT_ERR_INVALID, "max_depth must be >= 0");
             if (m->pair_stride < m->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
+            if (((uintptr_t)m->pairs & 31u) != 0)
+                return set_error(JT_ERR_INVALID, "pairs must be 32-byte aligned (256-bit records)");
             return check_storage(m->storage);
         }
         case JT_FIELD_NEAREST: return check_nearest(f->nearest);

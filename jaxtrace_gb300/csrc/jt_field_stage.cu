@@ -38,10 +38,14 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32(jt_grid_field F, const jt_
 // node: its quad's four nodes (j,k), (j,k1), (j1,k), (j1,k1) blended with
 // the exact arithmetic of k_stage_f32, so the values are the same bits.
 template <bool EXACT>
+// A float32-quad slot holds S = stage_f32q_stride(N) part-A records (32 B)
+// then S part-B records (16 B): S is even, so every slot starts on a 32-byte
+// boundary for the tracking kernel's 256-bit loads.
 __global__ void __launch_bounds__(kBlock) k_stage_f32q(jt_grid_field F, const jt_blend* __restrict__ ent, int n,
                                                         char* __restrict__ out) {
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t N = F.pair_stride;
+    const int64_t S = N + (N & 1);
     if (node >= N) return;
     const int k = (int)(node % F.nz);
     const int j = (int)((node / F.nz) % F.ny);
@@ -66,11 +70,11 @@ __global__ void __launch_bounds__(kBlock) k_stage_f32q(jt_grid_field F, const jt
 #pragma unroll
         for (int c = 0; c < 4; ++c)
             v[c] = blend_cv<EXACT, JT_STORE_F32>(pv[c], e, splat(e.wa), splat(e.wb), e.form == JT_BLEND_WEIGHTED);
-        char* slot = out + (int64_t)jj * N * 48;
+        char* slot = out + (int64_t)jj * S * 48;
         float4* a = reinterpret_cast<float4*>(slot + node * 32);
         a[0] = make_float4(v[0].xy.x, v[0].xy.y, v[1].xy.x, v[1].xy.y);
         a[1] = make_float4(v[2].xy.x, v[2].xy.y, v[3].xy.x, v[3].xy.y);
-        reinterpret_cast<float4*>(slot + N * 32)[node] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
+        reinterpret_cast<float4*>(slot + S * 32)[node] = make_float4(v[0].z, v[1].z, v[2].z, v[3].z);
     }
 }
 
@@ -303,6 +307,8 @@ extern "C" int jt_stage_fields(const jt_field* field, const jt_blend* entries, c
     if (n == 0) return JT_OK;
     if (entries == nullptr || out == nullptr) return set_error(JT_ERR_INVALID, "entries and out are required");
     if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshot pairs");
+    if (((uintptr_t)out & 31u) != 0 || ((uintptr_t)F.pairs & 31u) != 0)
+        return set_error(JT_ERR_INVALID, "pairs and out must be 32-byte aligned (256-bit records)");
     const int64_t N = (int64_t)F.nx * F.ny * F.nz;
     if (F.pair_stride != N) return set_error(JT_ERR_INVALID, "pair_stride must equal the node count");
     const unsigned g = grid_blocks(N);
@@ -346,6 +352,8 @@ extern "C" int jt_stage_tile_fields(const jt_field* field, const jt_blend* entri
     if (entries == nullptr || out == nullptr || out_scales == nullptr)
         return set_error(JT_ERR_INVALID, "entries, out_scales and out are required");
     if (F.pairs == nullptr || F.n_pairs < 1) return set_error(JT_ERR_INVALID, "field has no snapshots");
+    if (((uintptr_t)out & 31u) != 0)
+        return set_error(JT_ERR_INVALID, "out must be 32-byte aligned (256-bit records)");
     const int64_t tiles = (int64_t)F.tiles[0] * F.tiles[1] * F.tiles[2];
     if (F.pair_stride != tiles * JT_TILE_NODES)
         return set_error(JT_ERR_INVALID, "pair_stride must be tiles * JT_TILE_NODES");

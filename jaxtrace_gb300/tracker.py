@@ -874,10 +874,13 @@ class _StageFields:
             self.src_field = field.jt_field()
         nodes = len(field.grid_x) * len(field.grid_y) * len(field.grid_z)
         rec = 12 if self.f32 else 8                                          # float32 words per node
-        self.buf = torch.empty(self.slots * nodes * rec, dtype=torch.float32, device=dev)
-        self.nodes, self.rec = nodes, rec
+        # float32-quad slots hold an even number of node records, so that
+        # every slot starts on a 32-byte boundary (jt_stage_fields)
+        stride = nodes + (nodes & 1) if self.f32 else nodes
+        self.buf = torch.empty(self.slots * stride * rec, dtype=torch.float32, device=dev)
+        self.nodes, self.rec, self.stride = nodes, rec, stride
         self.n_fields = int(self.uid[-1]) + 1 if len(self.uid) else 0
-        self.field_bytes = nodes * rec * 4
+        self.field_bytes = stride * rec * 4
         self.side = self.before = self.pending = None
         if self.overlap:
             self.side = torch.cuda.Stream(device=dev, priority=-1)
@@ -886,7 +889,7 @@ class _StageFields:
         C.memmove(C.byref(g), C.byref(g0), C.sizeof(L.GridField))            # copy the descriptor
         g.storage = self.out_storage
         g.n_pairs = self.slots
-        g.pair_stride = nodes
+        g.pair_stride = stride
         g.pairs = self.buf.data_ptr()
         g.tile_base = None
         g.tiles[:] = [0, 0, 0]
@@ -925,7 +928,7 @@ class _StageFields:
         for lo, run in runs:
             ent = self.src.data_ptr() + lo * 32
             sc = self.scales.data_ptr() + lo * 4
-            out = self.buf.data_ptr() + (lo % self.slots) * self.nodes * self.rec * 4
+            out = self.buf.data_ptr() + (lo % self.slots) * self.stride * self.rec * 4
             if self.tile:
                 L.check(self.lib.jt_stage_tile_fields(C.byref(self.src_field), C.c_void_p(ent), C.c_void_p(sc),
                                                       run, C.c_void_p(out), stream))

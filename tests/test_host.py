@@ -163,15 +163,15 @@ def test_new_entry_points_validate_before_touching_the_device():
     g.nx = g.ny = g.nz = 4
     g.pair_stride = 64
     g.n_pairs = 1
-    g.pairs = 16                     # never dereferenced: rejected first
+    g.pairs = 256                    # never dereferenced: rejected first
     f = L.Field(kind=L.JT_FIELD_GRID, grid=C.pointer(g))
     with pytest.raises(ValueError, match="out_storage"):
-        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, 7, C.c_void_p(16), None))
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(256), None, 3, 7, C.c_void_p(256), None))
     with pytest.raises(ValueError, match="out_scales"):
         g.storage = L.JT_STORE_BF16
-        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F16, C.c_void_p(16), None))
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(256), None, 3, L.JT_STORE_STAGE_F16, C.c_void_p(256), None))
     with pytest.raises(NotImplementedError, match="float32 stage fields"):
-        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(16), None))
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(256), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(256), None))
     assert lib.jt_stage_fields(C.byref(f), None, None, 0, L.JT_STORE_STAGE_F32, None, None) == 0
     # grid shapes the kernels index safely: axes of at most 2^24 nodes, < 2^31 nodes in all
     g.storage = L.JT_STORE_F32
@@ -179,7 +179,7 @@ def test_new_entry_points_validate_before_touching_the_device():
         g.nx, g.ny, g.nz = shape
         g.pair_stride = max(1, shape[0] * shape[1] * shape[2])
         with pytest.raises(ValueError, match="grid"):
-            L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(16), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(16),
+            L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(256), None, 3, L.JT_STORE_STAGE_F32, C.c_void_p(256),
                                         None))
     g.nx = g.ny = g.nz = 4
     g.pair_stride = 64
@@ -195,6 +195,17 @@ def test_new_entry_points_validate_before_touching_the_device():
     g.storage = L.JT_STORE_F32
     with pytest.raises(ValueError, match="block_size"):
         L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    # 256-bit records: pairs and stage outputs 32-byte aligned, float32-quad slots of an even stride
+    with pytest.raises(ValueError, match="32-byte aligned"):
+        L.check(lib.jt_stage_fields(C.byref(f), C.c_void_p(256), None, 3, L.JT_STORE_STAGE_F32Q, C.c_void_p(272),
+                                    None))
+    g.pairs = 272
+    with pytest.raises(ValueError, match="32-byte aligned"):
+        L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    g.pairs, g.storage, g.pair_stride = 256, L.JT_STORE_STAGE_F32Q, 65
+    with pytest.raises(ValueError, match="even pair_stride"):
+        L.check(lib.jt_track(C.byref(f), C.byref(bc), C.byref(p), None))
+    g.storage, g.pair_stride = L.JT_STORE_F32, 64
     # stage fields track without velocity recording (the host gathers pairs for it)
     p.block_size = 0
     p.traj, p.vel, p.record_every = 16, 16, 1
