@@ -1137,6 +1137,12 @@ def main():
     ok_bf16 = [v for v in ok if VARIANTS[v][0] == "bf16"]
     pool = ok_bf16 or ok or sixteen or list(results)
     head = max(pool, key=lambda v: results[v]["value"])
+    if world > 1:
+        # the error analysis runs on rank 0 alone: every rank takes its choice
+        import torch.distributed as dist
+        pick = torch.tensor([list(results).index(head)], dtype=torch.int64, device="cuda")
+        dist.broadcast(pick, src=0)
+        head = list(results)[int(pick.item())]
     fp32 = {k: results[k]["value"] for k in ("f32", "f32c") if k in results}
     line = {"metric": METRIC, "value": results[head]["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": results[head]["ms_per_step"], "higher_is_better": True,
