@@ -196,18 +196,37 @@ class ParticleTracker:
         return k, False, np.arange(T)
 
     def track_particles(self, initial_positions, time_span: Tuple[float, float], n_timesteps: int,
-                        dt: Optional[float] = None, **kwargs) -> Trajectory:
-        """tracker.py:320-358: T = n_timesteps rows from linspace(t0, t1, T)."""
+                        dt: Optional[float] = None, return_device: bool = False, **kwargs):
+        """tracker.py:320-358: T = n_timesteps rows from linspace(t0, t1, T).
+
+        ``initial_positions`` may also be a float32 (N, 3) torch tensor: on the
+        host (pinned memory: one DMA) or already on the device (no copy in).
+        ``return_device=True`` (with ``record_final_only``) returns the final
+        positions as a (N, 3) CUDA tensor instead of a host ``Trajectory``,
+        for callers that keep the particles on the device."""
         import torch
-        src = None
-        if isinstance(initial_positions, torch.Tensor) and initial_positions.device.type == "cpu" \
+        src = dev_in = None
+        if isinstance(initial_positions, torch.Tensor) and initial_positions.is_cuda:
+            dev_in = initial_positions.to(torch.float32).reshape(-1, 3).contiguous()
+            x0 = None
+            n = dev_in.shape[0]
+        elif isinstance(initial_positions, torch.Tensor) and initial_positions.device.type == "cpu" \
                 and initial_positions.dtype == torch.float32 and initial_positions.ndim == 2 \
                 and initial_positions.shape[1] == 3 and initial_positions.is_contiguous():
             src = initial_positions          # e.g. pinned host memory: one DMA to the device
             x0 = src.numpy()
         else:
             x0 = ensure_positions_shape(initial_positions)
-        n = x0.shape[0]
+        if x0 is not None:
+            n = x0.shape[0]
+        if return_device:
+            if int(n_timesteps) > 1 and not self.options.record_final_only:
+                raise ValueError("return_device=True returns the final positions: use record_final_only=True")
+            if self.options.record_velocities or self.options.row_sink is not None:
+                raise ValueError("return_device=True records no rows (no velocities, no row sink)")
+            return self._track_on_device(dev_in if dev_in is not None else
+                                         (src if src is not None else torch.from_numpy(x0)),
+                                         time_span, n_timesteps, dt)
         t_start, t_end = time_span
         times = np.linspace(float(t_start), float(t_end), int(n_timesteps), dtype=np.float32)
         if dt is None:
@@ -224,8 +243,12 @@ class ParticleTracker:
         velocities = _host_rows((n_rows, n, 3), zero=not compact) if self.options.record_velocities else None
         if n == 0 or T == 0:
             return self._trajectory(positions, times[row_idx], velocities, n, T, dt, batch_size, 0)
-        host0 = src if src is not None else torch.from_numpy(x0)
-        pos = host0.to("cuda", non_blocking=src is not None)
+        if dev_in is not None:
+            pos = dev_in.clone()               # the caller's tensor stays as it is
+            host0 = pos.cpu()
+        else:
+            host0 = src if src is not None else torch.from_numpy(x0)
+            pos = host0.to("cuda", non_blocking=src is not None)
         if velocities is not None:
             torch.from_numpy(velocities[0]).copy_(self._field.sample_at_positions(pos, times[0], arith=self._arith()))
         # row 0 is a host copy of the input: made on a helper thread while
@@ -269,6 +292,18 @@ class ParticleTracker:
             if traj.path_length is None:       # no step ran
                 traj.path_length = np.zeros(n, dtype=F32)
         return traj
+
+    def _track_on_device(self, x0, time_span, n_timesteps: int, dt: Optional[float]):
+        """track_particles for return_device=True: the final positions as a
+        CUDA tensor, no host rows."""
+        import torch
+        times = np.linspace(float(time_span[0]), float(time_span[1]), int(n_timesteps), dtype=np.float32)
+        if dt is None:
+            dt = float(times[1] - times[0]) if len(times) > 1 else 0.0
+        pos = x0.to("cuda", non_blocking=True).to(torch.float32).reshape(-1, 3).clone()
+        if pos.shape[0] and len(times) > 1:
+            self._run(pos, times, float(dt), 1, True, 2, None, None)
+        return pos
 
     def _trajectory(self, positions, times, velocities, n, T, dt, batch_size, n_chunks):
         meta = {

@@ -113,3 +113,25 @@ def test_particles_far_outside_the_grid(mode):
     spec = oracle.GridSpec(data, times, g, g, g, mode)
     ref = _oracle(spec, ("none",) * 3, x0, 30, 0.01)
     assert same(out, ref)
+
+
+def test_device_inputs_and_device_results(plain):
+    """A CUDA tensor as the initial positions gives the host input's
+    trajectory bit for bit (the caller's tensor untouched), and
+    return_device=True hands back the same final positions on the device."""
+    import torch
+    c, f, _ = plain
+    x0 = c["x0"][:500]
+    tr = jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT), record_final_only=True)
+    ref = tr.track_particles(x0, (0.0, 0.2), 21, dt=0.01)
+    xd = torch.from_numpy(x0).cuda()
+    keep = xd.clone()
+    got = tr.track_particles(xd, (0.0, 0.2), 21, dt=0.01)
+    assert same(got.positions, ref.positions) and torch.equal(xd, keep)
+    fin = tr.track_particles(xd, (0.0, 0.2), 21, dt=0.01, return_device=True)
+    assert fin.is_cuda and fin.shape == (500, 3) and same(fin.cpu().numpy(), ref.positions[-1])
+    fin_host_in = tr.track_particles(x0, (0.0, 0.2), 21, dt=0.01, return_device=True)
+    assert same(fin_host_in.cpu().numpy(), ref.positions[-1])
+    every = jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT))
+    with pytest.raises(ValueError, match="record_final_only"):
+        every.track_particles(xd, (0.0, 0.2), 21, dt=0.01, return_device=True)
