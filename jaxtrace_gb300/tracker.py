@@ -318,6 +318,7 @@ class ParticleTracker:
             "kernel": f"jt_track/{type(self._field).__name__}",
             "storage": self._field.storage,
             "arith": "exact" if self._arith() == L.JT_ARITH_EXACT else "compensated",
+            "precision": "exact" if self._arith() == L.JT_ARITH_EXACT else "compensated",
             "time_chunks": n_chunks,
             "device_status": self.last_status,
         }
