@@ -51,3 +51,15 @@ def test_breadth_first_descent_makes_the_same_moves(n, mpl, depth):
                         m.nodes["c"][rng.integers(0, len(m.nodes), 1000)]]).astype(np.float32)
     for p in q:
         assert _dfs(m.nodes, p, depth) == _bfs(desc, dtab, p, depth)
+
+
+def test_auto_sub_div_follows_the_element_size():
+    """fields.auto_sub_div: sub-cells about a sixth of the median element box,
+    1..16, lowered while the estimated list entries exceed the budget."""
+    P, T4 = W.kuhn_mesh(64, 0.2, 1)
+    size = P.max(axis=0) - P.min(axis=0)
+    assert F.auto_sub_div(P, T4, size / 32) == 10            # the FEM configuration
+    assert F.auto_sub_div(P, T4, size / 256) == 1            # cells already finer than elements
+    assert F.auto_sub_div(P, T4, size / 4) == 16             # capped
+    assert F.auto_sub_div(P, T4, size / 32, max_entries=10 ** 8) < 10
+    assert F.auto_sub_div(P, T4[:0], size / 32) == 1
