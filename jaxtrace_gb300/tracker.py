@@ -347,11 +347,17 @@ class ParticleTracker:
     def _sort_every(self, n: int) -> int:
         """Locality re-sort interval: measured best at 100 steps for float32
         snapshots and 200 for 16-bit ones (whose launches are shorter, so the
-        sort is a larger share) on the 16.8M-particle precision workload."""
+        sort is a larger share) on the 16.8M-particle precision workload of a
+        regular grid; 32 on tetrahedral meshes, whose lookups lose locality
+        sooner (FEM configuration, octree: 5.28e9 particle-steps/s at 25, 5.27e9
+        at 50, 5.11e9 at 100, 5.15e9 at 10)."""
         se = self.options.sort_every
         if se is None:
             if n < (1 << 18):
                 return 0
+            from .fields import FEMTimeSeriesField, OctreeFEMTimeSeriesFieldOptimized
+            if isinstance(self._field, (OctreeFEMTimeSeriesFieldOptimized, FEMTimeSeriesField)):
+                return 32
             return 100 if self._field._storage == L.JT_STORE_F32 else 200
         return max(int(se), 0)
 
