@@ -65,6 +65,7 @@ def args_parse():
     p.add_argument("--fem-steps", type=int, default=1000)
     p.add_argument("--fem-hash-sub-div", type=int, default=None, help="hash-grid sub-cells per axis of a cell (default: automatic)")
     p.add_argument("--fem-sort-every", type=int, default=None, help="locality re-sort interval of the FEM legs (default: automatic)")
+    p.add_argument("--fem-sort-bits", type=int, default=None, help="re-sort cells per axis of the FEM legs as 2^bits (default 7)")
     p.add_argument("--adj-lattice", default="256,256,64", help="seed lattice of the adjoint leg")
     p.add_argument("--adj-steps", type=int, default=500)
     p.add_argument("--density-particles", type=int, default=16_000_000)
@@ -392,7 +393,8 @@ def fem_leg(a, profile=False):
     c = W.fem_case(n_steps=n_steps)
     f = jt.OctreeFEMTimeSeriesFieldOptimized(c["data"], c["times"], c["points"], c["tets"])
     bc = jt.mixed_boundary(W.UNIT, c["conditions"])
-    tr = jt.create_tracker("rk4", f, bc, record_final_only=True, sort_every=a.fem_sort_every)
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True, sort_every=a.fem_sort_every,
+                           sort_bits=a.fem_sort_bits)
     times = np.linspace(c["time_span"][0], c["time_span"][1], c["n_timesteps"], dtype=np.float32)
     x0 = torch.from_numpy(c["x0"]).cuda()
     pos = torch.empty_like(x0)
@@ -482,7 +484,8 @@ def fem_hash_leg(a, profile=False):
     c = W.fem_case(n_steps=a.fem_steps)
     f = jt.FEMTimeSeriesField(c["data"], c["times"], c["points"], c["tets"], sub_div=a.fem_hash_sub_div)
     bc = jt.mixed_boundary(W.UNIT, c["conditions"])
-    tr = jt.create_tracker("rk4", f, bc, record_final_only=True, sort_every=a.fem_sort_every)
+    tr = jt.create_tracker("rk4", f, bc, record_final_only=True, sort_every=a.fem_sort_every,
+                           sort_bits=a.fem_sort_bits)
     times = np.linspace(c["time_span"][0], c["time_span"][1], c["n_timesteps"], dtype=np.float32)
     x0 = torch.from_numpy(c["x0"]).cuda()
     pos = torch.empty_like(x0)
