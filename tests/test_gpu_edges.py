@@ -135,3 +135,27 @@ def test_device_inputs_and_device_results(plain):
     every = jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT))
     with pytest.raises(ValueError, match="record_final_only"):
         every.track_particles(xd, (0.0, 0.2), 21, dt=0.01, return_device=True)
+
+
+def test_octree_tracking_on_a_tree_deeper_than_its_staged_top():
+    """A 16^3-hexahedron Kuhn mesh (24,576 tetrahedra, 4,681 octree nodes over
+    five levels): the tracking kernel reads the tree's top from shared memory
+    and the rest from global memory, and the trajectory is the oracle's bit
+    for bit, inside the mesh and across its faces."""
+    P, tets = W.kuhn_mesh(16, 0.2, 3)
+    st = np.linspace(0, 1, 4).astype(F32)
+    data = W.abc_snapshots(P, st)
+    f = jt.OctreeFEMTimeSeriesFieldOptimized(data, st, P, tets)
+    m = f.octree_mesh
+    assert len(m.nodes) > 585
+    spec = oracle.MeshSpec(data, st, P, tets, m.element_bounds, m.nodes_min, m.nodes_max, m.nodes_elements,
+                           m.nodes_children, m.nodes_is_leaf, max_depth=m.max_depth)
+    rng = np.random.default_rng(12)
+    x0 = rng.uniform(-0.05, 1.05, (3000, 3)).astype(F32)
+    T, dt = 16, 0.01
+    for sort_every in (0, 5):
+        tr = jt.create_tracker("rk4", f, jt.no_boundary(), record_final_only=True, sort_every=sort_every)
+        out = tr.track_particles(x0, (0.0, (T - 1) * dt), T, dt=dt).positions[-1]
+        ref, _, _ = oracle.track(spec, oracle.BoundarySpec(kinds=("none",) * 3), x0,
+                                 np.linspace(0.0, (T - 1) * dt, T, dtype=F32), dt)
+        assert same(out, ref)
