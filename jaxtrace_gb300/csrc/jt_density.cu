@@ -293,21 +293,26 @@ __global__ void __launch_bounds__(kKdeThreads) k_kde_grid(jt_kde_params P) {
     }
 }
 
-// 3-D KDE with register blocking: a block owns an 8^3 tile of grid points
-// and each of its 128 threads four consecutive z points, so one particle
-// costs a thread two scalar shared loads (x and y factors), one 128-bit
-// shared load (four z factors) and one multiply plus four FMAs, instead of
-// three shared loads per point.  z factors are stored particle-major (32 B
-// per particle).  The tile stays 8^3 so the dilated box of particles each
-// tile visits stays small.
-constexpr int kKbT = 8;
-constexpr int kKbThreads = 128;
-constexpr int kKbChunk = 480;  // 16 rows x 481 x 4 B + 480 x 32 B = 46.2 KB
-static_assert(kKbThreads * 4 == kKbT * kKbT * kKbT, "four z points per thread");
+constexpr int kKbT = 8;  // the 3-D KDE's grid tile edge
 
-__global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params P) {
-    __shared__ float fab[2 * kKbT][kKbChunk + 1];
-    __shared__ __align__(16) float fc[kKbChunk][kKbT];
+// 3-D KDE with register blocking: a block of 64 threads owns an 8^3 tile of
+// grid points and each thread eight of them (two y by four z), so one particle
+// costs a thread three shared loads (its x factor, two y factors in one
+// 64-bit load, four z factors in one 128-bit load), two multiplies and eight
+// FMAs.  All factors are stored particle-major (32 B per particle and axis):
+// a warp's loads of one particle fall in one 32-byte row per axis, one
+// shared-memory wavefront each.  The tile stays 8^3 so the dilated box of
+// particles each tile visits stays small.  (Four z points per thread of
+// 128, with x and y factors in axis-major rows, took 3 shared loads per 4
+// terms and was 12 % slower, bound by the shared-memory pipe.)
+constexpr int kK8Threads = 64;
+constexpr int kK8Chunk = 240;  // 3 x 240 x 32 B = 22.5 KB: eight blocks (16 warps) per SM
+static_assert(kK8Threads * 8 == kKbT * kKbT * kKbT, "eight grid points per thread");
+
+__global__ void __launch_bounds__(kK8Threads, 8) k_kde_grid3_blocked(jt_kde_params P) {
+    __shared__ __align__(16) float fx[kK8Chunk][kKbT];
+    __shared__ __align__(16) float fy[kK8Chunk][kKbT];
+    __shared__ __align__(16) float fz[kK8Chunk][kKbT];
     __shared__ float gcoord[3][kKbT];
     const int t = threadIdx.x;
     const int tiles_a = (P.res[0] + kKbT - 1) / kKbT, tiles_b = (P.res[1] + kKbT - 1) / kKbT;
@@ -321,10 +326,10 @@ __global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params 
         gcoord[a][k] = k < na ? __ldg(P.axis[a] + ba + k) : 0.0f;
     }
     __syncthreads();
-    // thread -> (pa, pb, four z points from pc0); z fastest
-    const int pc0 = 4 * (t % (kKbT / 4));
-    const int pb = (t / (kKbT / 4)) % kKbT;
-    const int pa = t / ((kKbT / 4) * kKbT);
+    // thread -> (pa, y points pb0 and pb0 + 1, z points pc0 .. pc0 + 3); z fastest
+    const int pc0 = 4 * (t & 1);
+    const int pb0 = 2 * ((t >> 1) & 3);
+    const int pa = t >> 3;
     const jt_sort_grid& g = P.grid;
     const int lim = (1 << g.bits) - 1;
     const int lo0 = cell_of(gcoord[0][0] - P.radius, g.origin[0], g.inv_cell[0], lim);
@@ -333,48 +338,55 @@ __global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params 
     const int hi1 = cell_of(gcoord[1][n1 - 1] + P.radius, g.origin[1], g.inv_cell[1], lim);
     const int lo2 = cell_of(gcoord[2][0] - P.radius, g.origin[2], g.inv_cell[2], lim);
     const int hi2 = cell_of(gcoord[2][n2 - 1] + P.radius, g.origin[2], g.inv_cell[2], lim);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    double acc[2][4] = {{0.0, 0.0, 0.0, 0.0}, {0.0, 0.0, 0.0, 0.0}};
     unsigned long long visits = 0;
     for (int cz = lo2; cz <= hi2; ++cz)
         for (int cy = lo1; cy <= hi1; ++cy) {
             uint32_t b, e;
             row_range(P.cell_end, lo0, hi0, cy, cz, g.bits, b, e);
             visits += e - b;
-            for (uint32_t c0 = b; c0 < e; c0 += kKbChunk) {
-                const int n = (int)min((uint32_t)kKbChunk, e - c0);
-                for (int j = t; j < n; j += kKbThreads) {
+            for (uint32_t c0 = b; c0 < e; c0 += kK8Chunk) {
+                const int n = (int)min((uint32_t)kK8Chunk, e - c0);
+                for (int j = t; j < n; j += kK8Threads) {
                     const int64_t pj = c0 + j;
                     const float px = __ldg(P.particles + 3 * pj), py = __ldg(P.particles + 3 * pj + 1);
                     const float pz = __ldg(P.particles + 3 * pj + 2);
-                    float zf[kKbT];
+                    float ax[kKbT], ay[kKbT], az[kKbT];
 #pragma unroll
                     for (int q = 0; q < kKbT; ++q) {
                         const float dx = gcoord[0][q] - px, dy = gcoord[1][q] - py, dz = gcoord[2][q] - pz;
-                        fab[q][j] = __expf(-dx * dx * P.half_inv_h2);
-                        fab[kKbT + q][j] = __expf(-dy * dy * P.half_inv_h2);
-                        zf[q] = __expf(-dz * dz * P.half_inv_h2);
+                        ax[q] = __expf(-dx * dx * P.half_inv_h2);
+                        ay[q] = __expf(-dy * dy * P.half_inv_h2);
+                        az[q] = __expf(-dz * dz * P.half_inv_h2);
                     }
 #pragma unroll
-                    for (int q = 0; q < kKbT; q += 4)
-                        *reinterpret_cast<float4*>(&fc[j][q]) = make_float4(zf[q], zf[q + 1], zf[q + 2], zf[q + 3]);
+                    for (int q = 0; q < kKbT; q += 4) {
+                        *reinterpret_cast<float4*>(&fx[j][q]) = make_float4(ax[q], ax[q + 1], ax[q + 2], ax[q + 3]);
+                        *reinterpret_cast<float4*>(&fy[j][q]) = make_float4(ay[q], ay[q + 1], ay[q + 2], ay[q + 3]);
+                        *reinterpret_cast<float4*>(&fz[j][q]) = make_float4(az[q], az[q + 1], az[q + 2], az[q + 3]);
+                    }
                 }
                 __syncthreads();
-                float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-                const float* fa = fab[pa];
-                const float* fb = fab[kKbT + pb];
+                float p[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll 4
                 for (int j = 0; j < n; ++j) {
-                    const float ab = fa[j] * fb[j];
-                    const float4 c = *reinterpret_cast<const float4*>(&fc[j][pc0]);
-                    p0 = fmaf(ab, c.x, p0);
-                    p1 = fmaf(ab, c.y, p1);
-                    p2 = fmaf(ab, c.z, p2);
-                    p3 = fmaf(ab, c.w, p3);
+                    const float a = fx[j][pa];
+                    const float2 y2 = *reinterpret_cast<const float2*>(&fy[j][pb0]);
+                    const float4 c = *reinterpret_cast<const float4*>(&fz[j][pc0]);
+                    const float ab0 = a * y2.x, ab1 = a * y2.y;
+                    p[0][0] = fmaf(ab0, c.x, p[0][0]);
+                    p[0][1] = fmaf(ab0, c.y, p[0][1]);
+                    p[0][2] = fmaf(ab0, c.z, p[0][2]);
+                    p[0][3] = fmaf(ab0, c.w, p[0][3]);
+                    p[1][0] = fmaf(ab1, c.x, p[1][0]);
+                    p[1][1] = fmaf(ab1, c.y, p[1][1]);
+                    p[1][2] = fmaf(ab1, c.z, p[1][2]);
+                    p[1][3] = fmaf(ab1, c.w, p[1][3]);
                 }
-                a0 += (double)p0;
-                a1 += (double)p1;
-                a2 += (double)p2;
-                a3 += (double)p3;
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) acc[r][k] += (double)p[r][k];
                 __syncthreads();
             }
         }
@@ -382,12 +394,15 @@ __global__ void __launch_bounds__(kKbThreads) k_kde_grid3_blocked(jt_kde_params 
         atomicAdd(P.counters, visits);
         atomicAdd(P.counters + 1, visits * (unsigned long long)(n0 * n1 * n2));
     }
-    if (pa < n0 && pb < n1) {
-        const int64_t row = ((int64_t)(b0 + pa) * P.res[1] + (b1 + pb)) * P.res[2] + b2 + pc0;
-        if (pc0 < n2) P.out[row] = a0;
-        if (pc0 + 1 < n2) P.out[row + 1] = a1;
-        if (pc0 + 2 < n2) P.out[row + 2] = a2;
-        if (pc0 + 3 < n2) P.out[row + 3] = a3;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int pb = pb0 + r;
+        if (pa < n0 && pb < n1) {
+            const int64_t row = ((int64_t)(b0 + pa) * P.res[1] + (b1 + pb)) * P.res[2] + b2 + pc0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (pc0 + k < n2) P.out[row + k] = acc[r][k];
+        }
     }
 }
 
@@ -488,7 +503,7 @@ extern "C" int jt_kde_grid(const jt_kde_params* p, void* stream) {
         const int64_t blocks = (int64_t)((p->res[0] + kKbT - 1) / kKbT) * ((p->res[1] + kKbT - 1) / kKbT) *
                                ((p->res[2] + kKbT - 1) / kKbT);
         if (blocks > 0x7fffffff) return set_error(JT_ERR_INVALID, "grid too large");
-        k_kde_grid3_blocked<<<(unsigned)blocks, kKbThreads, 0, st>>>(*p);
+        k_kde_grid3_blocked<<<(unsigned)blocks, kK8Threads, 0, st>>>(*p);
     } else {
         const int T = kTile2;
         const int64_t blocks = (int64_t)((p->res[0] + T - 1) / T) * ((p->res[1] + T - 1) / T);
