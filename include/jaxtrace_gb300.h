@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JT_ABI_VERSION 4
+#define JT_ABI_VERSION 5
 
 /* ---- return codes ------------------------------------------------------ */
 #define JT_OK 0
@@ -548,7 +548,10 @@ typedef struct {
     int32_t reach[3];          /* cells searched on each side, per axis      */
     int32_t packed;            /* 0: particles (N,3) and masses apart; 1:
                                   particles (N,4) {x,y,z,mass} in one 16-byte
-                                  record (masses then unused)                */
+                                  record; 2: particle pairs (ceil(N/2),8)
+                                  {x0,x1,y0,y1,z0,z1,mass0,mass1} (16-byte
+                                  aligned; an odd N pads the last pair).  1
+                                  and 2 leave masses unused and need h NULL */
     const float* particles;    /* device (N,3) or (N,4) in cell order        */
     const float* masses;       /* device (N) in cell order, or NULL (unit masses) */
     const float* h;            /* device (N) in cell order, or NULL (h_const) */

@@ -16,7 +16,7 @@ from . import _build
 i32, i64, f32, vp = C.c_int32, C.c_int64, C.c_float, C.c_void_p
 
 # ---- constants (mirror of the header) ------------------------------------
-ABI_VERSION = 4
+ABI_VERSION = 5
 JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STATUS = 0, -1, -2, -3, -4, -5
 JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
 JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2

@@ -98,11 +98,43 @@ __device__ __forceinline__ float sph_shape(float q) {
     return expf(-q * q);
 }
 
+// sph_shape of two distances at once: the cubic spline in float32x2
+// arithmetic (each lane rounds as sph_shape does), the other kernels per lane.
+template <int KERN>
+__device__ __forceinline__ float2 sph_shape2(float2 q) {
+    if (KERN == JT_SPH_CUBIC) {
+        const float2 d = __fadd2_rn(make_float2(2.0f, 2.0f), make_float2(-q.x, -q.y));
+        const float2 t = make_float2(fmaxf(d.x, 0.0f), fmaxf(d.y, 0.0f));
+        const float2 outer = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(0.25f, 0.25f), t), t), t);
+        const float2 inner = __ffma2_rn(__fmul2_rn(q, q), __ffma2_rn(make_float2(0.75f, 0.75f), q,
+                                                                     make_float2(-1.5f, -1.5f)),
+                                        make_float2(1.0f, 1.0f));
+        return make_float2(q.x <= 1.0f ? inner.x : outer.x, q.y <= 1.0f ? inner.y : outer.y);
+    }
+    return make_float2(sph_shape<KERN>(q.x), sph_shape<KERN>(q.y));
+}
+
 // Sum of a per-thread count over the warp, added once per warp.
 __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
     const unsigned m = __activemask();
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(m, v, o);
     if ((threadIdx.x & 31) == (__ffs(m) - 1)) atomicAdd(dst, v);
+}
+
+// One particle j of the paired layout (a row's first or last particle when
+// the row starts or ends mid-pair), with the scalar arithmetic of the
+// {x, y, z, m} records.
+template <int DIM, int KERN, bool COUNT>
+__device__ __forceinline__ float sph_pair_one(const float* pairs, uint32_t j, float qx, float qy, float qz,
+                                              float inv, float r2lim, float part, unsigned long long& n_in) {
+    const float* f = pairs + 8 * (int64_t)(j >> 1) + (j & 1u);
+    const float dx = __ldg(f) - qx, dy = __ldg(f + 2) - qy, dz = DIM == 3 ? __ldg(f + 4) - qz : 0.0f;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (d2 <= r2lim) {
+        part = fmaf(__ldg(f + 6), sph_shape<KERN>(fast_dist(d2) * inv), part);
+        if (COUNT) ++n_in;
+    }
+    return part;
 }
 
 // COUNT: also count the candidate pairs examined and those inside the
@@ -148,7 +180,40 @@ __global__ void __launch_bounds__(kBlock) k_sph(jt_sph_params P) {
                 uint32_t b, e;
                 row_range(P.cell_end, xa, xb, y, z, g.bits, b, e);
                 float part = 0.0f;
-                if (P.packed) {
+                if (P.packed == 2) {
+                    // pairs of particles (x0 x1 y0 y1 z0 z1 m0 m1): two
+                    // candidates per iteration in float32x2 arithmetic, their
+                    // terms added in particle order as one at a time
+                    if (COUNT) n_cand += e - b;
+                    const float2 nqx = make_float2(-qx, -qx), nqy = make_float2(-qy, -qy),
+                                 nqz = make_float2(-qz, -qz), inv2 = make_float2(inv, inv);
+                    uint32_t j = b;
+                    if (j < e && (j & 1u)) {  // a row that starts on a pair's second particle
+                        part = sph_pair_one<DIM, KERN, COUNT>(P.particles, j, qx, qy, qz, inv, r2lim, part, n_in);
+                        ++j;
+                    }
+                    const float4* p4 = reinterpret_cast<const float4*>(P.particles);
+#pragma unroll 2
+                    for (; j + 1 < e; j += 2) {
+                        const float4 u = __ldg(p4 + j), w = __ldg(p4 + j + 1);  // j even: pair j/2
+                        const float2 dx = __fadd2_rn(make_float2(u.x, u.y), nqx);
+                        const float2 dy = __fadd2_rn(make_float2(u.z, u.w), nqy);
+                        const float2 dz = DIM == 3 ? __fadd2_rn(make_float2(w.x, w.y), nqz) : make_float2(0.0f, 0.0f);
+                        const float2 d2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                        const float2 sh =
+                            sph_shape2<KERN>(__fmul2_rn(make_float2(fast_dist(d2.x), fast_dist(d2.y)), inv2));
+                        if (d2.x <= r2lim) {
+                            part = fmaf(w.z, sh.x, part);
+                            if (COUNT) ++n_in;
+                        }
+                        if (d2.y <= r2lim) {
+                            part = fmaf(w.w, sh.y, part);
+                            if (COUNT) ++n_in;
+                        }
+                    }
+                    if (j < e)  // a row that ends on a pair's first particle
+                        part = sph_pair_one<DIM, KERN, COUNT>(P.particles, j, qx, qy, qz, inv, r2lim, part, n_in);
+                } else if (P.packed) {
                     // {x, y, z, m} records; FMA-contracted distance (no parity
                     // constraint on the density passes)
                     const float4* p4 = reinterpret_cast<const float4*>(P.particles);
@@ -454,6 +519,9 @@ extern "C" int jt_sph_density(const jt_sph_params* p, void* stream) {
         return set_error(JT_ERR_INVALID, "queries, out, cell_end and particles are required");
     for (int a = 0; a < 3; ++a)
         if (p->reach[a] < 0 || p->reach[a] > 127) return set_error(JT_ERR_INVALID, "reach must be 0..127");
+    if (p->packed < 0 || p->packed > 2) return set_error(JT_ERR_INVALID, "packed must be 0, 1 or 2");
+    if (p->packed != 0 && p->h != nullptr)
+        return set_error(JT_ERR_UNSUPPORTED, "packed records need a uniform smoothing length");
     const unsigned gb = grid_blocks(p->n_queries);
     cudaStream_t st = (cudaStream_t)stream;
     if (p->counters != nullptr) {

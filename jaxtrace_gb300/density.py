@@ -484,10 +484,14 @@ class SPHDensityEstimator:
         p.reach[:] = cl.reach(search)
         p.masses = None
         if h_sorted is None:
-            # uniform h: {x, y, z, mass} records, one 16-byte load per candidate
+            # uniform h: pairs of particles {x0, x1, y0, y1, z0, z1, m0, m1},
+            # two 16-byte loads per two candidates (an odd count pads with zeros)
             P4 = torch.cat([cl.sorted, m_sorted[:, None] if m_sorted is not None else
-                            torch.ones((cl.n, 1), dtype=torch.float32, device="cuda")], dim=1).contiguous()
-            p.packed = 1
+                            torch.ones((cl.n, 1), dtype=torch.float32, device="cuda")], dim=1)
+            n_pairs = (cl.n + 1) // 2
+            P4 = torch.cat([P4, P4.new_zeros((2 * n_pairs - cl.n, 4))]) if 2 * n_pairs != cl.n else P4
+            P4 = P4.reshape(n_pairs, 2, 4).transpose(1, 2).contiguous()
+            p.packed = 2
             p.particles = P4.data_ptr()
         else:
             p.packed = 0

@@ -27,7 +27,7 @@ def test_library_exports_every_header_symbol():
     assert len(names) >= 8
     for n in names:
         assert hasattr(lib, n), n
-    assert lib.jt_abi_version() == L.ABI_VERSION == 4
+    assert lib.jt_abi_version() == L.ABI_VERSION == 5
     # the scratch allocator hook: both functions or neither
     with pytest.raises(ValueError, match="alloc and free"):
         L.check(lib.jt_set_allocator(L.ALLOC_FN(lambda n, s, c: None), L.FREE_FN(), None))
