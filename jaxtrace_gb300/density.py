@@ -358,6 +358,21 @@ class KDEEstimator:
 _SPH_KERNELS = {"cubic_spline": L.JT_SPH_CUBIC, "wendland": L.JT_SPH_WENDLAND, "gaussian": L.JT_SPH_GAUSSIAN}
 
 
+def pair_records(positions, masses=None):
+    """The paired particle records of jt_sph_params (packed = 2): (ceil(N/2), 8)
+    float32 rows {x0, x1, y0, y1, z0, z1, m0, m1} for particles 2k and 2k+1
+    of ``positions`` (N,3), unit masses when ``masses`` is None; an odd N
+    pads the last row with zeros.  On the positions' device."""
+    import torch
+    n = int(positions.shape[0])
+    m = masses[:, None] if masses is not None else torch.ones((n, 1), dtype=torch.float32, device=positions.device)
+    rec = torch.cat([positions, m], dim=1)
+    n_pairs = (n + 1) // 2
+    if 2 * n_pairs != n:
+        rec = torch.cat([rec, rec.new_zeros((1, 4))])
+    return rec.reshape(n_pairs, 2, 4).transpose(1, 2).reshape(n_pairs, 8).contiguous()
+
+
 @dataclass
 class SPHDensityEstimator:
     """sph.py:42-380 on the GPU (same fields)."""
@@ -484,13 +499,8 @@ class SPHDensityEstimator:
         p.reach[:] = cl.reach(search)
         p.masses = None
         if h_sorted is None:
-            # uniform h: pairs of particles {x0, x1, y0, y1, z0, z1, m0, m1},
-            # two 16-byte loads per two candidates (an odd count pads with zeros)
-            P4 = torch.cat([cl.sorted, m_sorted[:, None] if m_sorted is not None else
-                            torch.ones((cl.n, 1), dtype=torch.float32, device="cuda")], dim=1)
-            n_pairs = (cl.n + 1) // 2
-            P4 = torch.cat([P4, P4.new_zeros((2 * n_pairs - cl.n, 4))]) if 2 * n_pairs != cl.n else P4
-            P4 = P4.reshape(n_pairs, 2, 4).transpose(1, 2).contiguous()
+            # uniform h: two 16-byte loads per two candidates
+            P4 = pair_records(cl.sorted, m_sorted)
             p.packed = 2
             p.particles = P4.data_ptr()
         else:

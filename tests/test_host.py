@@ -220,3 +220,42 @@ def test_new_entry_points_validate_before_touching_the_device():
     ff = L.Field(kind=L.JT_FIELD_FEM, fem=C.pointer(h))
     with pytest.raises(ValueError, match="FEM field"):
         L.check(lib.jt_track(C.byref(ff), C.byref(bc), C.byref(p), None))
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 5, 8])
+def test_sph_pair_records_layout(n):
+    """Particles 2k and 2k+1 share a row {x0, x1, y0, y1, z0, z1, m0, m1};
+    an odd count pads the last row with zeros; unit masses by default."""
+    import torch
+    from jaxtrace_gb300.density import pair_records
+    pos = torch.arange(3 * n, dtype=torch.float32).reshape(n, 3)
+    m = torch.arange(n, dtype=torch.float32) + 100
+    for masses, want_m in ((m, m), (None, torch.ones(n))):
+        rec = pair_records(pos, masses)
+        assert rec.shape == ((n + 1) // 2, 8) and rec.dtype == torch.float32 and rec.is_contiguous()
+        for j in range(n):
+            row, lane = rec[j // 2], j % 2
+            assert [float(row[2 * c + lane]) for c in range(3)] == pos[j].tolist()
+            assert float(row[6 + lane]) == float(want_m[j])
+        if n % 2:
+            assert rec[-1, 1::2].tolist() == [0.0] * 4
+
+
+def test_sph_record_layouts_are_checked_before_launch():
+    """jt_sph_density accepts record layouts 0, 1 and 2 only, and the packed
+    ones only with a uniform smoothing length (their kernels read no h)."""
+    lib = L.load()
+    p = L.SphParams()
+    p.dims, p.kernel = 3, L.JT_SPH_CUBIC
+    p.n_particles, p.n_queries = 4, 4
+    p.radius, p.h_const = 0.1, 0.05
+    p.grid.bits = 3
+    p.particles = p.cell_end = p.queries = p.out = 256      # never dereferenced: rejected first
+    p.packed = 3
+    with pytest.raises(ValueError, match="packed"):
+        L.check(lib.jt_sph_density(C.byref(p), None))
+    p.h = 256
+    for packed in (1, 2):
+        p.packed = packed
+        with pytest.raises(NotImplementedError, match="uniform smoothing length"):
+            L.check(lib.jt_sph_density(C.byref(p), None))
