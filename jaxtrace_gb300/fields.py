@@ -62,6 +62,23 @@ def ensure_positions_shape(positions) -> np.ndarray:
     return np.ascontiguousarray(pos)
 
 
+def ensure_positions_tensor(positions):
+    """ensure_positions_shape for a torch tensor, on the tensor's own device:
+    (N,2|3) -> contiguous float32 (N,3), a 1-D tensor as one row, 2-D
+    positions given z = 0; the same errors."""
+    import torch
+    pos = positions.to(torch.float32)
+    if pos.ndim == 1:
+        pos = pos.reshape(1, -1)
+    if pos.ndim != 2:
+        raise ValueError(f"Positions must be 2D array, got shape {tuple(pos.shape)}")
+    if pos.shape[1] == 2:
+        pos = torch.cat([pos, pos.new_zeros((pos.shape[0], 1))], dim=1)
+    elif pos.shape[1] != 3:
+        raise ValueError(f"Positions must have 2 or 3 columns, got {pos.shape[1]}")
+    return pos.contiguous()
+
+
 def storage_code(storage: str) -> int:
     try:
         return L.STORAGE_CODES[str(storage).lower()]

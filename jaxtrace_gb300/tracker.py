@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _lib as L
 from .boundary import BoundaryDescriptor
-from .fields import ensure_positions_shape
+from .fields import ensure_positions_shape, ensure_positions_tensor
 from .integrators import INTEGRATORS, resolve_field
 from .particles import Trajectory
 from .schedule import build_schedule, step_constants
@@ -207,7 +207,7 @@ class ParticleTracker:
         import torch
         src = dev_in = None
         if isinstance(initial_positions, torch.Tensor) and initial_positions.is_cuda:
-            dev_in = initial_positions.to(torch.float32).reshape(-1, 3).contiguous()
+            dev_in = ensure_positions_tensor(initial_positions)
             x0 = None
             n = dev_in.shape[0]
         elif isinstance(initial_positions, torch.Tensor) and initial_positions.device.type == "cpu" \

@@ -132,6 +132,11 @@ def test_device_inputs_and_device_results(plain):
     assert fin.is_cuda and fin.shape == (500, 3) and same(fin.cpu().numpy(), ref.positions[-1])
     fin_host_in = tr.track_particles(x0, (0.0, 0.2), 21, dt=0.01, return_device=True)
     assert same(fin_host_in.cpu().numpy(), ref.positions[-1])
+    # 2-D positions on the device get z = 0, as 2-D arrays do
+    flat = np.ascontiguousarray(x0[:, :2])
+    ref2 = tr.track_particles(flat, (0.0, 0.2), 21, dt=0.01)
+    got2 = tr.track_particles(torch.from_numpy(flat).cuda(), (0.0, 0.2), 21, dt=0.01)
+    assert same(got2.positions, ref2.positions)
     every = jt.create_tracker("rk4", f, jt.periodic_boundary(W.UNIT))
     with pytest.raises(ValueError, match="record_final_only"):
         every.track_particles(xd, (0.0, 0.2), 21, dt=0.01, return_device=True)

@@ -259,3 +259,19 @@ def test_sph_record_layouts_are_checked_before_launch():
         p.packed = packed
         with pytest.raises(NotImplementedError, match="uniform smoothing length"):
             L.check(lib.jt_sph_density(C.byref(p), None))
+
+
+def test_tensor_positions_are_shaped_as_arrays_are():
+    """Tensor inputs (kept on their device) get the checks and the 2-D
+    padding of array inputs, with the same values and messages."""
+    import torch
+    from jaxtrace_gb300.fields import ensure_positions_shape, ensure_positions_tensor
+    rng = np.random.default_rng(3)
+    for a in (rng.uniform(0, 1, (7, 3)), rng.uniform(0, 1, (7, 2)), rng.uniform(0, 1, 3),
+              rng.uniform(0, 1, (5, 3)).astype(np.float32)):
+        got = ensure_positions_tensor(torch.from_numpy(a))
+        assert got.dtype == torch.float32 and got.is_contiguous()
+        assert np.array_equal(got.numpy(), ensure_positions_shape(a))
+    for bad, msg in ((np.zeros((4, 4)), "2 or 3 columns"), (np.zeros((2, 2, 3)), "2D array")):
+        with pytest.raises(ValueError, match=msg):
+            ensure_positions_tensor(torch.from_numpy(bad))
