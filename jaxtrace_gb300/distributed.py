@@ -78,6 +78,9 @@ def gather_rows(local, n_total: int, to_all: bool = False):
         return local
     local = torch.as_tensor(local).to(collective_device())
     counts = [shard_bounds(n_total, r, world) for r in range(world)]
+    lo, hi = counts[rank]
+    if local.shape[0] != hi - lo:
+        raise ValueError(f"rank {rank} holds {local.shape[0]} rows; its slice of {n_total} is {hi - lo}")
     width = max(hi - lo for lo, hi in counts)
     pad = torch.zeros((width,) + tuple(local.shape[1:]), dtype=local.dtype, device=local.device)
     pad[: local.shape[0]] = local

@@ -120,6 +120,8 @@ def test_nccl_collectives_take_device_tensors(monkeypatch):
     monkeypatch.setattr(dist, "all_reduce", fake_all_reduce)
     out = D.gather_rows(torch.zeros((3, 3)), 5)
     assert out.device.type == "meta" and out.shape == (5, 3)
+    with pytest.raises(ValueError, match="slice of 5 is 3"):   # rank 0 of 2 owns rows [0, 3)
+        D.gather_rows(torch.zeros((4, 3)), 5)
     D.allreduce_sum(torch.ones((2, 2), device="meta"))
     assert seen == ["meta", "meta"]
     monkeypatch.undo()
