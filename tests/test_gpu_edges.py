@@ -142,11 +142,11 @@ def test_device_inputs_and_device_results(plain):
         every.track_particles(xd, (0.0, 0.2), 21, dt=0.01, return_device=True)
 
 
-def test_octree_tracking_on_a_tree_deeper_than_its_staged_top():
+def test_octree_tracking_on_a_five_level_tree():
     """A 16^3-hexahedron Kuhn mesh (24,576 tetrahedra, 4,681 octree nodes over
-    five levels): the tracking kernel reads the tree's top from shared memory
-    and the rest from global memory, and the trajectory is the oracle's bit
-    for bit, inside the mesh and across its faces."""
+    five levels, deeper than the other tests' trees): the breadth-first
+    descent's trajectory is the oracle's bit for bit, inside the mesh and
+    across its faces, with and without re-sorting."""
     P, tets = W.kuhn_mesh(16, 0.2, 3)
     st = np.linspace(0, 1, 4).astype(F32)
     data = W.abc_snapshots(P, st)
