@@ -98,6 +98,7 @@ def test_nearest_candidate_lists_give_the_ring_search_result():
     ring = jt.TimeSeriesField(data, t, nodes, nearest_candidates=False)
     q = [rng.uniform(nodes.min(0), nodes.max(0), (20000, 3)), nodes, rng.uniform(-1, 2, (2000, 3))]
     with_lists.sample_at_positions(nodes[:4], 0.0)
+    ring.sample_at_positions(nodes[:4], 0.0)
     cn = with_lists._cnear
     assert with_lists._dev.get("cand_start") is not None and ring._dev.get("cand_start") is None
     o = np.array(cn.cand_origin[:], F32)
