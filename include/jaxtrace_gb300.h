@@ -240,16 +240,17 @@ typedef struct {
      * jt_nearest_candidates: a uniform grid of cand_cells cells from
      * cand_origin, edge 1 / cand_inv_cell.  A query inside it (float32
      * (q - cand_origin) * cand_inv_cell in [0, cand_cells) on every axis)
-     * scans only its cell's list, cand_slots[cand_start[c] ..
+     * scans only its cell's list, cand_recs[cand_start[c] ..
      * cand_start[c+1]) with c = (k * cand_cells[1] + j) * cand_cells[0] + i:
-     * the sorted slots of every node that can be its float32 argmin, so the
-     * result is the ring search's.  Other queries use the ring search. */
+     * every node that can be its float32 argmin, as {x, y, z, node id as
+     * int32 bits} records (one 16-byte load each), so the result is the ring
+     * search's.  Other queries use the ring search. */
     int32_t cand_cells[3];
     float cand_origin[3];
     float cand_inv_cell[3];
     int32_t cand_pad;
     const int32_t* cand_start;
-    const int32_t* cand_slots;
+    const float* cand_recs;
 } jt_nearest_field;
 
 /* Tetrahedral mesh field with the hash-grid point location of
@@ -553,12 +554,13 @@ int jt_cell_list(const jt_sort_grid* g, int32_t n, const float* pos_in, float* p
  * every side) is within the smallest farthest-point distance of any one
  * node, widened by 1e-4 in the squared distance: every node that can be the
  * float32 argmin of a query in the cell.  F's cell list must be complete
- * (its own cand_start is ignored).  With cand_slots NULL the call writes
+ * (its own cand_start is ignored).  With cand_recs NULL the call writes
  * the lists' CSR offsets to cand_start (device, cells product + 1 entries)
- * and their total to *total (host; the call waits for it); with cand_slots
- * set (device, *total entries) it fills the lists of that cand_start. */
+ * and their total to *total (host; the call waits for it); with cand_recs
+ * set (device, *total records of 4 floats, 16-byte aligned) it fills the
+ * lists of that cand_start. */
 int jt_nearest_candidates(const jt_nearest_field* F, const int32_t* cells, const float* origin,
-                          const float* inv_cell, int32_t* cand_start, int32_t* cand_slots, int64_t* total,
+                          const float* inv_cell, int32_t* cand_start, float* cand_recs, int64_t* total,
                           void* stream);
 
 /* ---- density passes ------------------------------------------------------ */

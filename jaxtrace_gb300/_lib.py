@@ -73,7 +73,7 @@ class NearestField(C.Structure):
                 ("storage", i32), ("n_pairs", i32), ("pair_stride", i64),
                 ("points", vp), ("point_ids", vp), ("cell_start", vp), ("pairs", vp),
                 ("cand_cells", i32 * 3), ("cand_origin", f32 * 3), ("cand_inv_cell", f32 * 3), ("cand_pad", i32),
-                ("cand_start", vp), ("cand_slots", vp)]
+                ("cand_start", vp), ("cand_recs", vp)]
 
 
 class FemField(C.Structure):

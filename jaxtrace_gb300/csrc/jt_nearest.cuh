@@ -76,7 +76,15 @@ __device__ __forceinline__ int nearest_core(const jt_nearest_field& F, float h_m
             const int b = __ldg(F.cand_start + cell), en = __ldg(F.cand_start + cell + 1);
             float best = __int_as_float(0x7f800000);
             int best_id = 0x7fffffff;
-            for (int k = b; k < en; ++k) nearest_try<EXACT>(F, q, __ldg(F.cand_slots + k), best, best_id, best_slot);
+            typedef Ar<EXACT> A;
+            for (int k = b; k < en; ++k) {
+                // the arithmetic and the tie rule of nearest_try on a self-contained record
+                const float4 r = __ldg(reinterpret_cast<const float4*>(F.cand_recs) + k);
+                const float ddx = A::sub(q.x, r.x), ddy = A::sub(q.y, r.y), ddz = A::sub(q.z, r.z);
+                const float d = A::add(A::add(A::mul(ddx, ddx), A::mul(ddy, ddy)), A::mul(ddz, ddz));
+                const int id = __float_as_int(r.w);
+                if (d < best || (d == best && id < best_id)) { best = d; best_id = id; }
+            }
             return best_id == 0x7fffffff ? 0 : best_id;
         }
     }

@@ -8,9 +8,9 @@
 // U^2 (1 + e)^2, e < 1e-6 the relative error of a float32 squared distance
 // (three subtractions, three products, two sums of non-negative terms), so
 // w lies within that distance of B.  The list of B is every node whose
-// squared distance to B is at most U^2 (1 + kCandSlack), in the sorted
-// slots of the field's cell list; m0 is the float32 nearest node of B's
-// centre, which keeps U small.
+// squared distance to B is at most U^2 (1 + kCandSlack), as {x, y, z, id}
+// records in the order of the field's cell list; m0 is the float32 nearest
+// node of B's centre, which keeps U small.
 #include <math.h>
 
 #include "jt_internal.h"
@@ -56,13 +56,13 @@ __device__ __forceinline__ double box_near2(const float4& p, const double* lo, c
     return s;
 }
 
-// FILL = false: the list length of each cell into out[c] and its sum into
-// *total; FILL = true: the list of cell c into out[start[c] ..].  Both
-// passes walk the same nodes in the same order.
+// FILL = false: the list length of each cell into count[c] and its sum
+// into *total; FILL = true: the list of cell c into recs[start[c] ..].
+// Both passes walk the same nodes in the same order.
 template <bool FILL>
 __global__ void __launch_bounds__(kCandBlock) k_cand(jt_nearest_field F, CandGrid G, float h_min, int64_t n_cells,
-                                                     const int32_t* __restrict__ start, int32_t* __restrict__ out,
-                                                     unsigned long long* total) {
+                                                     const int32_t* __restrict__ start, int32_t* __restrict__ count,
+                                                     float4* __restrict__ recs, unsigned long long* total) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int32_t n = 0;
     if (c < n_cells) {
@@ -93,14 +93,15 @@ __global__ void __launch_bounds__(kCandBlock) k_cand(jt_nearest_field F, CandGri
                     const int64_t row = ((int64_t)z * F.cells[1] + y) * F.cells[0];
                     const int b = __ldg(F.cell_start + row + clo[0]), e = __ldg(F.cell_start + row + chi[0] + 1);
                     for (int s = b; s < e; ++s) {
-                        if (box_near2(__ldg(reinterpret_cast<const float4*>(F.points) + s), lo, hi) <= u2) {
-                            if (FILL) out[w + n] = s;
+                        const float4 p = __ldg(reinterpret_cast<const float4*>(F.points) + s);
+                        if (box_near2(p, lo, hi) <= u2) {
+                            if (FILL) recs[w + n] = make_float4(p.x, p.y, p.z, __int_as_float(__ldg(F.point_ids + s)));
                             ++n;
                         }
                     }
                 }
         }
-        if (!FILL) out[c] = n;
+        if (!FILL) count[c] = n;
     }
     if (!FILL) {
         // the exact total (the offsets are 32-bit): one atomic per warp
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kCandBlock) k_cand(jt_nearest_field F, CandGri
 using namespace jt;
 
 extern "C" int jt_nearest_candidates(const jt_nearest_field* F, const int32_t* cells, const float* origin,
-                                     const float* inv_cell, int32_t* cand_start, int32_t* cand_slots, int64_t* total,
+                                     const float* inv_cell, int32_t* cand_start, float* cand_recs, int64_t* total,
                                      void* stream) {
     if (F == nullptr || cells == nullptr || origin == nullptr || inv_cell == nullptr || cand_start == nullptr ||
         total == nullptr)
@@ -139,12 +140,14 @@ extern "C" int jt_nearest_candidates(const jt_nearest_field* F, const int32_t* c
     }
     jt_nearest_field f = *F;
     f.cand_start = nullptr;
-    f.cand_slots = nullptr;
+    f.cand_recs = nullptr;
     const float h = nearest_min_cell_edge(f);
     cudaStream_t s = (cudaStream_t)stream;
     const unsigned blocks = (unsigned)((n_cells + kCandBlock - 1) / kCandBlock);
-    if (cand_slots != nullptr) {
-        k_cand<true><<<blocks, kCandBlock, 0, s>>>(f, G, h, n_cells, cand_start, cand_slots, nullptr);
+    if (cand_recs != nullptr) {
+        if (((uintptr_t)cand_recs & 15u) != 0) return set_error(JT_ERR_INVALID, "cand_recs must be 16-byte aligned");
+        k_cand<true><<<blocks, kCandBlock, 0, s>>>(f, G, h, n_cells, cand_start, nullptr,
+                                                   reinterpret_cast<float4*>(cand_recs), nullptr);
         return cuda_status(cudaGetLastError(), "candidate list fill");
     }
     unsigned long long* sum = nullptr;
@@ -155,7 +158,7 @@ extern "C" int jt_nearest_candidates(const jt_nearest_field* F, const int32_t* c
     if (e == cudaSuccess) e = cudaMemsetAsync(sum, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(cand_start + n_cells, 0, sizeof(int32_t), s);
     if (e == cudaSuccess) {
-        k_cand<false><<<blocks, kCandBlock, 0, s>>>(f, G, h, n_cells, nullptr, cand_start, sum);
+        k_cand<false><<<blocks, kCandBlock, 0, s>>>(f, G, h, n_cells, nullptr, cand_start, nullptr, sum);
         e = cudaGetLastError();
     }
     int rc = cuda_status(e, "candidate list count");

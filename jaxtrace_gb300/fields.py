@@ -660,14 +660,14 @@ class TimeSeriesField(_DeviceField):
         stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
         L.check(lib.jt_nearest_candidates(C.byref(q), c_cells, c_origin, c_inv, C.c_void_p(start.data_ptr()), None,
                                           C.byref(total), stream))
-        slots = torch.empty(max(int(total.value), 1), dtype=torch.int32, device="cuda")
+        recs = torch.empty((max(int(total.value), 1), 4), dtype=torch.float32, device="cuda")
         L.check(lib.jt_nearest_candidates(C.byref(q), c_cells, c_origin, c_inv, C.c_void_p(start.data_ptr()),
-                                          C.c_void_p(slots.data_ptr()), C.byref(total), stream))
-        self._dev["cand_start"], self._dev["cand_slots"] = start, slots
+                                          C.c_void_p(recs.data_ptr()), C.byref(total), stream))
+        self._dev["cand_start"], self._dev["cand_recs"] = start, recs
         q.cand_cells[:] = [int(v) for v in cells]
         q.cand_origin[:] = [float(v) for v in o32]
         q.cand_inv_cell[:] = [float(v) for v in inv32]
-        q.cand_start, q.cand_slots = start.data_ptr(), slots.data_ptr()
+        q.cand_start, q.cand_recs = start.data_ptr(), recs.data_ptr()
 
     def _device_pairs(self):
         self._device()
