@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JT_ABI_VERSION 6
+#define JT_ABI_VERSION 5
 
 /* ---- return codes ------------------------------------------------------ */
 #define JT_OK 0
@@ -236,21 +236,6 @@ typedef struct {
     const int32_t* point_ids; /* device (n_points) original node index of sorted slot */
     const int32_t* cell_start; /* device (cells+1) CSR offsets                 */
     const void* pairs;      /* device value pairs indexed by ORIGINAL node id */
-    /* Optional candidate lists (cand_start NULL: the ring search alone), from
-     * jt_nearest_candidates: a uniform grid of cand_cells cells from
-     * cand_origin, edge 1 / cand_inv_cell.  A query inside it (float32
-     * (q - cand_origin) * cand_inv_cell in [0, cand_cells) on every axis)
-     * scans only its cell's list, cand_recs[cand_start[c] ..
-     * cand_start[c+1]) with c = (k * cand_cells[1] + j) * cand_cells[0] + i:
-     * every node that can be its float32 argmin, as {x, y, z, node id as
-     * int32 bits} records (one 16-byte load each), so the result is the ring
-     * search's.  Other queries use the ring search. */
-    int32_t cand_cells[3];
-    float cand_origin[3];
-    float cand_inv_cell[3];
-    int32_t cand_pad;
-    const int32_t* cand_start;
-    const float* cand_recs;
 } jt_nearest_field;
 
 /* Tetrahedral mesh field with the hash-grid point location of
@@ -546,22 +531,6 @@ int jt_unpermute(int32_t n, const float* pos_sorted, const int32_t* ids, float* 
  * cell keys, argsort, unique starts/counts.  Other arguments as jt_cell_sort. */
 int jt_cell_list(const jt_sort_grid* g, int32_t n, const float* pos_in, float* pos_out, int32_t* ids_out,
                  uint32_t* cell_end, void* workspace, size_t workspace_bytes, void* stream);
-
-/* Candidate lists of a nearest-node field's search (jt_nearest_field
- * cand_*): a grid of `cells` cells from `origin` with edge 1 / inv_cell
- * (every axis: cells >= 1, inv_cell > 0).  Each cell lists the sorted slots
- * of the nodes whose distance to the cell (grown by 1e-3 of its edge on
- * every side) is within the smallest farthest-point distance of any one
- * node, widened by 1e-4 in the squared distance: every node that can be the
- * float32 argmin of a query in the cell.  F's cell list must be complete
- * (its own cand_start is ignored).  With cand_recs NULL the call writes
- * the lists' CSR offsets to cand_start (device, cells product + 1 entries)
- * and their total to *total (host; the call waits for it); with cand_recs
- * set (device, *total records of 4 floats, 16-byte aligned) it fills the
- * lists of that cand_start. */
-int jt_nearest_candidates(const jt_nearest_field* F, const int32_t* cells, const float* origin,
-                          const float* inv_cell, int32_t* cand_start, float* cand_recs, int64_t* total,
-                          void* stream);
 
 /* ---- density passes ------------------------------------------------------ */
 #define JT_SPH_CUBIC 0    /* sph.py:227-236 */

@@ -16,7 +16,7 @@ from . import _build
 i32, i64, f32, vp = C.c_int32, C.c_int64, C.c_float, C.c_void_p
 
 # ---- constants (mirror of the header) ------------------------------------
-ABI_VERSION = 6
+ABI_VERSION = 5
 JT_OK, JT_ERR_INVALID, JT_ERR_UNSUPPORTED, JT_ERR_CUDA, JT_ERR_NOMEM, JT_ERR_STATUS = 0, -1, -2, -3, -4, -5
 JT_STATUS_INDEX_WRAPPED, JT_STATUS_NONFINITE, JT_STATUS_OCTREE_FALLBACK = 0x1, 0x2, 0x4
 JT_STORE_F32, JT_STORE_BF16, JT_STORE_F16 = 0, 1, 2
@@ -71,9 +71,7 @@ class MeshField(C.Structure):
 class NearestField(C.Structure):
     _fields_ = [("n_points", i32), ("cells", i32 * 3), ("origin", f32 * 3), ("inv_cell", f32 * 3),
                 ("storage", i32), ("n_pairs", i32), ("pair_stride", i64),
-                ("points", vp), ("point_ids", vp), ("cell_start", vp), ("pairs", vp),
-                ("cand_cells", i32 * 3), ("cand_origin", f32 * 3), ("cand_inv_cell", f32 * 3), ("cand_pad", i32),
-                ("cand_start", vp), ("cand_recs", vp)]
+                ("points", vp), ("point_ids", vp), ("cell_start", vp), ("pairs", vp)]
 
 
 class FemField(C.Structure):
@@ -197,7 +195,6 @@ def load(build_if_missing: bool = True):
         "jt_cell_sort_noalloc": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, vp, vp]),
         "jt_cell_list": (i32, [P(SortGrid), i32, vp, vp, vp, vp, vp, C.c_size_t, vp]),
         "jt_sph_density": (i32, [P(SphParams), vp]),
-        "jt_nearest_candidates": (i32, [P(NearestField), vp, vp, vp, vp, vp, P(i64), vp]),
         "jt_kde_grid": (i32, [P(KdeParams), vp]),
         "jt_kde_points": (i32, [P(KdeParams), vp, i32, vp, vp]),
         "jt_adjoint_rk4": (i32, [P(Field), P(Boundary), P(AdjointParams), vp]),

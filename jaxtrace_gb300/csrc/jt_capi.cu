@@ -53,13 +53,6 @@ static int check_nearest(const jt_nearest_field* q) {
     if (q->pair_stride < q->n_points) return set_error(JT_ERR_INVALID, "pair_stride smaller than n_points");
     if (((uintptr_t)q->pairs & 31u) != 0)
         return set_error(JT_ERR_INVALID, "pairs must be 32-byte aligned (256-bit records)");
-    if (q->cand_start != nullptr) {
-        if (q->cand_recs == nullptr || ((uintptr_t)q->cand_recs & 15u) != 0)
-            return set_error(JT_ERR_INVALID, "cand_start needs 16-byte aligned cand_recs");
-        for (int a = 0; a < 3; ++a)
-            if (q->cand_cells[a] < 1 || !(q->cand_inv_cell[a] > 0.0f))
-                return set_error(JT_ERR_INVALID, "candidate grid needs cand_cells >= 1 and cand_inv_cell > 0");
-    }
     return check_storage(q->storage);
 }
 

@@ -53,10 +53,6 @@ int mesh_step_near(const jt_mesh_field& f, int arith, const StageBlends& sb, int
 int mesh_sample_near(const jt_mesh_field& f, int arith, const jt_blend& e, const float* pos, float* out,
                      int m, int32_t* status, cudaStream_t s);
 
-// Smallest live cell edge of the node cell list, scaled down slightly (the
-// ring search's stop bound); 0 with a single cell on every axis.
-float nearest_min_cell_edge(const jt_nearest_field& f);
-
 int nearest_track(const jt_nearest_field& f, const jt_boundary& b, const jt_track_params& p, cudaStream_t s);
 int nearest_step(const jt_nearest_field& f, int arith, const StageBlends& sb, int integ, StepConst k,
                  const float* dtpp, const float* xin, float* xout, int n, int32_t* status, cudaStream_t s);

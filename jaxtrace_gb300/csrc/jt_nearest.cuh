@@ -10,29 +10,22 @@
 
 namespace jt {
 
-// Node at sorted slot s against the best so far: argmin of the float32
-// squared distance, lowest id on ties (any visiting order gives the same
-// winner).  The id is read only for a distance at or below the best (a new
-// best or a tie).  best_slot follows the winner (the candidate-list build
-// reads it; the sampling paths drop it).
-template <bool EXACT>
-__device__ __forceinline__ void nearest_try(const jt_nearest_field& F, const V3& q, int s, float& best, int& best_id,
-                                            int& best_slot) {
-    typedef Ar<EXACT> A;
-    const float4 p = __ldg(reinterpret_cast<const float4*>(F.points) + s);
-    const float ddx = A::sub(q.x, p.x), ddy = A::sub(q.y, p.y), ddz = A::sub(q.z, p.z);
-    const float d = A::add(A::add(A::mul(ddx, ddx), A::mul(ddy, ddy)), A::mul(ddz, ddz));
-    if (d <= best) {
-        const int id = __ldg(F.point_ids + s);
-        if (d < best || id < best_id) { best = d; best_id = id; best_slot = s; }
-    }
-}
-
-// Nodes [b, en) of the sorted node array.
+// Nodes [b, en) of the sorted node array against the best so far: argmin of
+// the float32 squared distance, lowest id on ties.  The id is read only for
+// a distance at or below the best (a new best or a tie).
 template <bool EXACT>
 __device__ __forceinline__ void nearest_scan(const jt_nearest_field& F, const V3& q, int b, int en, float& best,
-                                             int& best_id, int& best_slot) {
-    for (int s = b; s < en; ++s) nearest_try<EXACT>(F, q, s, best, best_id, best_slot);
+                                             int& best_id) {
+    typedef Ar<EXACT> A;
+    for (int s = b; s < en; ++s) {
+        const float4 p = __ldg(reinterpret_cast<const float4*>(F.points) + s);
+        const float ddx = A::sub(q.x, p.x), ddy = A::sub(q.y, p.y), ddz = A::sub(q.z, p.z);
+        const float d = A::add(A::add(A::mul(ddx, ddx), A::mul(ddy, ddy)), A::mul(ddz, ddz));
+        if (d <= best) {
+            const int id = __ldg(F.point_ids + s);
+            if (d < best || id < best_id) { best = d; best_id = id; }
+        }
+    }
 }
 
 // Lower bound of the distance from the query to a neighbouring row of cells
@@ -52,42 +45,10 @@ __device__ __forceinline__ float row_gap(int d, float frac) {
 // first ring a row whose gap from the query already exceeds the best
 // distance (with a 1e-4 relative margin) is skipped; no node in it can reach
 // the best or tie with it.
-//
-// With candidate lists (F.cand_start) a query inside their grid scans only
-// its cell's list, which holds every node that can win for a query there,
-// so the winner is the same.
 template <bool EXACT>
-__device__ __forceinline__ int nearest_core(const jt_nearest_field& F, float h_min, const V3& q, bool use_cand,
-                                            int& best_slot) {
-    best_slot = -1;
+__device__ __forceinline__ int nearest_id(const jt_nearest_field& F, float h_min, const V3& q) {
     if (q.x != q.x || q.y != q.y || q.z != q.z) return 0;
     const float qq[3] = {q.x, q.y, q.z};
-    if (use_cand && F.cand_start != nullptr) {
-        int cc[3];
-        bool in = true;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float fc = (qq[a] - F.cand_origin[a]) * F.cand_inv_cell[a];
-            in = in && fc >= 0.0f && fc < (float)F.cand_cells[a];
-            cc[a] = in ? (int)fc : 0;
-        }
-        if (in) {
-            const int64_t cell = ((int64_t)cc[2] * F.cand_cells[1] + cc[1]) * F.cand_cells[0] + cc[0];
-            const int b = __ldg(F.cand_start + cell), en = __ldg(F.cand_start + cell + 1);
-            float best = __int_as_float(0x7f800000);
-            int best_id = 0x7fffffff;
-            typedef Ar<EXACT> A;
-            for (int k = b; k < en; ++k) {
-                // the arithmetic and the tie rule of nearest_try on a self-contained record
-                const float4 r = __ldg(reinterpret_cast<const float4*>(F.cand_recs) + k);
-                const float ddx = A::sub(q.x, r.x), ddy = A::sub(q.y, r.y), ddz = A::sub(q.z, r.z);
-                const float d = A::add(A::add(A::mul(ddx, ddx), A::mul(ddy, ddy)), A::mul(ddz, ddz));
-                const int id = __float_as_int(r.w);
-                if (d < best || (d == best && id < best_id)) { best = d; best_id = id; }
-            }
-            return best_id == 0x7fffffff ? 0 : best_id;
-        }
-    }
     int c[3];
     float frac[3];
 #pragma unroll
@@ -124,29 +85,23 @@ __device__ __forceinline__ int nearest_core(const jt_nearest_field& F, float h_m
                 if (face) {  // the whole row [c - r, c + r] as one node range
                     const int x0 = max(c[0] - r, 0), x1 = min(c[0] + r, nx - 1);
                     nearest_scan<EXACT>(F, q, __ldg(F.cell_start + row + x0), __ldg(F.cell_start + row + x1 + 1),
-                                        best, best_id, best_slot);
+                                        best, best_id);
                 } else {     // the two end cells of an inner row
                     if (c[0] - r >= 0) {
                         const int cell = row + c[0] - r;
                         nearest_scan<EXACT>(F, q, __ldg(F.cell_start + cell), __ldg(F.cell_start + cell + 1),
-                                            best, best_id, best_slot);
+                                            best, best_id);
                     }
                     if (c[0] + r < nx) {
                         const int cell = row + c[0] + r;
                         nearest_scan<EXACT>(F, q, __ldg(F.cell_start + cell), __ldg(F.cell_start + cell + 1),
-                                            best, best_id, best_slot);
+                                            best, best_id);
                     }
                 }
             }
         }
     }
     return best_id == 0x7fffffff ? 0 : best_id;
-}
-
-template <bool EXACT>
-__device__ __forceinline__ int nearest_id(const jt_nearest_field& F, float h_min, const V3& q) {
-    int slot;
-    return nearest_core<EXACT>(F, h_min, q, true, slot);
 }
 
 template <bool EXACT, int STORE>

@@ -565,9 +565,8 @@ class TimeSeriesField(_DeviceField):
 
     def __init__(self, data, times, positions, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None, *,
-                 storage: str = "f32", time_semantics: str = "numpy", nearest_candidates: bool = True):
+                 storage: str = "f32", time_semantics: str = "numpy"):
         data = _as_f32(data)
-        self.nearest_candidates = bool(nearest_candidates)
         positions = ensure_positions_shape(positions)
         if data.ndim != 3:
             raise ValueError(f"data must have 3 dims (T,N,3), got {data.shape}")
@@ -629,45 +628,8 @@ class TimeSeriesField(_DeviceField):
         q.point_ids = self._dev["ids"].data_ptr()
         q.cell_start = self._dev["start"].data_ptr()
         q.pairs = pairs.data_ptr()
-        if self.nearest_candidates:
-            self._candidates(q)
         self._cnear = q
         self._cfield = L.Field(kind=L.JT_FIELD_NEAREST, nearest=C.pointer(q))
-
-    def _candidates(self, q):
-        """Per-cell candidate lists of the nearest-node search
-        (jt_nearest_candidates) on a grid of cells about half the mean node
-        spacing: a query inside it scans the few nodes that can be its
-        nearest instead of rings of cells (same result).  Node sets flat
-        along an axis keep the ring search alone."""
-        P = self.positions.astype(np.float64)
-        lo, hi = P.min(axis=0), P.max(axis=0)
-        ext = hi - lo
-        if self.N < 2 or not np.all(ext > 0):
-            return
-        torch = _torch_cuda()
-        edge = 0.5 * (float(np.prod(ext)) / self.N) ** (1.0 / 3.0)
-        cells = np.clip(np.ceil(ext / edge), 1, 4096).astype(np.int64)
-        while np.prod(cells) > 16 * self.N + 64:
-            cells = np.maximum(cells // 2, 1)
-        o32, inv32 = lo.astype(F32), (cells / ext).astype(F32)
-        c_cells = (C.c_int32 * 3)(*[int(v) for v in cells])
-        c_origin = (C.c_float * 3)(*[float(v) for v in o32])
-        c_inv = (C.c_float * 3)(*[float(v) for v in inv32])
-        start = torch.empty(int(np.prod(cells)) + 1, dtype=torch.int32, device="cuda")
-        total = C.c_int64(0)
-        lib = L.load()
-        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-        L.check(lib.jt_nearest_candidates(C.byref(q), c_cells, c_origin, c_inv, C.c_void_p(start.data_ptr()), None,
-                                          C.byref(total), stream))
-        recs = torch.empty((max(int(total.value), 1), 4), dtype=torch.float32, device="cuda")
-        L.check(lib.jt_nearest_candidates(C.byref(q), c_cells, c_origin, c_inv, C.c_void_p(start.data_ptr()),
-                                          C.c_void_p(recs.data_ptr()), C.byref(total), stream))
-        self._dev["cand_start"], self._dev["cand_recs"] = start, recs
-        q.cand_cells[:] = [int(v) for v in cells]
-        q.cand_origin[:] = [float(v) for v in o32]
-        q.cand_inv_cell[:] = [float(v) for v in inv32]
-        q.cand_start, q.cand_recs = start.data_ptr(), recs.data_ptr()
 
     def _device_pairs(self):
         self._device()
@@ -902,9 +864,9 @@ class FEMTimeSeriesField(TimeSeriesField):
     def __init__(self, data, times, positions, connectivity, interpolation: str = "linear",
                  extrapolation: str = "constant", _source_info: Optional[dict] = None,
                  fem_grid_resolution: int = 32, *, storage: str = "f32", sub_div: Optional[int] = None,
-                 grid_build: str = "auto", nearest_candidates: bool = True):
+                 grid_build: str = "auto"):
         super().__init__(data, times, positions, interpolation, extrapolation, _source_info, storage=storage,
-                         time_semantics="jax", nearest_candidates=nearest_candidates)
+                         time_semantics="jax")
         self.fem_mesh = FemHashGrid(self.positions, connectivity, fem_grid_resolution, sub_div=sub_div,
                                     build=grid_build)
 

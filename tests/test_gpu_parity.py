@@ -81,39 +81,6 @@ def test_nearest_node_search_matches_brute_force_argmin_with_ties():
     assert np.array_equal(out, ref)
 
 
-def test_nearest_candidate_lists_give_the_ring_search_result():
-    """Candidate lists (the default for node sets spread on every axis) and
-    the ring search alone pick the same node for queries at random, on and
-    one ulp off the candidate cells' faces, on nodes (exact duplicates make
-    ties) and outside the grid."""
-    rng = np.random.default_rng(21)
-    g = np.arange(15) / 14
-    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
-    nodes = np.concatenate([lat + rng.uniform(-0.014, 0.014, lat.shape), lat[::5]]).astype(F32)
-    n = len(nodes)
-    data = np.zeros((2, n, 3), dtype=F32)
-    data[:, :, 0] = np.arange(n, dtype=F32)
-    t = np.array([0.0, 1.0], dtype=F32)
-    with_lists = jt.TimeSeriesField(data, t, nodes)
-    ring = jt.TimeSeriesField(data, t, nodes, nearest_candidates=False)
-    q = [rng.uniform(nodes.min(0), nodes.max(0), (20000, 3)), nodes, rng.uniform(-1, 2, (2000, 3))]
-    with_lists.sample_at_positions(nodes[:4], 0.0)
-    ring.sample_at_positions(nodes[:4], 0.0)
-    cn = with_lists._cnear
-    assert with_lists._dev.get("cand_start") is not None and ring._dev.get("cand_start") is None
-    o = np.array(cn.cand_origin[:], F32)
-    e = (F32(1) / np.array(cn.cand_inv_cell[:], F32)).astype(F32)
-    for a in range(3):
-        f = rng.uniform(0, 1, (3000, 3)) * np.array(cn.cand_cells[:])
-        f[:, a] = np.floor(f[:, a])
-        face = (o + f * e).astype(F32)
-        q += [face, np.nextafter(face, F32(-np.inf)), np.nextafter(face, F32(np.inf))]
-    q = np.concatenate([np.asarray(x, F32) for x in q])
-    a = with_lists.sample_at_positions(q, 0.0)[:, 0]
-    b = ring.sample_at_positions(q, 0.0)[:, 0]
-    assert np.array_equal(a, b)
-
-
 # ---------------------------------------------------------------- boundaries
 def _bc(name, B):
     conc = {"x": 9, "y": 17, "z": 5}

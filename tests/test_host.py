@@ -27,7 +27,7 @@ def test_library_exports_every_header_symbol():
     assert len(names) >= 8
     for n in names:
         assert hasattr(lib, n), n
-    assert lib.jt_abi_version() == L.ABI_VERSION == 6
+    assert lib.jt_abi_version() == L.ABI_VERSION == 5
     # the scratch allocator hook: both functions or neither
     with pytest.raises(ValueError, match="alloc and free"):
         L.check(lib.jt_set_allocator(L.ALLOC_FN(lambda n, s, c: None), L.FREE_FN(), None))
@@ -275,29 +275,3 @@ def test_tensor_positions_are_shaped_as_arrays_are():
     for bad, msg in ((np.zeros((4, 4)), "2 or 3 columns"), (np.zeros((2, 2, 3)), "2D array")):
         with pytest.raises(ValueError, match=msg):
             ensure_positions_tensor(torch.from_numpy(bad))
-
-
-def test_nearest_candidate_build_checks_its_arguments():
-    """jt_nearest_candidates refuses a missing or flat node cell list and a
-    bad candidate grid before touching the device."""
-    lib = L.load()
-    q = L.NearestField()
-    cells = (C.c_int32 * 3)(4, 4, 4)
-    origin = (C.c_float * 3)(0.0, 0.0, 0.0)
-    inv = (C.c_float * 3)(4.0, 4.0, 4.0)
-    total = C.c_int64(0)
-    start = C.c_void_p(256)               # never dereferenced: rejected first
-    with pytest.raises(ValueError, match="cell list"):
-        L.check(lib.jt_nearest_candidates(C.byref(q), cells, origin, inv, start, None, C.byref(total), None))
-    q.n_points, q.points, q.point_ids, q.cell_start = 10, 256, 256, 256
-    q.cells[:] = [2, 2, 1]
-    q.inv_cell[:] = [2.0, 2.0, 0.0]       # nodes flat in z
-    with pytest.raises(NotImplementedError, match="every axis"):
-        L.check(lib.jt_nearest_candidates(C.byref(q), cells, origin, inv, start, None, C.byref(total), None))
-    q.cells[:] = [2, 2, 2]
-    q.inv_cell[:] = [2.0, 2.0, 2.0]
-    for bad_cells, bad_inv in (((0, 4, 4), (4.0, 4.0, 4.0)), ((4, 4, 4), (4.0, 0.0, 4.0)),
-                               ((1 << 10, 1 << 10, 1 << 10), (4.0, 4.0, 4.0))):
-        with pytest.raises(ValueError, match="candidate"):
-            L.check(lib.jt_nearest_candidates(C.byref(q), (C.c_int32 * 3)(*bad_cells), origin,
-                                              (C.c_float * 3)(*bad_inv), start, None, C.byref(total), None))
