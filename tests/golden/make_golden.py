@@ -390,6 +390,40 @@ def phase_steps(ref: str):
     np.savez_compressed(HERE / "steps.npz", **out)
 
 
+
+def phase_seeding(ref: str):
+    """The NumPy branch of random_seeds and uniform_grid_seeds
+    (tracking/seeding.py:140-247) over every accepted bounds form, with and
+    without the boundaries, 3- and 2-tuple resolutions; a refusal is kept as
+    its error type and message."""
+    sys.path.insert(0, ref)
+    import warnings
+    warnings.simplefilter("ignore")
+    from jaxtrace.tracking.seeding import random_seeds, uniform_grid_seeds
+    from jaxtrace.utils.jax_utils import JAX_AVAILABLE
+    assert not JAX_AVAILABLE, "phase seeding must run without jax"
+    forms = {"b23": [[-1.0, 0.5, 2.0], [3.0, 1.5, 2.25]], "b6": [0.0, 2.0, -1.0, 1.0, 0.1, 0.3],
+             "b32": [[0.0, 1.0], [0.0, 2.0], [0.0, 3.0]], "b4": [0.0, 1.0, -2.0, 2.0], "b22": [[0.0, 1.0], [2.0, 3.0]],
+             "bad": [[1.0, 0.0, 0.0], [0.0, 1.0, 1.0]]}
+    calls = {"rand": lambda b: random_seeds(1000, b, rng_seed=7),
+             "rand0": lambda b: random_seeds(0, b),
+             "grid": lambda b: uniform_grid_seeds((5, 4, 3), b, True),
+             "grid_int": lambda b: uniform_grid_seeds(4, b, False),
+             "grid2": lambda b: uniform_grid_seeds((6, 5), b, True),
+             "grid2_int": lambda b: uniform_grid_seeds((6, 5), b, False)}
+    out, errors = {}, {}
+    for fname, b in forms.items():
+        for cname, fn in calls.items():
+            key = f"{cname}_{fname}"
+            try:
+                out[key] = np.asarray(fn(b))
+            except Exception as e:  # noqa: BLE001 -- the reference's refusal is the fixture
+                errors[key] = {"type": type(e).__name__, "message": str(e).split("\n")[0]}
+    out["forms"] = np.array(json.dumps(forms))
+    out["errors"] = np.array(json.dumps(errors))
+    np.savez_compressed(HERE / "seeding.npz", **out)
+    print(f"phase seeding: {len(out) - 2} arrays, {len(errors)} refusals")
+
 def _vtk_scenarios():
     """The time-series directories of phase vtk: per scenario its files
     (name, points, point-data arrays, pieces of a .pvtu) and the reader's
@@ -516,7 +550,7 @@ def phase_vtk(ref: str):
 
 
 PHASES = {"numpy": phase_numpy, "octree": phase_octree, "fem": phase_fem, "analytics": phase_analytics,
-          "steps": phase_steps, "vtk": phase_vtk}
+          "steps": phase_steps, "vtk": phase_vtk, "seeding": phase_seeding}
 
 if __name__ == "__main__":
     if len(sys.argv) >= 3 and sys.argv[1] in PHASES:
